@@ -1,0 +1,305 @@
+"""Benchmark: Mcell-updates/s per RK stage of the explicit Navier-Stokes step.
+
+Workload (default): the tetrahedral scaling case - a periodic [0,2pi]^3 box
+of 64^3 hexes each split into 6 tets (1,572,864 cells, 3,145,728 faces),
+Rusanov flux, Green-Gauss gradients + Barth-Jespersen, Re=1600, Pr=0.71,
+Taylor-Green vortex at Mach 0.8, Williamson RK3, CFL 0.5, the whole step
+replayed as a CUDA graph.  Synthetic mesh and initial state (no dataset).
+
+value  = cells * stages * steps / device time  (state resident in HBM)
+e2e    = the same metric through the public C ABI with host buffers: every
+         step uploads the conserved state from pinned host memory, runs one
+         step and reads the state back
+roofline: the dominant kernel's algorithmic bytes (fixed byte model, see
+         the design doc) / its average CUDA-event duration, against the measured
+         HBM copy bandwidth
+cpu_baseline: the FP64 CPU oracle on the host cores, bounded sample
+
+--impl reference times the CPU implementation of the path (the reference's
+own sources when they were built here, else the C restatement) on the host
+cores, as independent single-threaded replicas (the reference has no
+threading), and prints the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+STAGES = {"euler": 1, "rk33": 3, "rk45": 5, "ssprk3": 3}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--case", default="tgv_tet", choices=["tgv_tet", "tgv_hex", "euler16"])
+    p.add_argument("--n", type=int, default=64)
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    p.add_argument("--e2e-steps", type=int, default=20)
+    p.add_argument("--cpu-sample-stages", type=int, default=3)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def make_case(args):
+    from fv3d_gb300 import cases
+    if args.case == "tgv_tet":
+        return cases.tgv_tet(args.n)
+    if args.case == "tgv_hex":
+        return cases.tgv_hex(args.n)
+    return cases.euler16(args.n)
+
+
+# ---------------------------------------------------------------------------
+# algorithmic byte model (per kernel launch): reads of every array a pass
+# semantically needs once, writes once; neighbour re-reads, padding and
+# face-flux buffers not counted
+# ---------------------------------------------------------------------------
+def byte_model(case, precision):
+    nc, nf = case.mesh.n_cells, case.mesh.n_faces
+    r = 4 if precision == "mixed" else 8
+    ng, nr = 9, 8                      # gradient / limited variables
+    lsq = case.params.get("gradient", 0) == 1
+    state, kreg, vol = 40, 80, 8       # U (FP64), RK register r+w (FP64), 1/V
+    grad, mm = 3 * ng * r, 2 * nr * r
+    face_ids = 8
+    geo_grad = (6 * r) if lsq else (3 * r + r)   # LSQ weights | n*A + lambda
+    geo_flux = 3 * r + 3 * r + 3 * r            # n*A, r1, r2
+    k1 = nc * (state + vol + grad + mm) + nf * (face_ids + geo_grad)
+    k2 = nc * (grad + mm) + nf * (face_ids + geo_flux)
+    k3 = nc * (state + state + kreg + vol)
+    return {"gradients": k1, "face_flux": k2, "gather_update": k3, "stage": k1 + k2 + k3}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = threading.Thread(target=self._run, daemon=True)
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                      "--format=csv,noheader,nounits"], capture_output=True,
+                                     text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t.start()
+        return self
+
+    def __exit__(self, *exc):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 3 + i and s[3 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# CPU leg (oracle): bounded sample of residual evaluations + stage updates
+# ---------------------------------------------------------------------------
+def cpu_sample(case_args, n_stages, which):
+    from oracle import oracle as orc
+    from fv3d_gb300 import cases
+    c = {"tgv_tet": cases.tgv_tet, "tgv_hex": cases.tgv_hex, "euler16": cases.euler16}[case_args[0]](case_args[1])
+    o = orc.Oracle(which)
+    o.init(c.mesh, c.params, c.region_type, c.region_prim)
+    o.set_conserved(c.u0)
+    dt = o.timestep_convective(0.5)
+    t0 = time.perf_counter()
+    o.step_lserkw2(0, 0, 0.0, dt)           # warm-up stage (forward Euler = 1 stage)
+    t1 = time.perf_counter()
+    for k in range(n_stages):
+        o.step_lserkw2(0, k, 0.0, dt)
+    t2 = time.perf_counter()
+    return c.mesh.n_cells * n_stages / (t2 - t1) / 1e6, t2 - t1, t1 - t0
+
+
+def cpu_baseline(args, replicas=1):
+    from oracle import oracle as orc
+    which = "reference" if orc.available("reference") else "restated"
+    if which == "restated" and not orc.available("restated"):
+        orc.build("restated")
+    case_args = (args.case, args.n)
+    if replicas == 1:
+        v, secs, _ = cpu_sample(case_args, args.cpu_sample_stages, which)
+        vals = [v]
+    else:
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(replicas) as pool:
+            res = pool.starmap(cpu_sample, [(case_args, args.cpu_sample_stages, which)] * replicas)
+        vals = [r[0] for r in res]
+        secs = max(r[1] for r in res)
+    kind = "reference" if which == "reference" else "port"
+    return {"value": float(sum(vals)), "unit": "Mcell-updates/s per RK stage", "cores": replicas,
+            "kind": kind,
+            "sample": f"{args.cpu_sample_stages} explicit stages (FP64 residual + update) on the full "
+                      f"{args.case} n={args.n} mesh after 1 warm-up stage, {replicas} single-threaded "
+                      f"replica(s), {secs:.1f} s"}
+
+
+def workload_config(args, case):
+    return {"workload": f"{args.case}_{args.n}: {case.mesh.n_cells} cells, {case.mesh.n_faces} faces, "
+                        f"{'Rusanov' if case.params['flux_scheme'] == 1 else 'AUSM'}, "
+                        f"{'LSQ' if case.params.get('gradient', 0) else 'Green-Gauss'}+Barth-Jespersen, "
+                        f"viscous Re=1600, TGV, RK3 CFL 0.5, CUDA graph per step",
+            "cells": case.mesh.n_cells, "faces": case.mesh.n_faces, "precision": args.precision,
+            "l2": "working set > 129 MB L2 (records + fluxes + state ~1.3 GB); no flush needed",
+            "parallelism": "replicas only (1 GPU per process, no collectives)"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from fv3d_gb300 import cases  # noqa: F401
+    case = make_case(args)
+    replicas = max(1, min(len(os.sched_getaffinity(0)), 16))
+    cb = cpu_baseline(args, replicas)
+    metric = "Mcell-updates/s per RK stage"
+    line = {"impl": "reference", "metric": metric, "value": cb["value"], "unit": metric,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": workload_config(args, case), "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": metric, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # barrier + max over ranks only
+        dist.init_process_group("gloo")
+    from fv3d_gb300 import api
+    case = make_case(args)
+    scheme = "rk33"
+    nst = STAGES[scheme]
+    s = api.Solver(case.mesh, case.params, case.region_type, case.region_prim, args.precision,
+                   "morton", device=local)
+    s.set_state(case.u0)
+    # warm-up (includes graph capture)
+    s.step_explicit(scheme, max(3, args.warmup), cfl=0.5)
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        st = s.step_explicit(scheme, args.steps, cfl=0.5)   # CUDA events around the graph replays
+    ms = st["elapsed_ms"]
+    if dist:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    n_stages = args.steps * nst
+    value = case.mesh.n_cells * n_stages / (ms * 1e-3) / 1e6 * world
+    # per-kernel durations (CUDA events around each launch on the context stream)
+    kms = s.profile_stage(20, 0.5)
+    model = byte_model(case, args.precision)
+    names = ["gradients", "face_flux", "gather_update"]
+    dom = int(np.argmax(kms))
+    peak, peak_kind = measured_peaks()
+    achieved = model[names[dom]] / (kms[dom] * 1e-3) / 1e9
+    stage_ms = ms / n_stages
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            traffic = json.load(f).get(f"{args.case}_{args.n}_{args.precision}", {}).get(names[dom])
+    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": round(achieved, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
+                "peak_kind": peak_kind,
+                "algorithmic_bytes": model[names[dom]],
+                "kernel_ms": {n: round(float(k), 5) for n, k in zip(names, kms)},
+                "stage_frac": round(model["stage"] / (stage_ms * 1e-3) / 1e9 / peak, 4),
+                "stage_bytes": model["stage"]}
+    # end to end through the public API with pinned host buffers
+    e2e = None
+    try:
+        import torch
+        hb = torch.empty((case.mesh.n_cells, 5), dtype=torch.float64, pin_memory=True).numpy()
+    except Exception:
+        hb = np.empty((case.mesh.n_cells, 5))
+    hb[:] = s.get_conserved()
+    import ctypes
+    s.lib.fv3d_get_stream(s.h, ctypes.byref(ctypes.c_void_p()))
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        s.set_state(hb)
+        s.step_explicit(scheme, 1, cfl=0.5)
+        hb[:] = s.get_conserved()           # synchronises
+    t1 = time.perf_counter()
+    e2e = {"value": case.mesh.n_cells * nst * args.e2e_steps / (t1 - t0) / 1e6,
+           "unit": "Mcell-updates/s per RK stage", "h2d_bytes_per_step": int(hb.nbytes),
+           "d2h_bytes_per_step": int(hb.nbytes), "steps": args.e2e_steps,
+           "note": "wall clock around set_state (pinned H2D) + 1 graph step + get_conserved (D2H)"}
+    s.close()
+    if rank != 0:
+        return
+    cb = None
+    if not args.no_cpu_baseline and world == 1:
+        cb = cpu_baseline(args, 1)
+    line = {"metric": "Mcell-updates/s per RK stage", "value": round(value, 2),
+            "unit": "Mcell-updates/s per RK stage", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
+            "config": workload_config(args, case), "roofline": roofline, "cpu_baseline": cb,
+            "e2e": e2e, "gpu_launches": args.steps * (3 * nst + 1), "clocks": clk.summary()}
+    print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,215 @@
+"""Python host interface over the C ABI of libfv3d_gb300.so (include/fv3d_gpu.h).
+
+Mirrors the reference solver's entry points for the hot path:
+``Solver(...)`` ~ init_mesh + navier_stokes_initialize + boundary_initialize
++ init_reconstruction/init_limiter; ``time_derivative`` ~
+finite_volume_time_derivative; ``step_explicit`` ~ timestep_lserkw2 driven by
+timedisc; ``timestep`` ~ calc_ns_timestep; ``global_residual`` ~
+calc_global_residual.  Errors raise ``FV3DError`` carrying the status code
+(the reference aborts instead).
+
+There is no CPU fallback: without the compiled CUDA library (or without a GPU)
+every call fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfv3d_gb300.so")
+
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "UNSUPPORTED", 3: "NONFINITE", 4: "NOT_CONVERGED",
+          5: "STAGNATED_FALLBACK", 6: "DEVICE", 7: "TIMEOUT", 8: "BOUNDS", 9: "STATE"}
+SCHEMES = {"euler": 0, "rk33": 1, "rk45": 2, "ssprk3": 3}
+PRECISION = {"fp64": 0, "mixed": 1}
+RENUMBER = {"none": 0, "morton": 1, "rcm": 2}
+
+
+class FV3DError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+_f8p = C.POINTER(C.c_double)
+_i4p = C.POINTER(C.c_int)
+
+
+class Config(C.Structure):
+    _fields_ = [("kappa", C.c_double), ("R_mix", C.c_double), ("mu_mix", C.c_double),
+                ("Pr", C.c_double), ("cfl_scale", C.c_double), ("dfl_scale", C.c_double),
+                ("flux_scheme", C.c_int), ("reconstruction", C.c_int), ("limiter", C.c_int),
+                ("gradient", C.c_int), ("precision", C.c_int), ("renumber", C.c_int),
+                ("device", C.c_int)]
+
+
+class MeshArrays(C.Structure):
+    _fields_ = [("n_cells", C.c_int), ("n_faces", C.c_int), ("n_boundaries", C.c_int),
+                ("max_cell_faces", C.c_int), ("n_regions", C.c_int),
+                ("cell_x", _f8p), ("cell_volume", _f8p), ("cell_dx", _f8p),
+                ("cell_n_faces", _i4p), ("cell_faces", _i4p), ("face_cells", _i4p),
+                ("face_boundary", _i4p), ("face_area", _f8p), ("face_lambda", _f8p),
+                ("face_x", _f8p), ("face_n", _f8p), ("face_t1", _f8p), ("face_t2", _f8p),
+                ("face_dist_cell_2", _f8p), ("boundary_id", _i4p), ("boundary_face", _i4p),
+                ("region_is_boundary", _i4p)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("t", C.c_double), ("dt", C.c_double), ("steps", C.c_int),
+                ("elapsed_ms", C.c_double)]
+
+
+EXPORTS = {
+    "fv3d_create": ([C.POINTER(Config), C.POINTER(C.c_void_p)], C.c_int),
+    "fv3d_destroy": ([C.c_void_p], C.c_int),
+    "fv3d_last_error": ([C.c_void_p], C.c_char_p),
+    "fv3d_version": ([], C.c_char_p),
+    "fv3d_mesh_from_arrays": ([C.c_void_p, C.POINTER(MeshArrays)], C.c_int),
+    "fv3d_mesh_load_h5": ([C.c_void_p, C.c_char_p], C.c_int),
+    "fv3d_get_permutation": ([C.c_void_p, _i4p], C.c_int),
+    "fv3d_set_region": ([C.c_void_p, C.c_int, C.c_int, _f8p], C.c_int),
+    "fv3d_set_state": ([C.c_void_p, _f8p], C.c_int),
+    "fv3d_get_state": ([C.c_void_p, _f8p], C.c_int),
+    "fv3d_get_conserved": ([C.c_void_p, _f8p], C.c_int),
+    "fv3d_time_derivative": ([C.c_void_p, C.c_double, _f8p], C.c_int),
+    "fv3d_timestep": ([C.c_void_p, C.c_double, _f8p], C.c_int),
+    "fv3d_step_explicit": ([C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double,
+                            C.POINTER(StepStats)], C.c_int),
+    "fv3d_global_residual": ([C.c_void_p, C.c_double, _f8p], C.c_int),
+    "fv3d_profile_stage": ([C.c_void_p, C.c_int, C.c_double, _f8p], C.c_int),
+    "fv3d_get_stream": ([C.c_void_p, C.POINTER(C.c_void_p)], C.c_int),
+    "fv3d_device_state": ([C.c_void_p, C.POINTER(_f8p)], C.c_int),
+}
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load (once) the compiled CUDA library; raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FV3DError(6, f"CUDA library {path} not built (run __graft_entry__.build())")
+    lib = C.CDLL(path)
+    for name, (args, res) in EXPORTS.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = lib
+    return lib
+
+
+def _p(a, t):
+    return a.ctypes.data_as(t)
+
+
+class Solver:
+    """One GPU solver context for a mesh (FV3D's global solver state, per handle)."""
+
+    def __init__(self, mesh, params: dict, region_type, region_prim, precision: str = "fp64",
+                 renumber: str = "morton", device: int = 0):
+        self.lib = load_library()
+        self.h = C.c_void_p()
+        cfg = Config(params["kappa"], params["R_mix"], params["mu_mix"], params["Pr"],
+                     params.get("cfl_scale", 1.0), params.get("dfl_scale", 1.0),
+                     params["flux_scheme"], params["reconstruction"], params["limiter"],
+                     params.get("gradient", 0), PRECISION[precision], RENUMBER[renumber], device)
+        st = self.lib.fv3d_create(C.byref(cfg), C.byref(self.h))
+        if st != 0:
+            raise FV3DError(st, "fv3d_create failed (no CUDA device or bad configuration)")
+        self.nc = mesh.n_cells
+        self.precision = precision
+        a = mesh.arrays()
+        m = MeshArrays(mesh.n_cells, mesh.n_faces, mesh.n_boundaries, mesh.max_cell_faces,
+                       mesh.n_regions)
+        for k, v in a.items():
+            setattr(m, k, _p(v, _i4p if v.dtype == np.int32 else _f8p))
+        self._check(self.lib.fv3d_mesh_from_arrays(self.h, C.byref(m)))
+        for r, (t, prim) in enumerate(zip(region_type, np.asarray(region_prim, dtype=np.float64))):
+            pr = np.ascontiguousarray(prim, dtype=np.float64)
+            self._check(self.lib.fv3d_set_region(self.h, r, int(t), _p(pr, _f8p)))
+
+    def _check(self, st):
+        if st != 0:
+            raise FV3DError(st, self.lib.fv3d_last_error(self.h).decode())
+
+    def close(self):
+        if self.h:
+            self.lib.fv3d_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- state ----
+    def set_state(self, u):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        if u.shape != (self.nc, 5):
+            raise ValueError(f"state must have shape ({self.nc}, 5)")
+        self._check(self.lib.fv3d_set_state(self.h, _p(u, _f8p)))
+
+    def get_state(self):
+        out = np.empty((self.nc, 10))
+        self._check(self.lib.fv3d_get_state(self.h, _p(out, _f8p)))
+        return out
+
+    def get_conserved(self):
+        out = np.empty((self.nc, 5))
+        self._check(self.lib.fv3d_get_conserved(self.h, _p(out, _f8p)))
+        return out
+
+    def permutation(self):
+        out = np.empty(self.nc, dtype=np.int32)
+        self._check(self.lib.fv3d_get_permutation(self.h, _p(out, _i4p)))
+        return out
+
+    # ---- hot path ----
+    def time_derivative(self, t: float = 0.0):
+        out = np.empty((self.nc, 5))
+        self._check(self.lib.fv3d_time_derivative(self.h, t, _p(out, _f8p)))
+        return out
+
+    def timestep(self, cfl: float) -> float:
+        dt = C.c_double()
+        self._check(self.lib.fv3d_timestep(self.h, cfl, C.byref(dt)))
+        return dt.value
+
+    def step_explicit(self, scheme: str, n_steps: int, cfl: float = 0.0, dt_fixed: float = 0.0):
+        st = StepStats()
+        self._check(self.lib.fv3d_step_explicit(self.h, SCHEMES[scheme], n_steps, cfl, dt_fixed,
+                                                C.byref(st)))
+        return {"t": st.t, "dt": st.dt, "steps": st.steps, "elapsed_ms": st.elapsed_ms}
+
+    def global_residual(self, dt: float):
+        out = np.empty(5)
+        self._check(self.lib.fv3d_global_residual(self.h, dt, _p(out, _f8p)))
+        return out
+
+    def profile_stage(self, n_reps: int = 10, cfl: float = 0.5):
+        out = np.empty(3)
+        self._check(self.lib.fv3d_profile_stage(self.h, n_reps, cfl, _p(out, _f8p)))
+        return out
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._check(self.lib.fv3d_get_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+
+def from_case(case, precision="fp64", renumber="morton", device=0) -> Solver:
+    s = Solver(case.mesh, case.params, case.region_type, case.region_prim, precision, renumber, device)
+    s.set_state(case.u0)
+    return s

@@ -1,0 +1,631 @@
+// C ABI implementation (include/fv3d_gpu.h): context, mesh preparation
+// (metrics, validation, renumbering, structure-of-arrays upload), state
+// import/export, the residual entry point and the graph-captured explicit
+// step loop.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/fv3d_gpu.h"
+#include "launch.h"
+#include "context.h"
+
+using namespace fv3d;
+
+// ---------------------------------------------------------------------------
+// small device kernels owned by the host layer
+// ---------------------------------------------------------------------------
+namespace {
+
+// reference AoS [n][5] (reference order) -> SoA [5][n] (renumbered) + FP32 shadow
+__global__ void k_import(int nc, const int* __restrict__ perm, const double* __restrict__ in,
+                         double* __restrict__ U, float* __restrict__ Uf, double km1, double R) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const double* s = in + 5 * (size_t)perm[c];
+  double u[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) { u[j] = s[j]; U[(size_t)j * nc + c] = u[j]; }
+  if (Uf != nullptr) {
+    float rho = (float)u[0], mx = (float)u[1], my = (float)u[2], mz = (float)u[3];
+    float ke = 0.5f * (mx * (mx / rho) + my * (my / rho) + mz * (mz / rho));
+    float p = fmaxf(1.00E-10f, (float)(km1 * (u[4] - (double)ke)));
+    float T = p / (rho * (float)R);
+    float4* d = reinterpret_cast<float4*>(Uf) + 2 * (size_t)c;
+    d[0] = make_float4(rho, mx, my, mz);
+    d[1] = make_float4((float)u[4], p, T, 0.f);
+  }
+}
+
+// SoA [m][n] (renumbered) -> reference AoS [n][m]; with prims: [n][10]
+__global__ void k_export(int nc, int m, const int* __restrict__ perm, const double* __restrict__ S,
+                         double* __restrict__ out, int with_prims, double km1, double R) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  double q[10];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) q[j] = (j < m) ? S[(size_t)j * nc + c] : 0.0;
+  const int w = with_prims ? 10 : m;
+  double* d = out + (size_t)w * perm[c];
+  if (with_prims) {
+    // eos.c:81-92 in FP64
+    q[5] = q[1] / q[0];
+    q[6] = q[2] / q[0];
+    q[7] = q[3] / q[0];
+    double ke = q[1] * q[5];
+    ke += q[2] * q[6];
+    ke += q[3] * q[7];
+    q[8] = km1 * (q[4] - 0.5 * ke);
+    q[8] = (1.00E-10 > q[8]) ? 1.00E-10 : q[8];
+    q[9] = q[8] / (q[0] * R);
+  }
+  for (int j = 0; j < w; ++j) d[j] = q[j];
+}
+
+// calc_ns_timestep (navier_stokes.c:159-193) reduced over cells: min of the
+// convective and viscous bounds (exact, order independent)
+__global__ void k_timestep(int nc, const double* __restrict__ U, const double* __restrict__ vol,
+                           const double* __restrict__ dx, double kappa, double km1,
+                           unsigned long long* conv_bits, unsigned long long* visc_bits) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long bc = 0x7ff0000000000000ull, bv = 0x7ff0000000000000ull;
+  if (c < nc) {
+    double q[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) q[j] = U[(size_t)j * nc + c];
+    double u = q[1] / q[0], v = q[2] / q[0], w = q[3] / q[0];
+    double ke = q[1] * u;
+    ke += q[2] * v;
+    ke += q[3] * w;
+    double p = km1 * (q[4] - 0.5 * ke);
+    p = (1.00E-10 > p) ? 1.00E-10 : p;
+    double s_rho = 1.0 / q[0];
+    double cs = sqrt(kappa * p * s_rho);
+    const double* d = dx + 3 * (size_t)c;
+    double ds1 = (fabs(u) + cs) * d[0] + (fabs(v) + cs) * d[1] + (fabs(w) + cs) * d[2];
+    double lc = vol[c] / ds1;
+    double ds2 = d[0] * d[0];
+    ds2 += d[1] * d[1];
+    ds2 += d[2] * d[2];
+    double lv = s_rho * ds2 / vol[c];
+    if (lc > 0.0) bc = (unsigned long long)__double_as_longlong(lc);
+    if (lv > 0.0) bv = (unsigned long long)__double_as_longlong(lv);
+    if (!(lc == lc) || !(lv == lv)) { bc = 0x7ff8000000000000ull; }
+  }
+  bc = warp_min_u64(bc);
+  bv = warp_min_u64(bv);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMin(conv_bits, bc);
+    atomicMin(visc_bits, bv);
+  }
+}
+
+// end of an explicit step: advance time, next dt = cfl * min lambda
+__global__ void k_finish_step(DevScalars* sc, double cfl) {
+  sc->t += sc->dt;
+  sc->step += 1;
+  if (cfl > 0.0) {
+    double lam = __longlong_as_double((long long)sc->lam_bits);
+    sc->dt = lam * cfl;
+    sc->lam_bits = 0x7ff0000000000000ull;
+    if (!(sc->dt > 0.0) || isinf(sc->dt)) sc->status |= 1;
+  }
+}
+
+__global__ void k_set_dt(DevScalars* sc, const unsigned long long* lam_bits, double cfl, double dt_fixed) {
+  if (cfl > 0.0) sc->dt = __longlong_as_double((long long)lam_bits[0]) * cfl;
+  else sc->dt = dt_fixed;
+  sc->lam_bits = 0x7ff0000000000000ull;
+  if (!(sc->dt > 0.0) || isinf(sc->dt)) sc->status |= 1;
+}
+
+// calc_global_residual (analyze.c:37-61): per-block partial sums, then one
+// block sums the partials in a fixed order (deterministic)
+__global__ void k_residual_partial(int nc, const double* __restrict__ dphi,
+                                   const double* __restrict__ vol, double* __restrict__ part) {
+  __shared__ double sh[5][256];
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+#pragma unroll
+  for (int j = 0; j < 5; ++j) sh[j][threadIdx.x] = (c < nc) ? fabs(dphi[(size_t)j * nc + c]) * vol[c] : 0.0;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+#pragma unroll
+      for (int j = 0; j < 5; ++j) sh[j][threadIdx.x] += sh[j][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int j = 0; j < 5; ++j) part[(size_t)blockIdx.x * 5 + j] = sh[j][0];
+}
+
+__global__ void k_residual_final(int nb, const double* __restrict__ part, double scale, double* out) {
+  __shared__ double sh[5][256];
+  double acc[5] = {0, 0, 0, 0, 0};
+  for (int b = threadIdx.x; b < nb; b += blockDim.x)
+#pragma unroll
+    for (int j = 0; j < 5; ++j) acc[j] += part[(size_t)b * 5 + j];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) sh[j][threadIdx.x] = acc[j];
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+#pragma unroll
+      for (int j = 0; j < 5; ++j) sh[j][threadIdx.x] += sh[j][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int j = 0; j < 5; ++j) out[j] = sh[j][0] * scale;
+}
+
+int nblk(int n, int t = 256) { return (n + t - 1) / t; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// context helpers
+// ---------------------------------------------------------------------------
+namespace fv3d {
+fv3d_status Ctx::fail(fv3d_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  err = buf;
+  return st;
+}
+
+fv3d_status Ctx::cuda(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return FV3D_OK;
+  return fail(FV3D_ERR_DEVICE, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(expr)                                              \
+  do {                                                        \
+    fv3d_status st__ = ctx->cuda((expr), #expr);              \
+    if (st__ != FV3D_OK) return st__;                         \
+  } while (0)
+
+#define REQUIRE(cond, st, ...)                                \
+  do {                                                        \
+    if (!(cond)) return ctx->fail((st), __VA_ARGS__);         \
+  } while (0)
+
+void Ctx::release_graphs() {
+  for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+  graphs.clear();
+}
+
+template <class R>
+KArgs<R> Ctx::args() const {
+  KArgs<R> a;
+  memset(&a, 0, sizeof(a));
+  a.nc = nc; a.nf = nf; a.nf_int = nf_int; a.mcf = mcf;
+  a.fc0 = d_fc0.p; a.fc1 = d_fc1.p;
+  a.geo = (const R*)d_geo.p; a.lam = (const R*)d_lam.p; a.lsq = (const R*)d_lsq.p;
+  a.fregion = d_fregion.p; a.cface = d_cface.p; a.rvol = (const R*)d_rvol.p;
+  a.vol = d_vol.p; a.dx = d_dx.p;
+  a.U = d_U.p; a.K = d_K.p; a.U0 = d_U0.p; a.Uf = d_Uf.p;
+  a.rec = (R*)d_rec.p; a.FA = (R*)d_FA.p; a.dphi = d_dphi.p; a.sc = d_sc.p;
+  a.pc = phys;
+  return a;
+}
+
+Disc Ctx::disc() const {
+  Disc d;
+  d.linear = cfg.reconstruction == FV3D_RECON_LINEAR;
+  d.limit = cfg.limiter == FV3D_LIMITER_BARTH_JESPERSEN;
+  d.viscous = cfg.mu_mix != 0.0;
+  d.gmode = (!d.linear && !d.viscous) ? 0 : (cfg.gradient == FV3D_GRADIENT_LEAST_SQUARES ? 2 : 1);
+  return d;
+}
+
+cudaError_t Ctx::launch_stage_kernels(int mode, bool dt, const StageCoef& co, int which) {
+  cudaError_t e = cudaSuccess;
+  const Disc d = disc();
+  if (fp64()) {
+    KArgs<double> a = args<double>();
+    if (which & 1) e = launch_gradients<double>(a, d, stream);
+    if (e == cudaSuccess && (which & 2)) e = launch_face_flux<double>(a, d, stream);
+    if (e == cudaSuccess && (which & 4)) e = launch_gather<double>(a, mode, dt, co, stream);
+  } else {
+    KArgs<float> a = args<float>();
+    if (which & 1) e = launch_gradients<float>(a, d, stream);
+    if (e == cudaSuccess && (which & 2)) e = launch_face_flux<float>(a, d, stream);
+    if (e == cudaSuccess && (which & 4)) e = launch_gather<float>(a, mode, dt, co, stream);
+  }
+  return e;
+}
+}  // namespace fv3d
+
+// ---------------------------------------------------------------------------
+// lifecycle
+// ---------------------------------------------------------------------------
+extern "C" const char* fv3d_version(void) { return "fv3d_gb300 1.0 (sm_103a)"; }
+
+extern "C" fv3d_status fv3d_create(const fv3d_config* config, fv3d_ctx** out) {
+  if (config == nullptr || out == nullptr) return FV3D_ERR_INVALID_ARG;
+  *out = nullptr;
+  Ctx* ctx = new Ctx();
+  ctx->cfg = *config;
+  const fv3d_config& c = *config;
+  if (!(c.kappa > 1.0) || !(c.R_mix > 0.0) || !(c.mu_mix >= 0.0) || !(c.Pr > 0.0) ||
+      c.flux_scheme < 0 || c.flux_scheme > 1 || c.reconstruction < 0 || c.reconstruction > 1 ||
+      c.limiter < 0 || c.limiter > 1 || c.gradient < 0 || c.gradient > 1 || c.precision < 0 ||
+      c.precision > 1 || c.renumber < 0 || c.renumber > 2) {
+    delete ctx;
+    return FV3D_ERR_INVALID_ARG;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0 || c.device < 0 || c.device >= ndev) {
+    delete ctx;
+    return FV3D_ERR_DEVICE;
+  }
+  if (cudaSetDevice(c.device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+    delete ctx;
+    return FV3D_ERR_DEVICE;
+  }
+  // navier_stokes.c:85-124 derived constants
+  PhysConst& p = ctx->phys;
+  memset(&p, 0, sizeof(p));
+  p.kappa = c.kappa;
+  p.km1 = c.kappa - 1.0;
+  p.kp1 = c.kappa + 1.0;
+  p.s_km1 = 1.0 / p.km1;
+  p.s_kp1 = 1.0 / p.kp1;
+  p.R_mix = c.R_mix;
+  p.mu = c.mu_mix;
+  double cv = c.R_mix * p.s_km1;
+  double cp = c.kappa * cv;
+  p.heat_lambda = c.mu_mix * cp / c.Pr;
+  p.flux = c.flux_scheme;
+  ctx->kappa_pr = c.kappa / c.Pr;
+  *out = reinterpret_cast<fv3d_ctx*>(ctx);
+  return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_destroy(fv3d_ctx* handle) {
+  if (handle == nullptr) return FV3D_OK;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  cudaSetDevice(ctx->cfg.device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  ctx->release_graphs();
+  ctx->free_device();
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return FV3D_OK;
+}
+
+extern "C" const char* fv3d_last_error(const fv3d_ctx* handle) {
+  if (handle == nullptr) return "null context";
+  return reinterpret_cast<const Ctx*>(handle)->err.c_str();
+}
+
+extern "C" fv3d_status fv3d_get_stream(const fv3d_ctx* handle, void** stream) {
+  if (handle == nullptr || stream == nullptr) return FV3D_ERR_INVALID_ARG;
+  *stream = (void*)reinterpret_cast<const Ctx*>(handle)->stream;
+  return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_device_state(const fv3d_ctx* handle, double** u) {
+  if (handle == nullptr || u == nullptr) return FV3D_ERR_INVALID_ARG;
+  const Ctx* ctx = reinterpret_cast<const Ctx*>(handle);
+  if (!ctx->mesh_ready) return FV3D_ERR_STATE;
+  *u = ctx->d_U.p;
+  return FV3D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// mesh
+// ---------------------------------------------------------------------------
+extern "C" fv3d_status fv3d_mesh_load_h5(fv3d_ctx* handle, const char* path) {
+  if (handle == nullptr || path == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  return ctx->fail(FV3D_ERR_UNSUPPORTED,
+                   "HDF5 mesh files are not supported by this build (no HDF5 library); "
+                   "load the arrays and call fv3d_mesh_from_arrays");
+}
+
+extern "C" fv3d_status fv3d_get_permutation(const fv3d_ctx* handle, int* perm) {
+  if (handle == nullptr || perm == nullptr) return FV3D_ERR_INVALID_ARG;
+  const Ctx* ctx = reinterpret_cast<const Ctx*>(handle);
+  if (!ctx->mesh_ready) return FV3D_ERR_STATE;
+  std::copy(ctx->perm.begin(), ctx->perm.end(), perm);
+  return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_mesh_from_arrays(fv3d_ctx* handle, const fv3d_mesh_arrays* m) {
+  if (handle == nullptr || m == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  CK(cudaSetDevice(ctx->cfg.device));
+  fv3d_status st = prepare_mesh(*ctx, *m);
+  if (st != FV3D_OK) return st;
+  return upload_mesh(*ctx);
+}
+
+extern "C" fv3d_status fv3d_set_region(fv3d_ctx* handle, int region, int type, const double prim[5]) {
+  if (handle == nullptr || prim == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  REQUIRE(region >= 0 && region < MAX_REGIONS, FV3D_ERR_INVALID_ARG, "region %d out of range", region);
+  REQUIRE(type >= FV3D_BC_FLOW && type <= FV3D_BC_PRESSURE_OUTLET && type != FV3D_BC_FUNCTION,
+          FV3D_ERR_UNSUPPORTED, "boundary type %d not supported", type);
+  PhysConst& p = ctx->phys;
+  p.region_type[region] = type;
+  double* q = p.region_phi[region];
+  for (int j = 0; j < 10; ++j) q[j] = 0.0;
+  // parse_primitive_state (boundary.c:144-183) + prim_to_con (eos.c:120-127)
+  q[5] = prim[0]; q[6] = prim[1]; q[7] = prim[2]; q[8] = prim[3]; q[9] = prim[4];
+  q[0] = q[8] / (ctx->cfg.R_mix * q[9]);
+  q[1] = q[5] * q[0];
+  q[2] = q[6] * q[0];
+  q[3] = q[7] * q[0];
+  double ke = q[5] * q[1];
+  ke += q[6] * q[2];
+  ke += q[7] * q[3];
+  q[4] = p.s_km1 * q[8] + 0.5 * ke;
+  p.n_regions = std::max(p.n_regions, region + 1);
+  ctx->region_set |= 1u << region;
+  ctx->release_graphs();  // physics constants are baked into captured graphs
+  return FV3D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// state
+// ---------------------------------------------------------------------------
+static fv3d_status check_ready(Ctx* ctx) {
+  if (!ctx->mesh_ready) return ctx->fail(FV3D_ERR_STATE, "no mesh loaded");
+  for (int b = 0; b < ctx->nb; ++b) {
+    int r = ctx->h_fregion[b];
+    if (!(ctx->region_set & (1u << r)))
+      return ctx->fail(FV3D_ERR_STATE, "boundary region %d has no condition (fv3d_set_region)", r);
+  }
+  return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_set_state(fv3d_ctx* handle, const double* u) {
+  if (handle == nullptr || u == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (!ctx->mesh_ready) return ctx->fail(FV3D_ERR_STATE, "no mesh loaded");
+  CK(cudaSetDevice(ctx->cfg.device));
+  CK(cudaMemcpyAsync(ctx->d_stage.p, u, sizeof(double) * 5 * (size_t)ctx->nc, cudaMemcpyHostToDevice,
+                     ctx->stream));
+  k_import<<<nblk(ctx->nc), 256, 0, ctx->stream>>>(ctx->nc, ctx->d_perm.p, ctx->d_stage.p, ctx->d_U.p,
+                                                  ctx->fp64() ? nullptr : ctx->d_Uf.p, ctx->phys.km1,
+                                                  ctx->cfg.R_mix);
+  CK(cudaGetLastError());
+  ctx->state_ready = true;
+  return FV3D_OK;
+}
+
+static fv3d_status export_soa(Ctx* ctx, const double* src, int m, int with_prims, double* out) {
+  const int w = with_prims ? 10 : m;
+  k_export<<<nblk(ctx->nc), 256, 0, ctx->stream>>>(ctx->nc, m, ctx->d_perm.p, src, ctx->d_stage.p,
+                                                  with_prims, ctx->phys.km1, ctx->cfg.R_mix);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(out, ctx->d_stage.p, sizeof(double) * w * (size_t)ctx->nc, cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_get_state(fv3d_ctx* handle, double* phi_total) {
+  if (handle == nullptr || phi_total == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (!ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "no state set");
+  CK(cudaSetDevice(ctx->cfg.device));
+  return export_soa(ctx, ctx->d_U.p, 5, 1, phi_total);
+}
+
+extern "C" fv3d_status fv3d_get_conserved(fv3d_ctx* handle, double* u) {
+  if (handle == nullptr || u == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (!ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "no state set");
+  CK(cudaSetDevice(ctx->cfg.device));
+  return export_soa(ctx, ctx->d_U.p, 5, 0, u);
+}
+
+// ---------------------------------------------------------------------------
+// hot path
+// ---------------------------------------------------------------------------
+extern "C" fv3d_status fv3d_time_derivative(fv3d_ctx* handle, double t, double* phi_dt) {
+  (void)t;  // the implemented boundary conditions do not depend on time
+  if (handle == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  fv3d_status st = check_ready(ctx);
+  if (st != FV3D_OK) return st;
+  if (!ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "no state set");
+  CK(cudaSetDevice(ctx->cfg.device));
+  StageCoef co{0, 0, 0, 0, 1};
+  CK(ctx->launch_stage_kernels(0, false, co, 7));
+  ctx->residual_valid = true;
+  if (phi_dt != nullptr) return export_soa(ctx, ctx->d_dphi.p, 5, 0, phi_dt);
+  CK(cudaStreamSynchronize(ctx->stream));
+  return FV3D_OK;
+}
+
+static fv3d_status reduce_timestep(Ctx* ctx, bool with_visc) {
+  CK(cudaMemsetAsync(ctx->d_bits.p, 0xff, 2 * sizeof(unsigned long long), ctx->stream));
+  // 0xff.. is larger than any positive double's bits; k_timestep mins into it
+  k_timestep<<<nblk(ctx->nc), 256, 0, ctx->stream>>>(ctx->nc, ctx->d_U.p, ctx->d_vol.p, ctx->d_dx.p,
+                                                    ctx->cfg.kappa, ctx->phys.km1, ctx->d_bits.p,
+                                                    ctx->d_bits.p + 1);
+  CK(cudaGetLastError());
+  (void)with_visc;
+  return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_timestep(fv3d_ctx* handle, double cfl, double* dt) {
+  if (handle == nullptr || dt == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (!ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "no state set");
+  CK(cudaSetDevice(ctx->cfg.device));
+  fv3d_status st = reduce_timestep(ctx, cfl <= 0.0);
+  if (st != FV3D_OK) return st;
+  unsigned long long bits[2];
+  CK(cudaMemcpyAsync(bits, ctx->d_bits.p, sizeof(bits), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  double lc, lv;
+  memcpy(&lc, &bits[0], 8);
+  memcpy(&lv, &bits[1], 8);
+  if (bits[0] == ~0ull || !(lc > 0.0) || std::isinf(lc))
+    return ctx->fail(FV3D_ERR_NONFINITE, "non-finite state in time step reduction");
+  if (cfl > 0.0) {
+    *dt = lc * cfl;
+  } else {
+    // navier_stokes.c:186-192, including its viscous branch as written
+    lc *= ctx->cfg.cfl_scale;
+    lv *= ctx->cfg.dfl_scale * ctx->cfg.mu_mix * ctx->kappa_pr * lv;
+    *dt = (lc < lv) ? lc : lv;
+  }
+  return FV3D_OK;
+}
+
+// Williamson 2N low-storage tables (explicit.c:19-39): forward Euler,
+// Williamson RK3, Carpenter-Kennedy RK4(5) - published coefficients.
+static const double RK_A[3][5] = {
+    {0.0},
+    {0., -5. / 9., -153. / 128.},
+    {0., -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
+     -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0}};
+static const double RK_G[3][5] = {
+    {1.0},
+    {1. / 3., 15. / 16., 8. / 15.},
+    {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+     1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+     2277821191437.0 / 14882151754819.0}};
+static const int RK_S[3] = {1, 3, 5};
+
+static fv3d_status enqueue_step(Ctx* ctx, int scheme, double cfl) {
+  const bool dt_dev = cfl > 0.0;
+  if (scheme == FV3D_SSP_RK3) {
+    const double c0[3] = {0.0, 0.75, 1.0 / 3.0}, c1[3] = {1.0, 0.25, 2.0 / 3.0};
+    for (int s = 0; s < 3; ++s) {
+      StageCoef co{0, 0, c0[s], c1[s], s == 0};
+      CK(ctx->launch_stage_kernels(2, dt_dev && s == 2, co, 7));
+    }
+  } else {
+    for (int s = 0; s < RK_S[scheme]; ++s) {
+      StageCoef co{RK_A[scheme][s], RK_G[scheme][s], 0, 0, s == 0};
+      CK(ctx->launch_stage_kernels(1, dt_dev && s == RK_S[scheme] - 1, co, 7));
+    }
+  }
+  k_finish_step<<<1, 1, 0, ctx->stream>>>(ctx->d_sc.p, cfl);
+  CK(cudaGetLastError());
+  return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_step_explicit(fv3d_ctx* handle, int scheme, int n_steps, double cfl,
+                                          double dt_fixed, fv3d_step_stats* stats) {
+  if (handle == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  REQUIRE(scheme >= 0 && scheme <= 3, FV3D_ERR_INVALID_ARG, "bad explicit scheme %d", scheme);
+  REQUIRE(n_steps >= 0, FV3D_ERR_INVALID_ARG, "negative step count");
+  REQUIRE(cfl > 0.0 || dt_fixed > 0.0, FV3D_ERR_INVALID_ARG, "need cfl > 0 or dt_fixed > 0");
+  fv3d_status st = check_ready(ctx);
+  if (st != FV3D_OK) return st;
+  if (!ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "no state set");
+  CK(cudaSetDevice(ctx->cfg.device));
+  // initial dt from the current state (timedisc.c:163-165 at the first step)
+  CK(cudaMemsetAsync(ctx->d_sc.p, 0, sizeof(DevScalars), ctx->stream));
+  if (cfl > 0.0) {
+    st = reduce_timestep(ctx, false);
+    if (st != FV3D_OK) return st;
+  }
+  k_set_dt<<<1, 1, 0, ctx->stream>>>(ctx->d_sc.p, ctx->d_bits.p, cfl, dt_fixed);
+  CK(cudaGetLastError());
+  // one graph per (scheme, cfl) replayed n_steps times
+  const std::pair<int, double> key(scheme, cfl);
+  auto it = ctx->graphs.find(key);
+  cudaGraphExec_t exec = nullptr;
+  if (it == ctx->graphs.end()) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    fv3d_status est = enqueue_step(ctx, scheme, cfl);
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+    if (est != FV3D_OK) {
+      if (g) cudaGraphDestroy(g);
+      return est;
+    }
+    CK(ce);
+    ce = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    CK(ce);
+    ctx->graphs[key] = exec;
+  } else {
+    exec = it->second;
+  }
+  CK(cudaEventRecord(ctx->ev0, ctx->stream));
+  for (int i = 0; i < n_steps; ++i) CK(cudaGraphLaunch(exec, ctx->stream));
+  CK(cudaEventRecord(ctx->ev1, ctx->stream));
+  DevScalars hs;
+  CK(cudaMemcpyAsync(&hs, ctx->d_sc.p, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  ctx->residual_valid = false;
+  if (stats != nullptr) {
+    stats->t = hs.t;
+    stats->dt = hs.dt;
+    stats->steps = hs.step;
+    stats->elapsed_ms = ms;
+  }
+  if (hs.status & 1) return ctx->fail(FV3D_ERR_NONFINITE, "non-finite state or time step after %d steps", hs.step);
+  return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_global_residual(fv3d_ctx* handle, double dt, double res[5]) {
+  if (handle == nullptr || res == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (!ctx->residual_valid) return ctx->fail(FV3D_ERR_STATE, "no residual evaluated (call fv3d_time_derivative)");
+  CK(cudaSetDevice(ctx->cfg.device));
+  const int nb = nblk(ctx->nc);
+  k_residual_partial<<<nb, 256, 0, ctx->stream>>>(ctx->nc, ctx->d_dphi.p, ctx->d_vol.p, ctx->d_part.p);
+  k_residual_final<<<1, 256, 0, ctx->stream>>>(nb, ctx->d_part.p, dt / ctx->vol_total, ctx->d_part.p + 5 * (size_t)nb);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(res, ctx->d_part.p + 5 * (size_t)nb, 5 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_profile_stage(fv3d_ctx* handle, int n_reps, double cfl, double* ms) {
+  if (handle == nullptr || ms == nullptr || n_reps <= 0) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  fv3d_status st = check_ready(ctx);
+  if (st != FV3D_OK) return st;
+  CK(cudaSetDevice(ctx->cfg.device));
+  cudaEvent_t ev[4];
+  for (int i = 0; i < 4; ++i) CK(cudaEventCreate(&ev[i]));
+  double acc[3] = {0, 0, 0};
+  // keep the state unchanged: stage of a low-storage Euler step with dt = 0
+  CK(cudaMemsetAsync(ctx->d_sc.p, 0, sizeof(DevScalars), ctx->stream));
+  StageCoef co{0.0, 0.0, 0, 0, 1};
+  for (int r = 0; r < n_reps; ++r) {
+    CK(cudaEventRecord(ev[0], ctx->stream));
+    CK(ctx->launch_stage_kernels(1, cfl > 0.0, co, 1));
+    CK(cudaEventRecord(ev[1], ctx->stream));
+    CK(ctx->launch_stage_kernels(1, cfl > 0.0, co, 2));
+    CK(cudaEventRecord(ev[2], ctx->stream));
+    CK(ctx->launch_stage_kernels(1, cfl > 0.0, co, 4));
+    CK(cudaEventRecord(ev[3], ctx->stream));
+    CK(cudaEventSynchronize(ev[3]));
+    for (int k = 0; k < 3; ++k) {
+      float t = 0.f;
+      CK(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+      acc[k] += t;
+    }
+  }
+  for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
+  for (int k = 0; k < 3; ++k) ms[k] = acc[k] / n_reps;
+  return FV3D_OK;
+}

@@ -1,0 +1,22 @@
+// Host-side launch entry points of the explicit-stage kernels (instantiated
+// for double in kernels_f64.cu and float in kernels_f32.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include "kernels.cuh"
+
+namespace fv3d {
+
+struct Disc {
+  int gmode;     // 0 none, 1 Green-Gauss, 2 least squares
+  bool linear;   // linear reconstruction
+  bool limit;    // Barth-Jespersen
+  bool viscous;  // mu != 0
+};
+
+template <class R> cudaError_t launch_gradients(const KArgs<R>& a, const Disc& d, cudaStream_t s);
+template <class R> cudaError_t launch_face_flux(const KArgs<R>& a, const Disc& d, cudaStream_t s);
+template <class R>
+cudaError_t launch_gather(const KArgs<R>& a, int mode, bool dt, const StageCoef& co, cudaStream_t s);
+
+}  // namespace fv3d

@@ -1,0 +1,174 @@
+/*
+ * fv3d_gpu.h - C ABI of the GB300 (sm_103a) FV3D residual / explicit-RK /
+ * implicit-solve path.
+ *
+ * Drop-in boundary for the reference solver library's hot path
+ * (src/Solver/include/solver/solver_module.h:16-273 and the Navier-Stokes
+ * plug-in registered in src/FV3D/src/navier_stokes/navier_stokes.c:85-124):
+ * plain pointers and sizes, no CUDA or C++ types, every call returns a status
+ * instead of aborting (the reference aborts through BM_CHECK_EXPRESSION).
+ *
+ * Ownership: the context owns all device memory.  Host arrays passed in are
+ * read during the call only; outputs go to caller-provided host buffers.
+ * Arrays are in the reference's order and AoS layouts; the context renumbers
+ * internally and maps back.  One host thread per context; all work runs on
+ * the context's CUDA stream.
+ */
+#ifndef FV3D_GPU_H
+#define FV3D_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fv3d_ctx fv3d_ctx;
+
+typedef enum fv3d_status {
+    FV3D_OK = 0,
+    FV3D_ERR_INVALID_ARG = 1,      /* bad argument or inconsistent mesh */
+    FV3D_ERR_UNSUPPORTED = 2,      /* feature not available in this build */
+    FV3D_ERR_NONFINITE = 3,        /* NaN/Inf residual (timedisc.c:179-181) */
+    FV3D_ERR_NOT_CONVERGED = 4,    /* Newton did not converge (implicit.c:350-351) */
+    FV3D_ERR_STAGNATED_FALLBACK = 5, /* learned preconditioner stagnated, fell back */
+    FV3D_ERR_DEVICE = 6,           /* CUDA error */
+    FV3D_ERR_TIMEOUT = 7,          /* a bounded device wait ran out */
+    FV3D_ERR_BOUNDS = 8,           /* an index outside its array */
+    FV3D_ERR_STATE = 9             /* call out of order (e.g. no mesh yet) */
+} fv3d_status;
+
+/* Option codes follow the reference's option order:
+ * flux (flux.c:273), reconstruction / limiter (solver_type.h:212-226),
+ * explicit scheme (solver_type.h:236-241; SSP-RK3 is new). */
+enum { FV3D_FLUX_AUSM = 0, FV3D_FLUX_RUSANOV = 1 };
+enum { FV3D_RECON_FIRST_ORDER = 0, FV3D_RECON_LINEAR = 1 };
+enum { FV3D_LIMITER_BARTH_JESPERSEN = 0, FV3D_LIMITER_NONE = 1 };
+enum { FV3D_GRADIENT_GREEN_GAUSS = 0, FV3D_GRADIENT_LEAST_SQUARES = 1 };
+enum { FV3D_PRECISION_FP64 = 0, FV3D_PRECISION_MIXED = 1 };
+enum { FV3D_RENUMBER_NONE = 0, FV3D_RENUMBER_MORTON = 1, FV3D_RENUMBER_RCM = 2 };
+enum { FV3D_RK_EULER = 0, FV3D_RK_33 = 1, FV3D_RK_45 = 2, FV3D_SSP_RK3 = 3 };
+/* boundary (region) types: navier_stokes_module.h:47-59 + pressure outlet */
+enum {
+    FV3D_BC_FLOW = 0, FV3D_BC_INFLOW = 1, FV3D_BC_OUTFLOW = 2,
+    FV3D_BC_WALL_ADIABATIC = 3, FV3D_BC_WALL_ISOTHERMAL = 4,
+    FV3D_BC_WALL_SLIP = 5, FV3D_BC_SYMMETRY = 6, FV3D_BC_STATE = 7,
+    FV3D_BC_FUNCTION = 8, FV3D_BC_PRESSURE_OUTLET = 9
+};
+
+/* Physics and discretisation (parameter keys Equation/Navier-Stokes/...,
+ * navier_stokes.c:55-66; FV/Reconstruction, FV/Limiter, .../Flux/flux_scheme) */
+typedef struct fv3d_config {
+    double kappa;
+    double R_mix;
+    double mu_mix;
+    double Pr;
+    double cfl_scale;
+    double dfl_scale;
+    int flux_scheme;
+    int reconstruction;
+    int limiter;
+    int gradient;
+    int precision;
+    int renumber;
+    int device;
+} fv3d_config;
+
+/* Mesh in the reference's processed layout (Mesh_t, solver_type.h:22-168, as
+ * read by read_mesh_file mesh.c:121-630).  face_cells[2i+1] = -1 on boundary
+ * faces.  face_dist_cell_2 may be NULL; when given it replaces x_f - x_c1 for
+ * interior faces (periodic images). */
+typedef struct fv3d_mesh_arrays {
+    int n_cells;
+    int n_faces;
+    int n_boundaries;
+    int max_cell_faces;
+    int n_regions;
+    const double *cell_x;       /* [n_cells*3] */
+    const double *cell_volume;  /* [n_cells] */
+    const double *cell_dx;      /* [n_cells*3] */
+    const int *cell_n_faces;    /* [n_cells] */
+    const int *cell_faces;      /* [n_cells*max_cell_faces], -1 padded */
+    const int *face_cells;      /* [n_faces*2] */
+    const int *face_boundary;   /* [n_faces], -1 interior */
+    const double *face_area;    /* [n_faces] */
+    const double *face_lambda;  /* [n_faces] */
+    const double *face_x;       /* [n_faces*3] */
+    const double *face_n;       /* [n_faces*3] */
+    const double *face_t1;      /* [n_faces*3] */
+    const double *face_t2;      /* [n_faces*3] */
+    const double *face_dist_cell_2; /* [n_faces*3] or NULL */
+    const int *boundary_id;     /* [n_boundaries] region id */
+    const int *boundary_face;   /* [n_boundaries] */
+    const int *region_is_boundary; /* [n_regions] */
+} fv3d_mesh_arrays;
+
+typedef struct fv3d_step_stats {
+    double t;           /* time after the steps */
+    double dt;          /* last time step used */
+    int steps;          /* steps taken */
+    double elapsed_ms;  /* device time of the steps (CUDA events) */
+} fv3d_step_stats;
+
+/* ---- lifecycle ---------------------------------------------------------- */
+/* replaces navier_stokes_initialize + init_reconstruction/init_limiter
+ * (navier_stokes.c:85-124, reconstruction.c:110-137, limiter.c:27-41) */
+fv3d_status fv3d_create(const fv3d_config *config, fv3d_ctx **ctx);
+/* replaces the free_* routines (solver_module.h:61-115) */
+fv3d_status fv3d_destroy(fv3d_ctx *ctx);
+const char *fv3d_last_error(const fv3d_ctx *ctx);
+/* version string and the compiled device architecture */
+const char *fv3d_version(void);
+
+/* ---- mesh ------------------------------------------------------------------ */
+/* replaces init_mesh(mesh_file) (mesh.c:98-106): takes the arrays that
+ * read_mesh_file would load, runs calc_mesh_metrics (mesh.c:19-83),
+ * validates indices, renumbers and uploads structure-of-arrays */
+fv3d_status fv3d_mesh_from_arrays(fv3d_ctx *ctx, const fv3d_mesh_arrays *mesh);
+/* replaces read_mesh_file (mesh.c:121-630); FV3D_ERR_UNSUPPORTED when this
+ * build has no HDF5 library */
+fv3d_status fv3d_mesh_load_h5(fv3d_ctx *ctx, const char *path);
+/* cell permutation chosen by renumbering: perm[new] = reference index */
+fv3d_status fv3d_get_permutation(const fv3d_ctx *ctx, int *perm);
+
+/* replaces boundary_initialize / parse_primitive_state (boundary.c:55-183):
+ * prim = (u, v, w, p, T); rho = p / (R T) */
+fv3d_status fv3d_set_region(fv3d_ctx *ctx, int region, int bc_type, const double prim[5]);
+
+/* ---- state ---------------------------------------------------------------- */
+/* conserved state [n_cells*5] in reference order (set_solution,
+ * finite_volume.c:189-201, followed by the update routine) */
+fv3d_status fv3d_set_state(fv3d_ctx *ctx, const double *u_con);
+/* reference phi_total layout [n_cells*10]: rho, rho_u, rho_v, rho_w, rho_e,
+ * u, v, w, p, T (navier_stokes.c:107-117) */
+fv3d_status fv3d_get_state(fv3d_ctx *ctx, double *phi_total);
+fv3d_status fv3d_get_conserved(fv3d_ctx *ctx, double *u_con);
+
+/* ---- hot path ---------------------------------------------------------------- */
+/* finite_volume_time_derivative (finite_volume.c:81-124): phi_dt [n_cells*5] */
+fv3d_status fv3d_time_derivative(fv3d_ctx *ctx, double t, double *phi_dt);
+/* time step.  cfl > 0: cfl * min_i V_i / sum_d (|u_d| + c) dx_d (the
+ * convective part of calc_ns_timestep, navier_stokes.c:171-187);
+ * cfl <= 0: calc_ns_timestep as written (navier_stokes.c:159-193) */
+fv3d_status fv3d_timestep(fv3d_ctx *ctx, double cfl, double *dt);
+/* n_steps explicit steps (timestep_lserkw2, explicit.c:96-140, or SSP-RK3),
+ * dt recomputed on the device each step from cfl (cfl > 0) or fixed dt_fixed,
+ * replayed as one CUDA graph per step.  stats may be NULL. */
+fv3d_status fv3d_step_explicit(fv3d_ctx *ctx, int scheme, int n_steps, double cfl,
+                               double dt_fixed, fv3d_step_stats *stats);
+/* calc_global_residual (analyze.c:37-61) of the last residual evaluation */
+fv3d_status fv3d_global_residual(fv3d_ctx *ctx, double dt, double res[5]);
+
+/* ---- measurement helpers ------------------------------------------------------ */
+/* average device time (ms) per launch of each explicit-stage kernel over
+ * n_reps stages, each bracketed by CUDA events on the context stream:
+ * ms[0] gradients, ms[1] face flux, ms[2] gather+update */
+fv3d_status fv3d_profile_stage(fv3d_ctx *ctx, int n_reps, double cfl, double *ms);
+/* CUDA stream (cudaStream_t) the context launches on, for event timing */
+fv3d_status fv3d_get_stream(const fv3d_ctx *ctx, void **stream);
+/* device pointer of the conserved state, [5][n_cells] SoA in renumbered order */
+fv3d_status fv3d_device_state(const fv3d_ctx *ctx, double **u_dev);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FV3D_GPU_H */

@@ -1,0 +1,203 @@
+"""GPU (sm_103a) hot path against the CPU oracle, through the C ABI.
+
+Tolerances: FP64 path <= 1e-12 relative per residual evaluation and
+<= 1e-10 relative L2 per conserved variable after the stated steps; mixed
+path <= 1e-5 relative L2 after the stated steps (FP32 faces, FP64 state).
+"""
+import numpy as np
+import pytest
+
+import golden_io
+from fv3d_gb300 import api, cases, meshgen as mg
+from oracle import oracle as orc
+from parity import rel_l2, rel_max
+
+pytestmark = pytest.mark.gpu
+
+FP64_RESIDUAL_TOL = 1e-12
+FP64_STATE_TOL = 1e-10
+MIXED_STATE_TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def oracle():
+    return orc.Oracle("restated")
+
+
+def perturbed(c, amp=0.01, seed=5):
+    rng = np.random.default_rng(seed)
+    u = c.u0.copy()
+    u[:, 0] *= 1.0 + amp * rng.uniform(-1, 1, u.shape[0])
+    u[:, 1:4] += amp * rng.uniform(-1, 1, (u.shape[0], 3)) * u[:, :1]
+    u[:, 4] *= 1.0 + amp * rng.uniform(-1, 1, u.shape[0])
+    return u
+
+
+SMALL = {
+    "euler_hex4": lambda: cases.euler16(4),
+    "tgv_tet3_gg": lambda: cases.tgv_tet(3),
+    "tgv_hex4_lsq": lambda: cases.tgv_hex(4),
+    "channel_pressure_outlet": lambda: cases.channel(6, 4, 4),
+}
+
+
+def boundary_variants():
+    out = []
+    for t in (mg.BC_OUTFLOW, mg.BC_WALL_ISOTHERMAL, mg.BC_WALL_SLIP, mg.BC_SYMMETRY, mg.BC_STATE):
+        out.append((f"channel_outlet_type{t}", t))
+    return out
+
+
+@pytest.mark.parametrize("name", list(SMALL))
+@pytest.mark.parametrize("renumber", ["none", "morton", "rcm"])
+def test_residual_fp64_matches_oracle(oracle, name, renumber):
+    c = SMALL[name]()
+    u = perturbed(c)
+    oracle.init(c.mesh, c.params, c.region_type, c.region_prim)
+    oracle.set_conserved(u)
+    r_ref = oracle.time_derivative(0.0)
+    with api.Solver(c.mesh, c.params, c.region_type, c.region_prim, "fp64", renumber) as s:
+        s.set_state(u)
+        r = s.time_derivative(0.0)
+        assert rel_max(r, r_ref) < FP64_RESIDUAL_TOL
+        # state export in the reference phi_total layout
+        assert rel_max(s.get_state(), oracle.total()[: c.mesh.n_cells]) < 1e-14
+
+
+@pytest.mark.parametrize("label,btype", boundary_variants())
+def test_boundary_types_fp64(oracle, label, btype):
+    c = cases.channel(6, 4, 4)
+    c.params["mu_mix"] = 0.01
+    c.region_type[2] = btype
+    c.region_prim[2] = [0.2, 0.01, 0.0, 1 / 1.4, 0.9 / 1.4]
+    if btype == mg.BC_WALL_ISOTHERMAL:
+        c.region_type[3] = btype
+        c.region_prim[3] = [0.0, 0.0, 0.0, 1 / 1.4, 0.8 / 1.4]
+    u = perturbed(c)
+    oracle.init(c.mesh, c.params, c.region_type, c.region_prim)
+    oracle.set_conserved(u)
+    r_ref = oracle.time_derivative(0.0)
+    with api.Solver(c.mesh, c.params, c.region_type, c.region_prim, "fp64") as s:
+        s.set_state(u)
+        assert rel_max(s.time_derivative(0.0), r_ref) < FP64_RESIDUAL_TOL
+
+
+@pytest.mark.parametrize("name", golden_io.names())
+def test_residual_fp64_matches_reference_golden(name):
+    """Against outputs of the reference's own C code (committed fixtures)."""
+    mesh, params, z = golden_io.load(name)
+    with api.Solver(mesh, params, z["region_type"], z["region_prim"], "fp64") as s:
+        s.set_state(z["u_in"])
+        assert rel_max(s.time_derivative(0.0), z["dphi"]) < FP64_RESIDUAL_TOL
+        for k, (scheme, nsteps) in enumerate(z["rk_plan"]):
+            for st in range(nsteps):
+                s.step_explicit(["euler", "rk33", "rk45"][int(scheme)], 1, cfl=0.5)
+                key = f"rk{k}_s{scheme}_n{st}"
+                assert rel_max(s.get_conserved(), z[key]) < FP64_STATE_TOL, key
+
+
+def test_timestep_and_residual_norm(oracle):
+    c = cases.tgv_tet(4)
+    oracle.init(c.mesh, c.params, c.region_type, c.region_prim)
+    oracle.set_conserved(c.u0)
+    with api.from_case(c, "fp64") as s:
+        assert abs(s.timestep(0.5) / oracle.timestep_convective(0.5) - 1) < 1e-14
+        assert abs(s.timestep(0.0) / oracle.calc_ns_timestep() - 1) < 1e-14
+        dt = 1e-3
+        s.time_derivative(0.0)
+        oracle.time_derivative(0.0)
+        assert rel_max(s.global_residual(dt), oracle.global_residual(dt)) < 1e-12
+
+
+def run_oracle(oracle, c, scheme, steps, cfl):
+    oracle.init(c.mesh, c.params, c.region_type, c.region_prim)
+    oracle.set_conserved(c.u0)
+    t = 0.0
+    for k in range(steps):
+        dt = oracle.timestep_convective(cfl)
+        if scheme == "ssprk3":
+            oracle.step_ssprk3(t, dt)
+        else:
+            oracle.step_lserkw2({"euler": 0, "rk33": 1, "rk45": 2}[scheme], k, t, dt)
+        t += dt
+    return oracle.conserved(), t
+
+
+def test_euler16_ssprk3_100_steps(oracle):
+    """Plain FP64 explicit Euler on the periodic 16^3 box: SSP-RK3, CFL 0.5,
+    100 steps, against the CPU oracle."""
+    c = cases.euler16(16)
+    u_ref, t_ref = run_oracle(oracle, c, "ssprk3", 100, 0.5)
+    with api.from_case(c, "fp64") as s:
+        st = s.step_explicit("ssprk3", 100, cfl=0.5)
+        err = rel_l2(s.get_conserved(), u_ref, u_ref=0.5)
+    assert st["steps"] == 100 and abs(st["t"] / t_ref - 1) < 1e-12
+    assert err.max() < FP64_STATE_TOL, err
+
+
+@pytest.mark.parametrize("scheme", ["euler", "rk33", "rk45"])
+def test_euler16_low_storage_schemes(oracle, scheme):
+    c = cases.euler16(8)
+    u_ref, _ = run_oracle(oracle, c, scheme, 20, 0.5)
+    with api.from_case(c, "fp64") as s:
+        s.step_explicit(scheme, 20, cfl=0.5)
+        assert rel_l2(s.get_conserved(), u_ref, 0.5).max() < FP64_STATE_TOL
+
+
+@pytest.mark.parametrize("maker,steps", [
+    (lambda: cases.tgv_hex(8), 20),
+    (lambda: cases.tgv_tet(8), 20),
+])
+def test_navier_stokes_fp64_and_mixed(oracle, maker, steps):
+    c = maker()
+    u_ref, _ = run_oracle(oracle, c, "rk33", steps, 0.5)
+    with api.from_case(c, "fp64") as s:
+        s.step_explicit("rk33", steps, cfl=0.5)
+        e64 = rel_l2(s.get_conserved(), u_ref)
+    with api.from_case(c, "mixed") as s:
+        s.step_explicit("rk33", steps, cfl=0.5)
+        emx = rel_l2(s.get_conserved(), u_ref)
+    assert e64.max() < FP64_STATE_TOL, e64
+    assert emx.max() < MIXED_STATE_TOL, emx
+
+
+def test_deterministic_and_renumbering_invariant():
+    """No atomics in the accumulation: repeated runs are bit-identical, and
+    because every cell sums its faces in reference face order the result does
+    not depend on the renumbering either."""
+    c = cases.tgv_tet(6)
+    outs = []
+    for renumber in ("morton", "morton", "rcm", "none"):
+        with api.from_case(c, "mixed", renumber) as s:
+            s.step_explicit("rk33", 5, cfl=0.5)
+            outs.append(s.get_conserved())
+    for o in outs[1:]:
+        assert np.array_equal(o, outs[0])
+
+
+def test_nonfinite_state_is_reported():
+    c = cases.tgv_tet(4)
+    u = c.u0.copy()
+    u[7, 4] = np.nan
+    with api.Solver(c.mesh, c.params, c.region_type, c.region_prim, "fp64") as s:
+        s.set_state(u)
+        with pytest.raises(api.FV3DError) as e:
+            s.step_explicit("rk33", 3, cfl=0.5)
+        assert e.value.status == 3  # FV3D_ERR_NONFINITE
+
+
+def test_corrupt_mesh_rejected():
+    c = cases.channel(4, 4, 4)
+    fc = c.mesh.face_cells.copy()
+    fc[5, 0] = c.mesh.n_cells + 10
+    c.mesh.face_cells = fc
+    with pytest.raises(api.FV3DError) as e:
+        api.Solver(c.mesh, c.params, c.region_type, c.region_prim, "fp64")
+    assert e.value.status == 8  # FV3D_ERR_BOUNDS
+
+
+def test_hdf5_load_unsupported():
+    c = cases.euler16(4)
+    with api.from_case(c) as s:
+        st = s.lib.fv3d_mesh_load_h5(s.h, b"mesh.h5")
+        assert st == 2  # FV3D_ERR_UNSUPPORTED

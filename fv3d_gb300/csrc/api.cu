@@ -219,6 +219,18 @@ KArgs<R> Ctx::args() const {
   return a;
 }
 
+MxArgs Ctx::mx_args() const {
+  MxArgs a;
+  memset(&a, 0, sizeof(a));
+  a.nc = nc; a.nf = nf; a.nf_int = nf_int; a.mcf = mcf;
+  a.cface = d_cface.p; a.fcell = d_fcell.p; a.geoN = d_geoN.p; a.geoD = d_geoD.p;
+  a.lsqW = d_lsqW.p; a.fregion = d_fregion.p; a.rvol = (const float*)d_rvol.p;
+  a.vol = d_vol.p; a.dx = d_dx.p; a.Uf = d_Uf.p; a.fs = d_fs.p;
+  a.U = d_U.p; a.K = d_K.p; a.U0 = d_U0.p; a.dphi = d_dphi.p; a.sc = d_sc.p;
+  a.pc = phys;
+  return a;
+}
+
 Disc Ctx::disc() const {
   Disc d;
   d.linear = cfg.reconstruction == FV3D_RECON_LINEAR;
@@ -237,10 +249,10 @@ cudaError_t Ctx::launch_stage_kernels(int mode, bool dt, const StageCoef& co, in
     if (e == cudaSuccess && (which & 2)) e = launch_face_flux<double>(a, d, stream);
     if (e == cudaSuccess && (which & 4)) e = launch_gather<double>(a, mode, dt, co, stream);
   } else {
-    KArgs<float> a = args<float>();
-    if (which & 1) e = launch_gradients<float>(a, d, stream);
-    if (e == cudaSuccess && (which & 2)) e = launch_face_flux<float>(a, d, stream);
-    if (e == cudaSuccess && (which & 4)) e = launch_gather<float>(a, mode, dt, co, stream);
+    // mixed path: bit 1 = gradient pass, bit 4 = flux + update pass
+    MxArgs a = mx_args();
+    if (which & 1) e = launch_mx_sides(a, d, stream);
+    if (e == cudaSuccess && (which & 4)) e = launch_mx_flux_update(a, d, mode, dt, co, stream);
   }
   return e;
 }
@@ -610,13 +622,17 @@ extern "C" fv3d_status fv3d_profile_stage(fv3d_ctx* handle, int n_reps, double c
   // keep the state unchanged: stage of a low-storage Euler step with dt = 0
   CK(cudaMemsetAsync(ctx->d_sc.p, 0, sizeof(DevScalars), ctx->stream));
   StageCoef co{0.0, 0.0, 0, 0, 1};
+  // FP64 path: gradients, face flux, gather+update; mixed path: gradient
+  // pass, flux+update pass (ms[2] = 0)
+  const int masks[3] = {1, ctx->fp64() ? 2 : 0, ctx->fp64() ? 4 : 4};
   for (int r = 0; r < n_reps; ++r) {
     CK(cudaEventRecord(ev[0], ctx->stream));
-    CK(ctx->launch_stage_kernels(1, cfl > 0.0, co, 1));
+    CK(ctx->launch_stage_kernels(1, cfl > 0.0, co, masks[0]));
     CK(cudaEventRecord(ev[1], ctx->stream));
-    CK(ctx->launch_stage_kernels(1, cfl > 0.0, co, 2));
+    if (ctx->fp64()) CK(ctx->launch_stage_kernels(1, cfl > 0.0, co, masks[1]));
     CK(cudaEventRecord(ev[2], ctx->stream));
-    CK(ctx->launch_stage_kernels(1, cfl > 0.0, co, 4));
+    if (ctx->fp64()) CK(ctx->launch_stage_kernels(1, cfl > 0.0, co, masks[2]));
+    else CK(ctx->launch_stage_kernels(1, cfl > 0.0, co, 4));
     CK(cudaEventRecord(ev[3], ctx->stream));
     CK(cudaEventSynchronize(ev[3]));
     for (int k = 0; k < 3; ++k) {
@@ -627,5 +643,6 @@ extern "C" fv3d_status fv3d_profile_stage(fv3d_ctx* handle, int n_reps, double c
   }
   for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
   for (int k = 0; k < 3; ++k) ms[k] = acc[k] / n_reps;
+  if (!ctx->fp64()) { ms[1] = ms[2]; ms[2] = 0.0; }
   return FV3D_OK;
 }

@@ -7,7 +7,7 @@
 #include <vector>
 
 #include "../../include/fv3d_gpu.h"
-#include "kernels.cuh"
+#include "kernels_mixed.cuh"
 #include "launch.h"
 
 namespace fv3d {
@@ -62,6 +62,10 @@ struct Ctx {
   DevBuf<double> d_U, d_K, d_U0, d_dphi, d_stage, d_part;
   DevBuf<float> d_Uf;
   DevBuf<char> d_rec, d_FA;
+  // mixed path
+  DevBuf<int2> d_fcell;
+  DevBuf<float4> d_geoN, d_geoD, d_lsqW;
+  DevBuf<float> d_fs;
   DevBuf<DevScalars> d_sc;
   DevBuf<unsigned long long> d_bits;
 
@@ -77,8 +81,10 @@ struct Ctx {
     d_geo.release(); d_lam.release(); d_lsq.release(); d_rvol.release(); d_vol.release(); d_dx.release();
     d_U.release(); d_K.release(); d_U0.release(); d_dphi.release(); d_stage.release(); d_part.release();
     d_Uf.release(); d_rec.release(); d_FA.release(); d_sc.release(); d_bits.release();
+    d_fcell.release(); d_geoN.release(); d_geoD.release(); d_lsqW.release(); d_fs.release();
   }
   template <class R> KArgs<R> args() const;
+  MxArgs mx_args() const;
   Disc disc() const;
   cudaError_t launch_stage_kernels(int mode, bool dt, const StageCoef& co, int which);
 };

@@ -364,11 +364,12 @@ __global__ void __launch_bounds__(256) k_gather_update(const __grid_constant__ K
       for (int j = 0; j < 5; ++j) a.dphi[(size_t)j * a.nc + c] = r[j];
     } else {
       const double dt = a.sc->dt;
-      double u[5];
+      double u[5], uold[5];
 #pragma unroll
       for (int j = 0; j < 5; ++j) {
         const size_t i = (size_t)j * a.nc + c;
         double uj = a.U[i];
+        uold[j] = uj;
         if (MODE == 1) {
           double kj = co.first ? r[j] : r[j] + a.K[i] * co.a;
           a.K[i] = kj;
@@ -387,35 +388,43 @@ __global__ void __launch_bounds__(256) k_gather_update(const __grid_constant__ K
       }
       if (sizeof(R) == 4 || DT) {
         // primitive recovery of the new state: FP32 shadow for the next
-        // stage (mixed path) and the next CFL time step
+        // stage (mixed path) and the next CFL time step.  The reference's
+        // step loop evaluates calc_ns_timestep on phi_total whose density is
+        // already updated while u, v, w, p still hold the values of the last
+        // stage's input (timestep_lserkw2 updates only the conserved entries,
+        // explicit.c:136-139); the low-storage path reproduces that, SSP-RK3
+        // (whose stepper refreshes the primitives) uses the new state.
         const double km1 = a.pc.km1;
         if (sizeof(R) == 4) {
+          float4* sh = reinterpret_cast<float4*>(a.Uf) + 2 * (size_t)c;
+          float4 o0 = sh[0], o1 = sh[1];  // stage-input shadow (rho, m, E, p, T)
           float rho = (float)u[0], mx = (float)u[1], my = (float)u[2], mz = (float)u[3];
           float vx = mx / rho, vy = my / rho, vz = mz / rho;
           float ke = 0.5f * (mx * vx + my * vy + mz * vz);
           float p = (float)(km1 * (u[4] - (double)ke));
           p = fmaxf(1.00E-10f, p);
           float T = p / (rho * (float)a.pc.R_mix);
-          float4* dst = reinterpret_cast<float4*>(a.Uf) + 2 * (size_t)c;
-          dst[0] = make_float4(rho, mx, my, mz);
-          dst[1] = make_float4((float)u[4], p, T, 0.f);
+          sh[0] = make_float4(rho, mx, my, mz);
+          sh[1] = make_float4((float)u[4], p, T, 0.f);
           if (DT) {
-            const float c_s = sqrtf((float)a.pc.kappa * p / rho);
+            float pu = vx, pv = vy, pw = vz, pp = p;
+            if (MODE == 1) { pu = o0.y / o0.x; pv = o0.z / o0.x; pw = o0.w / o0.x; pp = o1.y; }
+            const float c_s = sqrtf((float)a.pc.kappa * pp / rho);
             const double* d = a.dx + 3 * (size_t)c;
-            float ds = (fabsf(vx) + c_s) * (float)d[0] + (fabsf(vy) + c_s) * (float)d[1] +
-                       (fabsf(vz) + c_s) * (float)d[2];
+            float ds = (fabsf(pu) + c_s) * (float)d[0] + (fabsf(pv) + c_s) * (float)d[1] +
+                       (fabsf(pw) + c_s) * (float)d[2];
             double lam = (double)((float)a.vol[c] / ds);
             if (lam > 0.0) lam_bits = (unsigned long long)__double_as_longlong(lam);
           }
-        } else {
+        } else if (DT) {
           double q[10];
           Phys<double> ph;
           ph.load(a.pc);
 #pragma unroll
-          for (int j = 0; j < 5; ++j) q[j] = u[j];
+          for (int j = 0; j < 5; ++j) q[j] = (MODE == 1) ? uold[j] : u[j];
           cons_to_prims(q, ph);
-          double s_rho = 1.0 / q[RHO];
-          double c_s = sqrt(ph.kappa * q[PR] * s_rho);
+          double s_rho = 1.0 / u[0];
+          double c_s = sqrt(a.pc.kappa * q[PR] * s_rho);
           const double* d = a.dx + 3 * (size_t)c;
           double ds = (fabs(q[VU]) + c_s) * d[0] + (fabs(q[VV]) + c_s) * d[1] + (fabs(q[VW]) + c_s) * d[2];
           double lam = a.vol[c] / ds;

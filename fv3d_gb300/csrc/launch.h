@@ -1,5 +1,6 @@
-// Host-side launch entry points of the explicit-stage kernels (instantiated
-// for double in kernels_f64.cu and float in kernels_f32.cu).
+// Host-side launch entry points of the explicit-stage kernels: the FP64 path
+// (kernels_f64.cu, three launches per stage) and the mixed path
+// (kernels_mixed.cu, two launches per stage).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -13,6 +14,11 @@ struct Disc {
   bool limit;    // Barth-Jespersen
   bool viscous;  // mu != 0
 };
+
+struct MxArgs;
+cudaError_t launch_mx_sides(const MxArgs& a, const Disc& d, cudaStream_t s);
+cudaError_t launch_mx_flux_update(const MxArgs& a, const Disc& d, int mode, bool dt,
+                                  const StageCoef& co, cudaStream_t s);
 
 template <class R> cudaError_t launch_gradients(const KArgs<R>& a, const Disc& d, cudaStream_t s);
 template <class R> cudaError_t launch_face_flux(const KArgs<R>& a, const Disc& d, cudaStream_t s);

@@ -332,8 +332,29 @@ fv3d_status upload_mesh(Ctx& ctx) {
   ALLOC(ctx.d_stage, (size_t)nc * 10);
   ALLOC(ctx.d_part, (size_t)((nc + 255) / 256 + 1) * 5 + 5);
   if (!ctx.fp64()) ALLOC(ctx.d_Uf, (size_t)nc * 8);
-  ALLOC(ctx.d_rec, (size_t)nc * REC * ctx.rsize());
-  ALLOC(ctx.d_FA, (size_t)nf * FAS * ctx.rsize());
+  if (ctx.fp64()) {
+    ALLOC(ctx.d_rec, (size_t)nc * REC * ctx.rsize());
+    ALLOC(ctx.d_FA, (size_t)nf * FAS * ctx.rsize());
+  } else {
+    // mixed path: compact float4 geometry and per-face-side records
+    std::vector<int2> fcell(nf);
+    std::vector<float4> gN(nf), gD(2 * (size_t)nf), lw(2 * (size_t)nf);
+    for (int f = 0; f < nf; ++f) {
+      const double* g = &ctx.h_geo[(size_t)f * GEO];
+      fcell[f] = make_int2(ctx.h_fc0[f], ctx.h_fc1[f]);
+      gN[f] = make_float4((float)g[G_N], (float)g[G_N + 1], (float)g[G_N + 2], (float)g[G_A]);
+      gD[f] = make_float4((float)g[G_D1], (float)g[G_D1 + 1], (float)g[G_D1 + 2], (float)ctx.h_lam[f]);
+      gD[(size_t)nf + f] = make_float4((float)g[G_D2], (float)g[G_D2 + 1], (float)g[G_D2 + 2], (float)ctx.h_lam[f]);
+      const double* w = &ctx.h_lsq[6 * (size_t)f];
+      lw[f] = make_float4((float)w[0], (float)w[1], (float)w[2], 0.f);
+      lw[(size_t)nf + f] = make_float4((float)w[3], (float)w[4], (float)w[5], 0.f);
+    }
+    UP(ctx.d_fcell, fcell.data(), (size_t)nf);
+    UP(ctx.d_geoN, gN.data(), (size_t)nf);
+    UP(ctx.d_geoD, gD.data(), 2 * (size_t)nf);
+    UP(ctx.d_lsqW, lw.data(), 2 * (size_t)nf);
+    ALLOC(ctx.d_fs, (size_t)nf * 2 * FS);
+  }
   ALLOC(ctx.d_sc, 1);
   ALLOC(ctx.d_bits, 2);
   ctx.mesh_ready = true;

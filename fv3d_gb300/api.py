@@ -166,8 +166,13 @@ class Solver:
         self._check(self.lib.fv3d_get_state(self.h, _p(out, _f8p)))
         return out
 
-    def get_conserved(self):
-        out = np.empty((self.nc, 5))
+    def get_conserved(self, out=None):
+        """Conserved state (n_cells, 5); `out` (C-contiguous float64, e.g. a
+        pinned host buffer) is filled in place when given."""
+        if out is None:
+            out = np.empty((self.nc, 5))
+        if out.shape != (self.nc, 5) or out.dtype != np.float64 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous float64 array of shape (n_cells, 5)")
         self._check(self.lib.fv3d_get_conserved(self.h, _p(out, _f8p)))
         return out
 

@@ -25,7 +25,8 @@ namespace {
 
 // reference AoS [n][5] (reference order) -> SoA [5][n] (renumbered) + FP32 shadow
 __global__ void k_import(int nc, const int* __restrict__ perm, const double* __restrict__ in,
-                         double* __restrict__ U, float* __restrict__ Uf, double km1, double R) {
+                         double* __restrict__ U, float* __restrict__ Uf, float* __restrict__ UfN,
+                         double km1, double R) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   const double* s = in + 5 * (size_t)perm[c];
@@ -40,6 +41,9 @@ __global__ void k_import(int nc, const int* __restrict__ perm, const double* __r
     float4* d = reinterpret_cast<float4*>(Uf) + 2 * (size_t)c;
     d[0] = make_float4(rho, mx, my, mz);
     d[1] = make_float4((float)u[4], p, T, 0.f);
+    float4* b = reinterpret_cast<float4*>(UfN) + 2 * (size_t)c;
+    b[0] = d[0];
+    b[1] = d[1];
   }
 }
 
@@ -224,9 +228,9 @@ MxArgs Ctx::mx_args() const {
   memset(&a, 0, sizeof(a));
   a.nc = nc; a.nf = nf; a.nf_int = nf_int; a.mcf = mcf;
   a.cface = d_cface.p; a.fcell = d_fcell.p; a.geoN = d_geoN.p; a.geoD = d_geoD.p;
-  a.lsqW = d_lsqW.p; a.fregion = d_fregion.p; a.rvol = (const float*)d_rvol.p;
-  a.vol = d_vol.p; a.dx = d_dx.p; a.Uf = d_Uf.p; a.fs = d_fs.p;
-  a.U = d_U.p; a.K = d_K.p; a.U0 = d_U0.p; a.dphi = d_dphi.p; a.sc = d_sc.p;
+  a.lsqW = d_lsqW.p; a.fregion = d_fregion.p; a.cgeo = d_cgeo.p; a.cdx = d_cdx.p;
+  a.Uf = d_Uf.p; a.UfN = d_UfN.p; a.fs = d_fs.p;
+  a.U = d_U.p; a.kf = d_kf.p; a.dU = d_dU.p; a.dphi = d_dphi.p; a.sc = d_sc.p;
   a.pc = phys;
   return a;
 }
@@ -413,7 +417,8 @@ extern "C" fv3d_status fv3d_set_state(fv3d_ctx* handle, const double* u) {
   CK(cudaMemcpyAsync(ctx->d_stage.p, u, sizeof(double) * 5 * (size_t)ctx->nc, cudaMemcpyHostToDevice,
                      ctx->stream));
   k_import<<<nblk(ctx->nc), 256, 0, ctx->stream>>>(ctx->nc, ctx->d_perm.p, ctx->d_stage.p, ctx->d_U.p,
-                                                  ctx->fp64() ? nullptr : ctx->d_Uf.p, ctx->phys.km1,
+                                                  ctx->fp64() ? nullptr : ctx->d_Uf.p,
+                                                  ctx->fp64() ? nullptr : ctx->d_UfN.p, ctx->phys.km1,
                                                   ctx->cfg.R_mix);
   CK(cudaGetLastError());
   ctx->state_ready = true;
@@ -458,7 +463,7 @@ extern "C" fv3d_status fv3d_time_derivative(fv3d_ctx* handle, double t, double* 
   if (st != FV3D_OK) return st;
   if (!ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "no state set");
   CK(cudaSetDevice(ctx->cfg.device));
-  StageCoef co{0, 0, 0, 0, 1};
+  StageCoef co{0, 0, 0, 0, 1, 1};
   CK(ctx->launch_stage_kernels(0, false, co, 7));
   ctx->residual_valid = true;
   if (phi_dt != nullptr) return export_soa(ctx, ctx->d_dphi.p, 5, 0, phi_dt);
@@ -523,12 +528,12 @@ static fv3d_status enqueue_step(Ctx* ctx, int scheme, double cfl) {
   if (scheme == FV3D_SSP_RK3) {
     const double c0[3] = {0.0, 0.75, 1.0 / 3.0}, c1[3] = {1.0, 0.25, 2.0 / 3.0};
     for (int s = 0; s < 3; ++s) {
-      StageCoef co{0, 0, c0[s], c1[s], s == 0};
+      StageCoef co{0, 0, c0[s], c1[s], s == 0, s == 2};
       CK(ctx->launch_stage_kernels(2, dt_dev && s == 2, co, 7));
     }
   } else {
     for (int s = 0; s < RK_S[scheme]; ++s) {
-      StageCoef co{RK_A[scheme][s], RK_G[scheme][s], 0, 0, s == 0};
+      StageCoef co{RK_A[scheme][s], RK_G[scheme][s], 0, 0, s == 0, s == RK_S[scheme] - 1};
       CK(ctx->launch_stage_kernels(1, dt_dev && s == RK_S[scheme] - 1, co, 7));
     }
   }
@@ -621,7 +626,7 @@ extern "C" fv3d_status fv3d_profile_stage(fv3d_ctx* handle, int n_reps, double c
   double acc[3] = {0, 0, 0};
   // keep the state unchanged: stage of a low-storage Euler step with dt = 0
   CK(cudaMemsetAsync(ctx->d_sc.p, 0, sizeof(DevScalars), ctx->stream));
-  StageCoef co{0.0, 0.0, 0, 0, 1};
+  StageCoef co{0.0, 0.0, 0, 0, 1, 0};
   // FP64 path: gradients, face flux, gather+update; mixed path: gradient
   // pass, flux+update pass (ms[2] = 0)
   const int masks[3] = {1, ctx->fp64() ? 2 : 0, ctx->fp64() ? 4 : 4};

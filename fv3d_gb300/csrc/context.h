@@ -64,8 +64,8 @@ struct Ctx {
   DevBuf<char> d_rec, d_FA;
   // mixed path
   DevBuf<int2> d_fcell;
-  DevBuf<float4> d_geoN, d_geoD, d_lsqW;
-  DevBuf<float> d_fs;
+  DevBuf<float4> d_geoN, d_geoD, d_lsqW, d_cgeo, d_cdx;
+  DevBuf<float> d_fs, d_UfN, d_kf, d_dU;
   DevBuf<DevScalars> d_sc;
   DevBuf<unsigned long long> d_bits;
 
@@ -82,6 +82,7 @@ struct Ctx {
     d_U.release(); d_K.release(); d_U0.release(); d_dphi.release(); d_stage.release(); d_part.release();
     d_Uf.release(); d_rec.release(); d_FA.release(); d_sc.release(); d_bits.release();
     d_fcell.release(); d_geoN.release(); d_geoD.release(); d_lsqW.release(); d_fs.release();
+    d_cgeo.release(); d_cdx.release(); d_UfN.release(); d_kf.release(); d_dU.release();
   }
   template <class R> KArgs<R> args() const;
   MxArgs mx_args() const;

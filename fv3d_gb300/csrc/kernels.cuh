@@ -319,6 +319,7 @@ struct StageCoef {
   double a, g;        // low-storage coefficients
   double c0, c1;      // SSP combination
   int first;          // first stage of the step
+  int last;           // last stage of the step
 };
 
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {

@@ -3,29 +3,39 @@
 //  k_mx_sides        (gradient pass, cell-gather) per cell: neighbour states
 //                    -> Green-Gauss / least-squares gradients and the
 //                    Barth-Jespersen bounds in registers, then for each of the
-//                    cell's faces the limited reconstructed state and that
-//                    side's viscous normal flux; one 48-byte record per face
-//                    side (the ghost side of a boundary face is written by its
-//                    interior cell).
+//                    cell's faces the limited reconstructed conserved state
+//                    and that side's viscous normal flux, written into the
+//                    face's record (the ghost side of a boundary face is
+//                    written by its interior cell).
 //  k_mx_flux_update  (flux + update pass, cell-gather) per cell: for each of
 //                    its faces the convective flux from both side records
 //                    plus the averaged viscous flux, summed with Kahan
 //                    compensation in ascending reference face id, -sum/V,
-//                    fused FP64 RK update, FP32 shadow state, next time step.
+//                    RK stage update, FP32 stage state, next time step.
 //
 // Each face flux is evaluated by both of its cells from identical inputs with
 // identical instructions, so the two contributions cancel exactly and the
 // scheme stays conservative; no face-flux buffer and no atomics.
+//
 // Fluxes are evaluated in the global frame: the reference rotates momenta
 // into (n, t1, t2), applies the 1-D flux and rotates back (flux.c:56-84),
 // which for Rusanov and AUSM is algebraically the global-frame formula below.
+//
+// Precision: faces, gradients, limiter, residual in FP32.  The conserved
+// state U_n is FP64; within a step the RK register and the increment
+// dU = U_stage - U_n are FP32 (they are O(dt R), so FP32 rounding of them is
+// far below the FP32 residual error), and the end of each step forms
+// U_{n+1} = U_n + dU in FP64.  The stage state the next gradient pass reads
+// is the FP32 record Uf = float(U_n) + dU.
 #pragma once
 
 #include "kernels.cuh"
 
 namespace fv3d {
 
-constexpr int FS = 12;  // floats per face-side record: q[0..7], viscous (mx, my, mz, e)
+// face record: side s at float4 [2s, 2s+1] = (rho, mx, my, mz), (E, vmx, vmy, vmz);
+// float4 [4] = (ve side 0, ve side 1, -, -).  v* = viscous normal flux times A.
+constexpr int FREC = 20;
 
 struct MxArgs {
   int nc, nf, nf_int, mcf;
@@ -35,14 +45,14 @@ struct MxArgs {
   const float4* __restrict__ geoD;   // [2][nf] (d_side, lambda)
   const float4* __restrict__ lsqW;   // [2][nf] (w_side, 0)
   const int* __restrict__ fregion;   // [nf - nf_int]
-  const float* __restrict__ rvol;    // [nc]
-  const double* __restrict__ vol;    // [nc]
-  const double* __restrict__ dx;     // [nc][3]
-  float* Uf;                         // [nc][8]
-  float* fs;                         // [nf][2][FS]
-  double* U;                         // [5][nc]
-  double* K;                         // [5][nc]
-  double* U0;                        // [5][nc]
+  const float4* __restrict__ cgeo;   // [nc] (sum_f s_f n_f A_f, 1/V)
+  const float4* __restrict__ cdx;    // [nc] (dx, V)
+  float* Uf;                         // [nc][8] stage state (rho, m, E, p, T, -)
+  float* UfN;                        // [nc][8] float(U_n) + p, T
+  float* fs;                         // [nf][FREC]
+  double* U;                         // [5][nc] conserved state U_n (FP64)
+  float* kf;                         // [5][nc] RK register (FP32)
+  float* dU;                         // [5][nc] U_stage - U_n (FP32)
   double* dphi;                      // [5][nc]
   DevScalars* sc;
   PhysConst pc;
@@ -57,9 +67,7 @@ struct MxPhys {
   }
 };
 
-__device__ __forceinline__ void mx_load_state(const float* __restrict__ Uf, int c, float* q) {
-  const float4* s = reinterpret_cast<const float4*>(Uf) + 2 * (size_t)c;
-  float4 x = __ldg(s), y = __ldg(s + 1);
+__device__ __forceinline__ void mx_unpack(const float4 x, const float4 y, float* q) {
   q[RHO] = x.x; q[MX] = x.y; q[MY] = x.z; q[MZ] = x.w; q[EN] = y.x; q[PR] = y.y; q[TT] = y.z;
   const float ir = 1.0f / x.x;
   q[VU] = x.y * ir; q[VV] = x.z * ir; q[VW] = x.w * ir;
@@ -132,60 +140,97 @@ __device__ __forceinline__ void mx_viscous(const float* q, const float* gm, cons
   v[3] = ex * nA[0] + ey * nA[1] + ez * nA[2];
 }
 
+template <int MCF>
+__device__ __forceinline__ void load_cface(const int* __restrict__ cf, int* e) {
+  if (MCF == 4) {
+    const int4 v = __ldg(reinterpret_cast<const int4*>(cf));
+    e[0] = v.x; e[1] = v.y; e[2] = v.z; e[3] = v.w;
+  } else if (MCF % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < MCF; k += 2) {
+      const int2 v = __ldg(reinterpret_cast<const int2*>(cf) + k / 2);
+      e[k] = v.x; e[k + 1] = v.y;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < MCF; ++k) e[k] = __ldg(cf + k);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // gradient pass
 // ---------------------------------------------------------------------------
-template <int GMODE, bool LINEAR, bool LIMIT, bool VISC>
+template <int MCF, int GMODE, bool LINEAR, bool LIMIT, bool VISC>
 __global__ void __launch_bounds__(256) k_mx_sides(const __grid_constant__ MxArgs a) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.nc) return;
   MxPhys ph;
   ph.load(a.pc);
+  const float4* Uf4 = reinterpret_cast<const float4*>(a.Uf);
   float q[10];
-  mx_load_state(a.Uf, c, q);
+  mx_unpack(__ldg(Uf4 + 2 * (size_t)c), __ldg(Uf4 + 2 * (size_t)c + 1), q);
+  int e[MCF];
+  load_cface<MCF>(a.cface + (size_t)c * MCF, e);
+  // neighbour cell (or -1 for a ghost) of every face, issued up front
+  int o[MCF];
+#pragma unroll
+  for (int k = 0; k < MCF; ++k) {
+    o[k] = -2;
+    if (e[k] >= 0) {
+      const int f = e[k] >> 1;
+      if (f < a.nf_int) {
+        const int2 fc = __ldg(&a.fcell[f]);
+        o[k] = (e[k] & 1) ? fc.x : fc.y;
+      } else {
+        o[k] = -1;
+      }
+    }
+  }
   float g[NG][3];
+#pragma unroll
+  for (int v = 0; v < NG; ++v) { g[v][0] = 0.f; g[v][1] = 0.f; g[v][2] = 0.f; }
   float mn[8], mxv[8];
 #pragma unroll
   for (int v = 0; v < 8; ++v) { mn[v] = q[v]; mxv[v] = q[v]; }
-  const int* cf = a.cface + (size_t)c * a.mcf;
   if (GMODE != 0) {
-    Acc<float, true> acc[NG][3];
-    for (int k = 0; k < a.mcf; ++k) {
-      const int e = cf[k];
-      if (e < 0) break;
-      const int f = e >> 1, side = e & 1;
+#pragma unroll
+    for (int k = 0; k < MCF; ++k) {
+      if (o[k] == -2) continue;
+      const int f = e[k] >> 1, side = e[k] & 1;
       const float4 nA = __ldg(&a.geoN[f]);
       float qo[10];
-      if (f >= a.nf_int) {
+      if (o[k] < 0) {
         const float n[3] = {nA.x, nA.y, nA.z};
         mx_ghost(q, a.fregion[f - a.nf_int], n, a.pc, ph, qo);
       } else {
-        const int2 fc = __ldg(&a.fcell[f]);
-        mx_load_state(a.Uf, side ? fc.x : fc.y, qo);
+        mx_unpack(__ldg(Uf4 + 2 * (size_t)o[k]), __ldg(Uf4 + 2 * (size_t)o[k] + 1), qo);
       }
       if (GMODE == 1) {
-        const float lam = __ldg(&a.geoD[(size_t)side * a.nf + f]).w;
-        const float sg = side ? -nA.w : nA.w;
-        const float ax = nA.x * sg, ay = nA.y * sg, az = nA.z * sg;
-        const float* q0 = side ? qo : q;
-        const float* q1 = side ? q : qo;
-#pragma unroll
-        for (int v = 0; v < NG; ++v) {
-          const int j = (v < 8) ? v : TT;
-          const float mean = q0[j] + lam * (q1[j] - q0[j]);
-          acc[v][0].add(mean * ax);
-          acc[v][1].add(mean * ay);
-          acc[v][2].add(mean * az);
-        }
-      } else {
-        const float4 w = __ldg(&a.lsqW[(size_t)side * a.nf + f]);
+        // Green-Gauss (reconstruction.c:43-71) in difference form:
+        // s_f mean_f nA_f = s_f q_c nA_f + s_f w_f (q_o - q_c) nA_f with
+        // w = lambda (cell 0 side) or 1 - lambda (cell 1 side); the q_c
+        // terms are added once per cell through sum_f s_f nA_f below
+        const float lam = __ldg(&a.geoD[f]).w;
+        const float w = side ? (nA.w - lam * nA.w) : lam * nA.w;
+        const float sw = side ? -w : w;
+        const float ax = nA.x * sw, ay = nA.y * sw, az = nA.z * sw;
 #pragma unroll
         for (int v = 0; v < NG; ++v) {
           const int j = (v < 8) ? v : TT;
           const float dq = qo[j] - q[j];
-          acc[v][0].add(w.x * dq);
-          acc[v][1].add(w.y * dq);
-          acc[v][2].add(w.z * dq);
+          g[v][0] += dq * ax;
+          g[v][1] += dq * ay;
+          g[v][2] += dq * az;
+        }
+      } else {
+        const float4 wl = __ldg(&a.lsqW[(size_t)side * a.nf + f]);
+#pragma unroll
+        for (int v = 0; v < NG; ++v) {
+          const int j = (v < 8) ? v : TT;
+          const float dq = qo[j] - q[j];
+          g[v][0] += wl.x * dq;
+          g[v][1] += wl.y * dq;
+          g[v][2] += wl.z * dq;
         }
       }
       if (LIMIT) {
@@ -193,20 +238,22 @@ __global__ void __launch_bounds__(256) k_mx_sides(const __grid_constant__ MxArgs
         for (int v = 0; v < 8; ++v) { mn[v] = fminf(mn[v], qo[v]); mxv[v] = fmaxf(mxv[v], qo[v]); }
       }
     }
-    const float s = (GMODE == 1) ? __ldg(&a.rvol[c]) : 1.0f;
+    if (GMODE == 1) {
+      const float4 cg = __ldg(&a.cgeo[c]);
 #pragma unroll
-    for (int v = 0; v < NG; ++v)
-#pragma unroll
-      for (int d = 0; d < 3; ++d) g[v][d] = acc[v][d].value() * s;
-  } else {
-#pragma unroll
-    for (int v = 0; v < NG; ++v) { g[v][0] = 0.f; g[v][1] = 0.f; g[v][2] = 0.f; }
+      for (int v = 0; v < NG; ++v) {
+        const int j = (v < 8) ? v : TT;
+        g[v][0] = (g[v][0] + q[j] * cg.x) * cg.w;
+        g[v][1] = (g[v][1] + q[j] * cg.y) * cg.w;
+        g[v][2] = (g[v][2] + q[j] * cg.z) * cg.w;
+      }
+    }
   }
   // per face side: limited reconstruction + viscous flux
-  for (int k = 0; k < a.mcf; ++k) {
-    const int e = cf[k];
-    if (e < 0) break;
-    const int f = e >> 1, side = e & 1;
+#pragma unroll
+  for (int k = 0; k < MCF; ++k) {
+    if (o[k] == -2) continue;
+    const int f = e[k] >> 1, side = e[k] & 1;
     const float4 nA4 = __ldg(&a.geoN[f]);
     const float nA[3] = {nA4.x * nA4.w, nA4.y * nA4.w, nA4.z * nA4.w};
     float r[12];
@@ -231,14 +278,16 @@ __global__ void __launch_bounds__(256) k_mx_sides(const __grid_constant__ MxArgs
         gm[d] = g[1][d]; gm[3 + d] = g[2][d]; gm[6 + d] = g[3][d]; gm[9 + d] = g[8][d];
       }
       mx_viscous(r, gm, nA, ph, &r[8]);
-    } else {
-      r[8] = r[9] = r[10] = r[11] = 0.f;
     }
-    float4* dst = reinterpret_cast<float4*>(a.fs + ((size_t)f * 2 + side) * FS);
-    dst[0] = make_float4(r[0], r[1], r[2], r[3]);
-    dst[1] = make_float4(r[4], r[5], r[6], r[7]);
-    dst[2] = make_float4(r[8], r[9], r[10], r[11]);
-    if (f >= a.nf_int) {
+    float4* rec = reinterpret_cast<float4*>(a.fs + (size_t)f * FREC);
+    rec[2 * side] = make_float4(r[0], r[1], r[2], r[3]);
+    if (VISC) {
+      rec[2 * side + 1] = make_float4(r[4], r[8], r[9], r[10]);
+      a.fs[(size_t)f * FREC + 16 + side] = r[11];
+    } else {
+      rec[2 * side + 1] = make_float4(r[4], 0.f, 0.f, 0.f);
+    }
+    if (o[k] == -1) {
       // ghost side: unlimited ghost of the cell-centre state
       // (reconstruction.c:249-253), gradient = interior gradient with the
       // normal part removed on slip walls / symmetry (boundary.c:377-405)
@@ -246,9 +295,7 @@ __global__ void __launch_bounds__(256) k_mx_sides(const __grid_constant__ MxArgs
       const float n[3] = {nA4.x, nA4.y, nA4.z};
       float gq[10];
       mx_ghost(q, region, n, a.pc, ph, gq);
-      float rg[12];
-#pragma unroll
-      for (int v = 0; v < 8; ++v) rg[v] = gq[v];
+      float vg[4] = {0.f, 0.f, 0.f, 0.f};
       if (VISC) {
         const int type = a.pc.region_type[region];
         if (type == BC_WALL_SLIP || type == BC_SYMMETRY) {
@@ -258,14 +305,11 @@ __global__ void __launch_bounds__(256) k_mx_sides(const __grid_constant__ MxArgs
             gm[3 * v] -= gn * n[0]; gm[3 * v + 1] -= gn * n[1]; gm[3 * v + 2] -= gn * n[2];
           }
         }
-        mx_viscous(rg, gm, nA, ph, &rg[8]);
-      } else {
-        rg[8] = rg[9] = rg[10] = rg[11] = 0.f;
+        mx_viscous(gq, gm, nA, ph, vg);
+        a.fs[(size_t)f * FREC + 17] = vg[3];
       }
-      float4* gd = reinterpret_cast<float4*>(a.fs + ((size_t)f * 2 + 1) * FS);
-      gd[0] = make_float4(rg[0], rg[1], rg[2], rg[3]);
-      gd[1] = make_float4(rg[4], rg[5], rg[6], rg[7]);
-      gd[2] = make_float4(rg[8], rg[9], rg[10], rg[11]);
+      rec[2] = make_float4(gq[0], gq[1], gq[2], gq[3]);
+      rec[3] = make_float4(gq[4], vg[0], vg[1], vg[2]);
     }
   }
 }
@@ -273,27 +317,27 @@ __global__ void __launch_bounds__(256) k_mx_sides(const __grid_constant__ MxArgs
 // ---------------------------------------------------------------------------
 // flux + update pass
 // ---------------------------------------------------------------------------
-// convective face flux in the global frame, times A
+// convective face flux in the global frame, times A.  l, r: (rho, m, E)
 __device__ __forceinline__ void mx_conv_flux(const float* l, const float* r, const float4 nA,
                                              const MxPhys& ph, float* F) {
   const float n0 = nA.x, n1 = nA.y, n2 = nA.z, A = nA.w;
   // primitives of the (reconstructed) conserved states (eos.c:81-92)
-  const float irl = 1.f / l[RHO], irr = 1.f / r[RHO];
-  const float ul = l[MX] * irl, vl = l[MY] * irl, wl = l[MZ] * irl;
-  const float ur = r[MX] * irr, vr = r[MY] * irr, wr = r[MZ] * irr;
-  const float pl = fmaxf(1.00E-10f, ph.km1 * (l[EN] - 0.5f * (l[MX] * ul + l[MY] * vl + l[MZ] * wl)));
-  const float pr = fmaxf(1.00E-10f, ph.km1 * (r[EN] - 0.5f * (r[MX] * ur + r[MY] * vr + r[MZ] * wr)));
+  const float irl = 1.f / l[0], irr = 1.f / r[0];
+  const float ul = l[1] * irl, vl = l[2] * irl, wl = l[3] * irl;
+  const float ur = r[1] * irr, vr = r[2] * irr, wr = r[3] * irr;
+  const float pl = fmaxf(1.00E-10f, ph.km1 * (l[4] - 0.5f * (l[1] * ul + l[2] * vl + l[3] * wl)));
+  const float pr = fmaxf(1.00E-10f, ph.km1 * (r[4] - 0.5f * (r[1] * ur + r[2] * vr + r[3] * wr)));
   const float unl = ul * n0 + vl * n1 + wl * n2;
   const float unr = ur * n0 + vr * n1 + wr * n2;
   const float cl = sqrtf(ph.kappa * pl * irl), cr = sqrtf(ph.kappa * pr * irr);
   if (ph.flux == 1) {  // Rusanov, flux.c:320-336
     const float lam = fmaxf(fabsf(unl) + cl, fabsf(unr) + cr);
-    const float ml = l[RHO] * unl, mr = r[RHO] * unr;
-    F[0] = 0.5f * (ml + mr) - 0.5f * lam * (r[RHO] - l[RHO]);
-    F[1] = 0.5f * (l[MX] * unl + pl * n0 + r[MX] * unr + pr * n0) - 0.5f * lam * (r[MX] - l[MX]);
-    F[2] = 0.5f * (l[MY] * unl + pl * n1 + r[MY] * unr + pr * n1) - 0.5f * lam * (r[MY] - l[MY]);
-    F[3] = 0.5f * (l[MZ] * unl + pl * n2 + r[MZ] * unr + pr * n2) - 0.5f * lam * (r[MZ] - l[MZ]);
-    F[4] = 0.5f * ((l[EN] + pl) * unl + (r[EN] + pr) * unr) - 0.5f * lam * (r[EN] - l[EN]);
+    const float ml = l[0] * unl, mr = r[0] * unr;
+    F[0] = 0.5f * (ml + mr) - 0.5f * lam * (r[0] - l[0]);
+    F[1] = 0.5f * (l[1] * unl + pl * n0 + r[1] * unr + pr * n0) - 0.5f * lam * (r[1] - l[1]);
+    F[2] = 0.5f * (l[2] * unl + pl * n1 + r[2] * unr + pr * n1) - 0.5f * lam * (r[2] - l[2]);
+    F[3] = 0.5f * (l[3] * unl + pl * n2 + r[3] * unr + pr * n2) - 0.5f * lam * (r[3] - l[3]);
+    F[4] = 0.5f * ((l[4] + pl) * unl + (r[4] + pr) * unr) - 0.5f * lam * (r[4] - l[4]);
   } else {  // AUSM, flux.c:344-406
     const float Ml = unl / cl, Mr = unr / cr;
     float mp, pp, mm, pm;
@@ -303,20 +347,32 @@ __device__ __forceinline__ void mx_conv_flux(const float* l, const float* r, con
     if (Mr <= -1.f) { mm = Mr; pm = pr; }
     else if (Mr < 1.f) { mm = -0.25f * (Mr - 1.f) * (Mr - 1.f); pm = 0.25f * pr * (1.f - Mr) * (1.f - Mr) * (2.f + Mr); }
     else { mm = 0.f; pm = 0.f; }
-    const float mdl = fmaxf(0.f, mp + mm) * cl * l[RHO];
-    const float mdr = fminf(0.f, mp + mm) * cr * r[RHO];
+    const float mdl = fmaxf(0.f, mp + mm) * cl * l[0];
+    const float mdr = fminf(0.f, mp + mm) * cr * r[0];
     const float P = pp + pm;
     F[0] = mdl + mdr;
     F[1] = mdl * ul + mdr * ur + P * n0;
     F[2] = mdl * vl + mdr * vr + P * n1;
     F[3] = mdl * wl + mdr * wr + P * n2;
-    F[4] = mdl * (l[EN] + pl) * irl + mdr * (r[EN] + pr) * irr;
+    F[4] = mdl * (l[4] + pl) * irl + mdr * (r[4] + pr) * irr;
   }
 #pragma unroll
   for (int j = 0; j < 5; ++j) F[j] *= A;
 }
 
-template <int MODE, bool DT, bool VISC>
+// FP32 stage state record from conserved floats
+__device__ __forceinline__ void mx_store_state(float4* dst, float rho, float mx, float my, float mz,
+                                               float E, const MxPhys& ph) {
+  const float ir = 1.f / rho;
+  const float ke = 0.5f * (mx * mx + my * my + mz * mz) * ir;
+  const float p = fmaxf(1.00E-10f, ph.km1 * (E - ke));
+  dst[0] = make_float4(rho, mx, my, mz);
+  dst[1] = make_float4(E, p, p * ir / ph.R, 0.f);
+}
+
+// MODE 0: residual only; 1: low-storage RK stage; 2: SSP-RK3 stage.
+// co.first / co.last mark the step's first and last stage.
+template <int MCF, int MODE, bool DT, bool VISC>
 __global__ void __launch_bounds__(256) k_mx_flux_update(const __grid_constant__ MxArgs a,
                                                         StageCoef co) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -325,28 +381,26 @@ __global__ void __launch_bounds__(256) k_mx_flux_update(const __grid_constant__ 
   if (c < a.nc) {
     MxPhys ph;
     ph.load(a.pc);
+    int e[MCF];
+    load_cface<MCF>(a.cface + (size_t)c * MCF, e);
     Acc<float, true> s[5];
-    const int* cf = a.cface + (size_t)c * a.mcf;
-    for (int k = 0; k < a.mcf; ++k) {
-      const int e = cf[k];
-      if (e < 0) break;
-      const int f = e >> 1, side = e & 1;
-      const float4* src = reinterpret_cast<const float4*>(a.fs + (size_t)f * 2 * FS);
-      float l[12], r[12];
-      float4 t;
-      t = __ldg(src + 0); l[0] = t.x; l[1] = t.y; l[2] = t.z; l[3] = t.w;
-      t = __ldg(src + 1); l[4] = t.x; l[5] = t.y; l[6] = t.z; l[7] = t.w;
-      t = __ldg(src + 3); r[0] = t.x; r[1] = t.y; r[2] = t.z; r[3] = t.w;
-      t = __ldg(src + 4); r[4] = t.x; r[5] = t.y; r[6] = t.z; r[7] = t.w;
+#pragma unroll
+    for (int k = 0; k < MCF; ++k) {
+      if (e[k] < 0) continue;
+      const int f = e[k] >> 1, side = e[k] & 1;
+      const float4* src = reinterpret_cast<const float4*>(a.fs + (size_t)f * FREC);
+      const float4 l0 = __ldg(src + 0), l1 = __ldg(src + 1), r0 = __ldg(src + 2), r1 = __ldg(src + 3);
+      const float l[5] = {l0.x, l0.y, l0.z, l0.w, l1.x};
+      const float r[5] = {r0.x, r0.y, r0.z, r0.w, r1.x};
       const float4 nA = __ldg(&a.geoN[f]);
       float F[5];
       mx_conv_flux(l, r, nA, ph, F);
       if (VISC) {
-        const float4 vl = __ldg(src + 2), vr = __ldg(src + 5);
-        F[1] += 0.5f * (vl.x + vr.x);
-        F[2] += 0.5f * (vl.y + vr.y);
-        F[3] += 0.5f * (vl.z + vr.z);
-        F[4] += 0.5f * (vl.w + vr.w);
+        const float2 ve = __ldg(reinterpret_cast<const float2*>(src + 4));
+        F[1] += 0.5f * (l1.y + r1.y);
+        F[2] += 0.5f * (l1.z + r1.z);
+        F[3] += 0.5f * (l1.w + r1.w);
+        F[4] += 0.5f * (ve.x + ve.y);
       }
 #pragma unroll
       for (int j = 0; j < 5; ++j) {
@@ -354,62 +408,78 @@ __global__ void __launch_bounds__(256) k_mx_flux_update(const __grid_constant__ 
         else s[j].add(F[j]);
       }
     }
-    const float rv = __ldg(&a.rvol[c]);
-    double rr[5];
+    const float rv = __ldg(&a.cgeo[c]).w;
+    float rr[5];
 #pragma unroll
-    for (int j = 0; j < 5; ++j) rr[j] = (double)(-s[j].value() * rv);
+    for (int j = 0; j < 5; ++j) rr[j] = -s[j].value() * rv;
     if (MODE == 0) {
 #pragma unroll
-      for (int j = 0; j < 5; ++j) a.dphi[(size_t)j * a.nc + c] = rr[j];
+      for (int j = 0; j < 5; ++j) a.dphi[(size_t)j * a.nc + c] = (double)rr[j];
     } else {
       const double dt = a.sc->dt;
-      const double dtg = dt * co.g;
-      double u[5];
+      float du[5];
+      if (MODE == 1) {
+        const float gdt = (float)(dt * co.g);
 #pragma unroll
-      for (int j = 0; j < 5; ++j) {
-        const size_t i = (size_t)j * a.nc + c;
-        double uj = a.U[i];
-        if (MODE == 1) {
-          const double kj = co.first ? rr[j] : fma(a.K[i], co.a, rr[j]);
-          a.K[i] = kj;
-          uj = fma(kj, dtg, uj);
-        } else {
-          if (co.first) {
-            a.U0[i] = uj;
-            uj = fma(dt, rr[j], uj);
-          } else {
-            uj = co.c0 * a.U0[i] + co.c1 * fma(dt, rr[j], uj);
-          }
+        for (int j = 0; j < 5; ++j) {
+          const size_t i = (size_t)j * a.nc + c;
+          const float kj = co.first ? rr[j] : fmaf(a.kf[i], (float)co.a, rr[j]);
+          if (!co.last) a.kf[i] = kj;
+          du[j] = co.first ? gdt * kj : fmaf(gdt, kj, a.dU[i]);
         }
-        a.U[i] = uj;
-        u[j] = uj;
-        finite = finite && isfinite(uj);
+      } else {
+        const float fdt = (float)dt, c1 = (float)co.c1;
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+          const size_t i = (size_t)j * a.nc + c;
+          du[j] = co.first ? fdt * rr[j] : c1 * fmaf(fdt, rr[j], a.dU[i]);
+        }
       }
       float4* sh = reinterpret_cast<float4*>(a.Uf) + 2 * (size_t)c;
-      const float4 o0 = sh[0], o1 = sh[1];
-      const float rho = (float)u[0], mx = (float)u[1], my = (float)u[2], mz = (float)u[3];
-      const float ir = 1.f / rho;
-      const float vx = mx * ir, vy = my * ir, vz = mz * ir;
-      const float ke = 0.5f * (mx * vx + my * vy + mz * vz);
-      float p = (float)(a.pc.km1 * (u[4] - (double)ke));
-      p = fmaxf(1.00E-10f, p);
-      const float T = p * ir / ph.R;
-      sh[0] = make_float4(rho, mx, my, mz);
-      sh[1] = make_float4((float)u[4], p, T, 0.f);
+      float4 o0 = make_float4(0.f, 0.f, 0.f, 0.f), o1 = o0;
+      if (DT && MODE == 1) { o0 = sh[0]; o1 = sh[1]; }  // stage-input state
+      float un[5];
+      if (co.last) {
+        // end of step: U_{n+1} = U_n + dU in FP64, new base record
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+          const size_t i = (size_t)j * a.nc + c;
+          const double uj = a.U[i] + (double)du[j];
+          a.U[i] = uj;
+          un[j] = (float)uj;
+          finite = finite && isfinite(uj);
+        }
+        float4* base = reinterpret_cast<float4*>(a.UfN) + 2 * (size_t)c;
+        mx_store_state(base, un[0], un[1], un[2], un[3], un[4], ph);
+        sh[0] = base[0];
+        sh[1] = base[1];
+      } else {
+        const float4* base = reinterpret_cast<const float4*>(a.UfN) + 2 * (size_t)c;
+        const float4 b0 = base[0], b1 = base[1];
+        un[0] = b0.x + du[0]; un[1] = b0.y + du[1]; un[2] = b0.z + du[2]; un[3] = b0.w + du[3];
+        un[4] = b1.x + du[4];
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+          a.dU[(size_t)j * a.nc + c] = du[j];
+          finite = finite && isfinite(du[j]);
+        }
+        mx_store_state(sh, un[0], un[1], un[2], un[3], un[4], ph);
+      }
       if (DT) {
         // calc_ns_timestep on the reference's phi_total: new density, the
         // stage-input u, v, w, p for the low-storage schemes (see
         // k_gather_update); new state for SSP-RK3
-        float pu = vx, pv = vy, pw = vz, pp = p;
+        const float ir = 1.f / un[0];
+        float pu = un[1] * ir, pv = un[2] * ir, pw = un[3] * ir;
+        float pp = fmaxf(1.00E-10f, ph.km1 * (un[4] - 0.5f * (un[1] * pu + un[2] * pv + un[3] * pw)));
         if (MODE == 1) {
           const float io = 1.f / o0.x;
           pu = o0.y * io; pv = o0.z * io; pw = o0.w * io; pp = o1.y;
         }
         const float cs = sqrtf(ph.kappa * pp * ir);
-        const double* d = a.dx + 3 * (size_t)c;
-        const float ds = (fabsf(pu) + cs) * (float)d[0] + (fabsf(pv) + cs) * (float)d[1] +
-                         (fabsf(pw) + cs) * (float)d[2];
-        const double lam = (double)((float)a.vol[c] / ds);
+        const float4 dxv = __ldg(&a.cdx[c]);
+        const float ds = (fabsf(pu) + cs) * dxv.x + (fabsf(pv) + cs) * dxv.y + (fabsf(pw) + cs) * dxv.z;
+        const double lam = (double)(dxv.w / ds);
         if (lam > 0.0) lam_bits = (unsigned long long)__double_as_longlong(lam);
       }
     }

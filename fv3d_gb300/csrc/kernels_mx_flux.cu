@@ -1,0 +1,32 @@
+// Mixed-precision explicit-stage launchers (flux + update pass).
+#include "kernels_mixed.cuh"
+#include "launch.h"
+
+namespace fv3d {
+
+template <int MCF>
+static void flux_mcf(const MxArgs& a, const Disc& d, int mode, bool dt, const StageCoef& co,
+                     cudaStream_t s, int B) {
+#define MX_FU(M, D, V) k_mx_flux_update<MCF, M, D, V><<<B, 256, 0, s>>>(a, co)
+  if (mode == 0) { if (d.viscous) MX_FU(0, false, true); else MX_FU(0, false, false); }
+  else if (mode == 1) {
+    if (dt) { if (d.viscous) MX_FU(1, true, true); else MX_FU(1, true, false); }
+    else { if (d.viscous) MX_FU(1, false, true); else MX_FU(1, false, false); }
+  } else {
+    if (dt) { if (d.viscous) MX_FU(2, true, true); else MX_FU(2, true, false); }
+    else { if (d.viscous) MX_FU(2, false, true); else MX_FU(2, false, false); }
+  }
+#undef MX_FU
+}
+
+cudaError_t launch_mx_flux_update(const MxArgs& a, const Disc& d, int mode, bool dt,
+                                  const StageCoef& co, cudaStream_t s) {
+  const int B = (a.nc + 255) / 256;
+  if (a.mcf == 4) flux_mcf<4>(a, d, mode, dt, co, s, B);
+  else if (a.mcf == 6) flux_mcf<6>(a, d, mode, dt, co, s, B);
+  else if (a.mcf == 8) flux_mcf<8>(a, d, mode, dt, co, s, B);
+  else return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+}  // namespace fv3d

@@ -218,8 +218,12 @@ fv3d_status prepare_mesh(Ctx& ctx, const fv3d_mesh_arrays& m) {
       d2[3 * (size_t)nfid + d] = g[G_D2 + d];
     }
   }
-  // cell face lists: entries (new face << 1) | side, ascending reference id
-  ctx.h_cface.assign((size_t)nc * mcf, -1);
+  // cell face lists: entries (new face << 1) | side, ascending reference id;
+  // the stride is padded to 4, 6 or 8 (the face-count variants the kernels
+  // are compiled for)
+  const int mcf_pad = (mcf <= 4) ? 4 : (mcf <= 6 ? 6 : 8);
+  ctx.mcf = mcf_pad;
+  ctx.h_cface.assign((size_t)nc * mcf_pad, -1);
   ctx.h_vol.assign(nc, 0.0);
   ctx.h_dx.assign((size_t)nc * 3, 0.0);
   ctx.vol_total = 0.0;
@@ -232,7 +236,7 @@ fv3d_status prepare_mesh(Ctx& ctx, const fv3d_mesh_arrays& m) {
     for (size_t k = 0; k < fl.size(); ++k) {
       const int f = fl[k];
       const int side = (m.face_cells[2 * f] == old) ? 0 : 1;
-      ctx.h_cface[(size_t)c * mcf + k] = (ifperm[f] << 1) | side;
+      ctx.h_cface[(size_t)c * mcf_pad + k] = (ifperm[f] << 1) | side;
     }
     ctx.h_vol[c] = m.cell_volume[old];
     for (int d = 0; d < 3; ++d) ctx.h_dx[3 * (size_t)c + d] = m.cell_dx[3 * old + d];
@@ -245,8 +249,8 @@ fv3d_status prepare_mesh(Ctx& ctx, const fv3d_mesh_arrays& m) {
       double M[6] = {0, 0, 0, 0, 0, 0};
       double dv[8][3];
       int nfc = 0;
-      for (int k = 0; k < mcf; ++k) {
-        int e = ctx.h_cface[(size_t)c * mcf + k];
+      for (int k = 0; k < mcf_pad; ++k) {
+        int e = ctx.h_cface[(size_t)c * mcf_pad + k];
         if (e < 0) break;
         int f = e >> 1, side = e & 1;
         for (int q = 0; q < 3; ++q) {
@@ -273,7 +277,7 @@ fv3d_status prepare_mesh(Ctx& ctx, const fv3d_mesh_arrays& m) {
       if (!(std::fabs(det) > 0.0)) return ctx.fail(FV3D_ERR_INVALID_ARG, "cell %d: singular least-squares matrix", order[c]);
       double s = 1.0 / det;
       for (int k = 0; k < nfc; ++k) {
-        int e = ctx.h_cface[(size_t)c * mcf + k];
+        int e = ctx.h_cface[(size_t)c * mcf_pad + k];
         int f = e >> 1, side = e & 1;
         double* w = &ctx.h_lsq[6 * (size_t)f + 3 * side];
         w[0] = s * (c00 * dv[k][0] + c01 * dv[k][1] + c02 * dv[k][2]);
@@ -308,7 +312,7 @@ fv3d_status upload_mesh(Ctx& ctx) {
   UP(ctx.d_fc0, ctx.h_fc0.data(), (size_t)nf);
   UP(ctx.d_fc1, ctx.h_fc1.data(), (size_t)nf);
   if (ctx.nb > 0) UP(ctx.d_fregion, ctx.h_fregion.data(), (size_t)ctx.nb);
-  UP(ctx.d_cface, ctx.h_cface.data(), (size_t)nc * ctx.mcf);
+  UP(ctx.d_cface, ctx.h_cface.data(), (size_t)nc * ctx.mcf);  // ctx.mcf = padded stride
   std::vector<double> rvol(nc);
   for (int i = 0; i < nc; ++i) rvol[i] = 1.0 / ctx.h_vol[i];  // s_volume (reconstruction.c:82)
   auto up_r = [&](DevBuf<char>& b, const std::vector<double>& src) -> fv3d_status {
@@ -349,11 +353,32 @@ fv3d_status upload_mesh(Ctx& ctx) {
       lw[f] = make_float4((float)w[0], (float)w[1], (float)w[2], 0.f);
       lw[(size_t)nf + f] = make_float4((float)w[3], (float)w[4], (float)w[5], 0.f);
     }
+    // per cell: sum_f s_f n_f A_f (closure of the Green-Gauss difference
+    // form) with 1/V, and (dx, V) for the time step
+    std::vector<float4> cg(nc), cd(nc);
+    for (int c = 0; c < nc; ++c) {
+      double S[3] = {0.0, 0.0, 0.0};
+      for (int k = 0; k < ctx.mcf; ++k) {
+        const int e = ctx.h_cface[(size_t)c * ctx.mcf + k];
+        if (e < 0) break;
+        const double* g = &ctx.h_geo[(size_t)(e >> 1) * GEO];
+        const double sg = (e & 1) ? -g[G_A] : g[G_A];
+        for (int d = 0; d < 3; ++d) S[d] += sg * g[G_N + d];
+      }
+      cg[c] = make_float4((float)S[0], (float)S[1], (float)S[2], (float)(1.0 / ctx.h_vol[c]));
+      cd[c] = make_float4((float)ctx.h_dx[3 * (size_t)c], (float)ctx.h_dx[3 * (size_t)c + 1],
+                          (float)ctx.h_dx[3 * (size_t)c + 2], (float)ctx.h_vol[c]);
+    }
+    UP(ctx.d_cgeo, cg.data(), (size_t)nc);
+    UP(ctx.d_cdx, cd.data(), (size_t)nc);
+    ALLOC(ctx.d_UfN, (size_t)nc * 8);
+    ALLOC(ctx.d_kf, (size_t)nc * 5);
+    ALLOC(ctx.d_dU, (size_t)nc * 5);
     UP(ctx.d_fcell, fcell.data(), (size_t)nf);
     UP(ctx.d_geoN, gN.data(), (size_t)nf);
     UP(ctx.d_geoD, gD.data(), 2 * (size_t)nf);
     UP(ctx.d_lsqW, lw.data(), 2 * (size_t)nf);
-    ALLOC(ctx.d_fs, (size_t)nf * 2 * FS);
+    ALLOC(ctx.d_fs, (size_t)nf * FREC);
   }
   ALLOC(ctx.d_sc, 1);
   ALLOC(ctx.d_bits, 2);

@@ -227,7 +227,7 @@ MxArgs Ctx::mx_args() const {
   MxArgs a;
   memset(&a, 0, sizeof(a));
   a.nc = nc; a.nf = nf; a.nf_int = nf_int; a.mcf = mcf;
-  a.cface = d_cface.p; a.fcell = d_fcell.p; a.geoN = d_geoN.p; a.geoD = d_geoD.p;
+  a.cface = d_cface.p; a.cnbr = d_cnbr.p; a.fcell = d_fcell.p; a.geoN = d_geoN.p; a.geoD = d_geoD.p;
   a.lsqW = d_lsqW.p; a.fregion = d_fregion.p; a.cgeo = d_cgeo.p; a.cdx = d_cdx.p;
   a.Uf = d_Uf.p; a.UfN = d_UfN.p; a.fs = d_fs.p;
   a.U = d_U.p; a.kf = d_kf.p; a.dU = d_dU.p; a.dphi = d_dphi.p; a.sc = d_sc.p;
@@ -304,6 +304,9 @@ extern "C" fv3d_status fv3d_create(const fv3d_config* config, fv3d_ctx** out) {
   double cp = c.kappa * cv;
   p.heat_lambda = c.mu_mix * cp / c.Pr;
   p.flux = c.flux_scheme;
+  p.f32[0] = (float)p.kappa; p.f32[1] = (float)p.km1; p.f32[2] = (float)p.s_km1;
+  p.f32[3] = (float)p.s_kp1; p.f32[4] = (float)p.R_mix; p.f32[5] = (float)p.mu;
+  p.f32[6] = (float)p.heat_lambda; p.f32[7] = 0.f;
   ctx->kappa_pr = c.kappa / c.Pr;
   *out = reinterpret_cast<fv3d_ctx*>(ctx);
   return FV3D_OK;
@@ -390,6 +393,7 @@ extern "C" fv3d_status fv3d_set_region(fv3d_ctx* handle, int region, int type, c
   ke += q[6] * q[2];
   ke += q[7] * q[3];
   q[4] = p.s_km1 * q[8] + 0.5 * ke;
+  for (int j = 0; j < 10; ++j) p.region_phi_f[region][j] = (float)q[j];
   p.n_regions = std::max(p.n_regions, region + 1);
   ctx->region_set |= 1u << region;
   ctx->release_graphs();  // physics constants are baked into captured graphs

@@ -33,6 +33,12 @@
 
 namespace fv3d {
 
+// minimum resident blocks of 256 threads for the gradient pass (a register
+// cap; 2 keeps it spill-free)
+#ifndef FV3D_SIDES_MINBLOCKS
+#define FV3D_SIDES_MINBLOCKS 2
+#endif
+
 // face record: side s at float4 [2s, 2s+1] = (rho, mx, my, mz), (E, vmx, vmy, vmz);
 // float4 [4] = (ve side 0, ve side 1, -, -).  v* = viscous normal flux times A.
 constexpr int FREC = 20;
@@ -40,6 +46,7 @@ constexpr int FREC = 20;
 struct MxArgs {
   int nc, nf, nf_int, mcf;
   const int* __restrict__ cface;     // [nc][mcf]
+  const int* __restrict__ cnbr;      // [nc][mcf] neighbour cell, -1 ghost, -2 none
   const int2* __restrict__ fcell;    // [nf] (cell 0, cell 1 or ghost)
   const float4* __restrict__ geoN;   // [nf] (n, A)
   const float4* __restrict__ geoD;   // [2][nf] (d_side, lambda)
@@ -62,8 +69,8 @@ struct MxPhys {
   float kappa, km1, s_km1, s_kp1, R, mu, heat;
   int flux;
   __device__ __forceinline__ void load(const PhysConst& c) {
-    kappa = (float)c.kappa; km1 = (float)c.km1; s_km1 = (float)c.s_km1; s_kp1 = (float)c.s_kp1;
-    R = (float)c.R_mix; mu = (float)c.mu; heat = (float)c.heat_lambda; flux = c.flux;
+    kappa = c.f32[0]; km1 = c.f32[1]; s_km1 = c.f32[2]; s_kp1 = c.f32[3];
+    R = c.f32[4]; mu = c.f32[5]; heat = c.f32[6]; flux = c.flux;
   }
 };
 
@@ -92,9 +99,9 @@ __device__ __forceinline__ void mx_ghost(const float* in, int region, const floa
   const int type = pc.region_type[region];
   if (type == BC_INFLOW || type == BC_STATE) {
 #pragma unroll
-    for (int j = 0; j < 10; ++j) g[j] = (float)pc.region_phi[region][j];
+    for (int j = 0; j < 10; ++j) g[j] = pc.region_phi_f[region][j];
   } else if (type == BC_PRESSURE_OUTLET) {
-    g[PR] = (float)pc.region_phi[region][PR];
+    g[PR] = pc.region_phi_f[region][PR];
     g[TT] = g[PR] / (g[RHO] * ph.R);
   } else if (type == BC_WALL_ADIABATIC || type == BC_WALL_ISOTHERMAL || type == BC_WALL_SLIP ||
              type == BC_SYMMETRY) {
@@ -107,7 +114,7 @@ __device__ __forceinline__ void mx_ghost(const float* in, int region, const floa
       g[TT] = g[PR] / (g[RHO] * ph.R);
     } else {
       g[VU] = 0.f; g[VV] = 0.f; g[VW] = 0.f;
-      if (type == BC_WALL_ISOTHERMAL) g[TT] = (float)pc.region_phi[region][TT];
+      if (type == BC_WALL_ISOTHERMAL) g[TT] = pc.region_phi_f[region][TT];
       g[RHO] = g[PR] / (ph.R * g[TT]);
     }
   }
@@ -118,25 +125,32 @@ __device__ __forceinline__ void mx_ghost(const float* in, int region, const floa
   g[EN] = ph.s_km1 * g[PR] + 0.5f * (g[VU] * g[MX] + g[VV] * g[MY] + g[VW] * g[MZ]);
 }
 
-// viscous normal flux of one side times the area: F_visc . (n A) for the
-// momentum and energy rows (flux.c:215-263; stresses from the conserved
-// momentum gradients as in the reference).  gm[v*3+d], v: rho_u, rho_v, rho_w, T.
-__device__ __forceinline__ void mx_viscous(const float* q, const float* gm, const float* nA,
-                                           const MxPhys& ph, float* v) {
+// Viscous stresses of a cell (flux.c:223-238: from the gradients of the
+// conserved momenta, as the reference computes them).  gm[v*3+d], v: rho_u,
+// rho_v, rho_w, T.  tau = (xx, yy, zz, xy, xz, yz).
+__device__ __forceinline__ void mx_stress(const float* gm, const MxPhys& ph, float* tau) {
   const float s23 = 2.0f / 3.0f, s43 = 4.0f / 3.0f, mu = ph.mu;
-  const float txx = mu * (s43 * gm[0] - s23 * gm[4] - s23 * gm[8]);
-  const float tyy = mu * (-s23 * gm[0] + s43 * gm[4] - s23 * gm[8]);
-  const float tzz = mu * (-s23 * gm[0] - s23 * gm[4] + s43 * gm[8]);
-  const float txy = mu * (gm[1] + gm[3]);
-  const float txz = mu * (gm[2] + gm[6]);
-  const float tyz = mu * (gm[5] + gm[7]);
+  tau[0] = mu * (s43 * gm[0] - s23 * gm[4] - s23 * gm[8]);
+  tau[1] = mu * (-s23 * gm[0] + s43 * gm[4] - s23 * gm[8]);
+  tau[2] = mu * (-s23 * gm[0] - s23 * gm[4] + s43 * gm[8]);
+  tau[3] = mu * (gm[1] + gm[3]);
+  tau[4] = mu * (gm[2] + gm[6]);
+  tau[5] = mu * (gm[5] + gm[7]);
+}
+
+// viscous normal flux of one side times the area: F_visc . (n A) for the
+// momentum and energy rows (flux.c:240-262) with the side's reconstructed
+// velocity q[VU..VW] and heat flux k grad T (gT).
+__device__ __forceinline__ void mx_viscous(const float* q, const float* tau, const float* gT,
+                                           const float* nA, const MxPhys& ph, float* v) {
+  const float txx = tau[0], tyy = tau[1], tzz = tau[2], txy = tau[3], txz = tau[4], tyz = tau[5];
   const float k = ph.heat;
   v[0] = -(txx * nA[0] + txy * nA[1] + txz * nA[2]);
   v[1] = -(txy * nA[0] + tyy * nA[1] + tyz * nA[2]);
   v[2] = -(txz * nA[0] + tyz * nA[1] + tzz * nA[2]);
-  const float ex = -txx * q[VU] - txy * q[VV] - txz * q[VW] - k * gm[9];
-  const float ey = -txy * q[VU] - tyy * q[VV] - tyz * q[VW] - k * gm[10];
-  const float ez = -txz * q[VU] - tyz * q[VV] - tzz * q[VW] - k * gm[11];
+  const float ex = -txx * q[VU] - txy * q[VV] - txz * q[VW] - k * gT[0];
+  const float ey = -txy * q[VU] - tyy * q[VV] - tyz * q[VW] - k * gT[1];
+  const float ez = -txz * q[VU] - tyz * q[VV] - tzz * q[VW] - k * gT[2];
   v[3] = ex * nA[0] + ey * nA[1] + ez * nA[2];
 }
 
@@ -161,7 +175,7 @@ __device__ __forceinline__ void load_cface(const int* __restrict__ cf, int* e) {
 // gradient pass
 // ---------------------------------------------------------------------------
 template <int MCF, int GMODE, bool LINEAR, bool LIMIT, bool VISC>
-__global__ void __launch_bounds__(256) k_mx_sides(const __grid_constant__ MxArgs a) {
+__global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __grid_constant__ MxArgs a) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.nc) return;
   MxPhys ph;
@@ -169,23 +183,9 @@ __global__ void __launch_bounds__(256) k_mx_sides(const __grid_constant__ MxArgs
   const float4* Uf4 = reinterpret_cast<const float4*>(a.Uf);
   float q[10];
   mx_unpack(__ldg(Uf4 + 2 * (size_t)c), __ldg(Uf4 + 2 * (size_t)c + 1), q);
-  int e[MCF];
+  int e[MCF], o[MCF];
   load_cface<MCF>(a.cface + (size_t)c * MCF, e);
-  // neighbour cell (or -1 for a ghost) of every face, issued up front
-  int o[MCF];
-#pragma unroll
-  for (int k = 0; k < MCF; ++k) {
-    o[k] = -2;
-    if (e[k] >= 0) {
-      const int f = e[k] >> 1;
-      if (f < a.nf_int) {
-        const int2 fc = __ldg(&a.fcell[f]);
-        o[k] = (e[k] & 1) ? fc.x : fc.y;
-      } else {
-        o[k] = -1;
-      }
-    }
-  }
+  load_cface<MCF>(a.cnbr + (size_t)c * MCF, o);  // neighbour cell, -1 ghost, -2 none
   float g[NG][3];
 #pragma unroll
   for (int v = 0; v < NG; ++v) { g[v][0] = 0.f; g[v][1] = 0.f; g[v][2] = 0.f; }
@@ -249,6 +249,15 @@ __global__ void __launch_bounds__(256) k_mx_sides(const __grid_constant__ MxArgs
       }
     }
   }
+  float tau[6];
+  if (VISC) {
+    float gm[12];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      gm[d] = g[1][d]; gm[3 + d] = g[2][d]; gm[6 + d] = g[3][d]; gm[9 + d] = g[8][d];
+    }
+    mx_stress(gm, ph, tau);
+  }
   // per face side: limited reconstruction + viscous flux
 #pragma unroll
   for (int k = 0; k < MCF; ++k) {
@@ -271,14 +280,7 @@ __global__ void __launch_bounds__(256) k_mx_sides(const __grid_constant__ MxArgs
 #pragma unroll
       for (int v = 0; v < 8; ++v) r[v] = q[v];
     }
-    float gm[12];
-    if (VISC) {
-#pragma unroll
-      for (int d = 0; d < 3; ++d) {
-        gm[d] = g[1][d]; gm[3 + d] = g[2][d]; gm[6 + d] = g[3][d]; gm[9 + d] = g[8][d];
-      }
-      mx_viscous(r, gm, nA, ph, &r[8]);
-    }
+    if (VISC) mx_viscous(r, tau, g[8], nA, ph, &r[8]);
     float4* rec = reinterpret_cast<float4*>(a.fs + (size_t)f * FREC);
     rec[2 * side] = make_float4(r[0], r[1], r[2], r[3]);
     if (VISC) {
@@ -298,14 +300,25 @@ __global__ void __launch_bounds__(256) k_mx_sides(const __grid_constant__ MxArgs
       float vg[4] = {0.f, 0.f, 0.f, 0.f};
       if (VISC) {
         const int type = a.pc.region_type[region];
+        float tg[6], gT[3] = {g[8][0], g[8][1], g[8][2]};
+#pragma unroll
+        for (int j = 0; j < 6; ++j) tg[j] = tau[j];
         if (type == BC_WALL_SLIP || type == BC_SYMMETRY) {
+          // ghost gradient without its normal part (boundary.c:377-405)
+          float gm[12];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            gm[d] = g[1][d]; gm[3 + d] = g[2][d]; gm[6 + d] = g[3][d]; gm[9 + d] = g[8][d];
+          }
 #pragma unroll
           for (int v = 0; v < 4; ++v) {
             const float gn = gm[3 * v] * n[0] + gm[3 * v + 1] * n[1] + gm[3 * v + 2] * n[2];
             gm[3 * v] -= gn * n[0]; gm[3 * v + 1] -= gn * n[1]; gm[3 * v + 2] -= gn * n[2];
           }
+          mx_stress(gm, ph, tg);
+          gT[0] = gm[9]; gT[1] = gm[10]; gT[2] = gm[11];
         }
-        mx_viscous(gq, gm, nA, ph, vg);
+        mx_viscous(gq, tg, gT, nA, ph, vg);
         a.fs[(size_t)f * FREC + 17] = vg[3];
       }
       rec[2] = make_float4(gq[0], gq[1], gq[2], gq[3]);
@@ -372,28 +385,29 @@ __device__ __forceinline__ void mx_store_state(float4* dst, float rho, float mx,
 
 // MODE 0: residual only; 1: low-storage RK stage; 2: SSP-RK3 stage.
 // co.first / co.last mark the step's first and last stage.
+// One lane per face slot (LANES = 4 for up to 4 faces per cell, else 8): each
+// lane evaluates one face flux; lane 0 of the group sums the slots in order
+// (= ascending reference face id) with Kahan compensation and updates the cell.
 template <int MCF, int MODE, bool DT, bool VISC>
 __global__ void __launch_bounds__(256) k_mx_flux_update(const __grid_constant__ MxArgs a,
                                                         StageCoef co) {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long lam_bits = 0x7ff0000000000000ull;
-  bool finite = true;
-  if (c < a.nc) {
-    MxPhys ph;
-    ph.load(a.pc);
-    int e[MCF];
-    load_cface<MCF>(a.cface + (size_t)c * MCF, e);
-    Acc<float, true> s[5];
-#pragma unroll
-    for (int k = 0; k < MCF; ++k) {
-      if (e[k] < 0) continue;
-      const int f = e[k] >> 1, side = e[k] & 1;
+  constexpr int LANES = (MCF <= 4) ? 4 : 8;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = gt / LANES, slot = gt % LANES;
+  const int lane = threadIdx.x & 31;
+  const int lead = lane & ~(LANES - 1);
+  MxPhys ph;
+  ph.load(a.pc);
+  float F[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  if (c < a.nc && slot < MCF) {
+    const int e = __ldg(a.cface + (size_t)c * MCF + slot);
+    if (e >= 0) {
+      const int f = e >> 1, side = e & 1;
       const float4* src = reinterpret_cast<const float4*>(a.fs + (size_t)f * FREC);
       const float4 l0 = __ldg(src + 0), l1 = __ldg(src + 1), r0 = __ldg(src + 2), r1 = __ldg(src + 3);
+      const float4 nA = __ldg(&a.geoN[f]);
       const float l[5] = {l0.x, l0.y, l0.z, l0.w, l1.x};
       const float r[5] = {r0.x, r0.y, r0.z, r0.w, r1.x};
-      const float4 nA = __ldg(&a.geoN[f]);
-      float F[5];
       mx_conv_flux(l, r, nA, ph, F);
       if (VISC) {
         const float2 ve = __ldg(reinterpret_cast<const float2*>(src + 4));
@@ -402,12 +416,22 @@ __global__ void __launch_bounds__(256) k_mx_flux_update(const __grid_constant__ 
         F[3] += 0.5f * (l1.w + r1.w);
         F[4] += 0.5f * (ve.x + ve.y);
       }
+      if (side) {
 #pragma unroll
-      for (int j = 0; j < 5; ++j) {
-        if (side) s[j].sub(F[j]);
-        else s[j].add(F[j]);
+        for (int j = 0; j < 5; ++j) F[j] = -F[j];
       }
     }
+  }
+  // ordered Kahan sum of the slots on the group's lead lane
+  Acc<float, true> s[5];
+#pragma unroll
+  for (int k = 0; k < MCF; ++k) {
+#pragma unroll
+    for (int j = 0; j < 5; ++j) s[j].add(__shfl_sync(0xffffffffu, F[j], lead + k));
+  }
+  unsigned long long lam_bits = 0x7ff0000000000000ull;
+  bool finite = true;
+  if (c < a.nc && slot == 0) {
     const float rv = __ldg(&a.cgeo[c]).w;
     float rr[5];
 #pragma unroll
@@ -488,8 +512,7 @@ __global__ void __launch_bounds__(256) k_mx_flux_update(const __grid_constant__ 
     if (!finite) atomicOr(&a.sc->status, 1);
     if (DT) {
       lam_bits = warp_min_u64(lam_bits);
-      if ((threadIdx.x & 31) == 0 && lam_bits != 0x7ff0000000000000ull)
-        atomicMin(&a.sc->lam_bits, lam_bits);
+      if (lane == 0 && lam_bits != 0x7ff0000000000000ull) atomicMin(&a.sc->lam_bits, lam_bits);
     }
   }
 }

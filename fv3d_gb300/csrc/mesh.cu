@@ -370,6 +370,16 @@ fv3d_status upload_mesh(Ctx& ctx) {
                           (float)ctx.h_dx[3 * (size_t)c + 2], (float)ctx.h_vol[c]);
     }
     UP(ctx.d_cgeo, cg.data(), (size_t)nc);
+    // neighbour of every face slot: cell, -1 for a ghost, -2 for padding
+    std::vector<int> nbr((size_t)nc * ctx.mcf, -2);
+    for (int c = 0; c < nc; ++c)
+      for (int k = 0; k < ctx.mcf; ++k) {
+        const int e = ctx.h_cface[(size_t)c * ctx.mcf + k];
+        if (e < 0) break;
+        const int f = e >> 1;
+        nbr[(size_t)c * ctx.mcf + k] = (f >= ctx.nf_int) ? -1 : ((e & 1) ? ctx.h_fc0[f] : ctx.h_fc1[f]);
+      }
+    UP(ctx.d_cnbr, nbr.data(), nbr.size());
     UP(ctx.d_cdx, cd.data(), (size_t)nc);
     ALLOC(ctx.d_UfN, (size_t)nc * 8);
     ALLOC(ctx.d_kf, (size_t)nc * 5);

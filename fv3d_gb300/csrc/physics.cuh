@@ -30,6 +30,9 @@ struct PhysConst {
   int n_regions;
   int region_type[MAX_REGIONS];
   double region_phi[MAX_REGIONS][10];  // conserved + primitive region states
+  // FP32 copies for the mixed path (kappa, km1, s_km1, s_kp1, R, mu, heat, -)
+  float f32[8];
+  float region_phi_f[MAX_REGIONS][10];
 };
 
 template <class R>

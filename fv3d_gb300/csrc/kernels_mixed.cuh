@@ -385,29 +385,28 @@ __device__ __forceinline__ void mx_store_state(float4* dst, float rho, float mx,
 
 // MODE 0: residual only; 1: low-storage RK stage; 2: SSP-RK3 stage.
 // co.first / co.last mark the step's first and last stage.
-// One lane per face slot (LANES = 4 for up to 4 faces per cell, else 8): each
-// lane evaluates one face flux; lane 0 of the group sums the slots in order
-// (= ascending reference face id) with Kahan compensation and updates the cell.
 template <int MCF, int MODE, bool DT, bool VISC>
 __global__ void __launch_bounds__(256) k_mx_flux_update(const __grid_constant__ MxArgs a,
                                                         StageCoef co) {
-  constexpr int LANES = (MCF <= 4) ? 4 : 8;
-  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-  const int c = gt / LANES, slot = gt % LANES;
-  const int lane = threadIdx.x & 31;
-  const int lead = lane & ~(LANES - 1);
-  MxPhys ph;
-  ph.load(a.pc);
-  float F[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  if (c < a.nc && slot < MCF) {
-    const int e = __ldg(a.cface + (size_t)c * MCF + slot);
-    if (e >= 0) {
-      const int f = e >> 1, side = e & 1;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long lam_bits = 0x7ff0000000000000ull;
+  bool finite = true;
+  if (c < a.nc) {
+    MxPhys ph;
+    ph.load(a.pc);
+    int e[MCF];
+    load_cface<MCF>(a.cface + (size_t)c * MCF, e);
+    Acc<float, true> s[5];
+#pragma unroll
+    for (int k = 0; k < MCF; ++k) {
+      if (e[k] < 0) continue;
+      const int f = e[k] >> 1, side = e[k] & 1;
       const float4* src = reinterpret_cast<const float4*>(a.fs + (size_t)f * FREC);
       const float4 l0 = __ldg(src + 0), l1 = __ldg(src + 1), r0 = __ldg(src + 2), r1 = __ldg(src + 3);
-      const float4 nA = __ldg(&a.geoN[f]);
       const float l[5] = {l0.x, l0.y, l0.z, l0.w, l1.x};
       const float r[5] = {r0.x, r0.y, r0.z, r0.w, r1.x};
+      const float4 nA = __ldg(&a.geoN[f]);
+      float F[5];
       mx_conv_flux(l, r, nA, ph, F);
       if (VISC) {
         const float2 ve = __ldg(reinterpret_cast<const float2*>(src + 4));
@@ -416,22 +415,12 @@ __global__ void __launch_bounds__(256) k_mx_flux_update(const __grid_constant__ 
         F[3] += 0.5f * (l1.w + r1.w);
         F[4] += 0.5f * (ve.x + ve.y);
       }
-      if (side) {
 #pragma unroll
-        for (int j = 0; j < 5; ++j) F[j] = -F[j];
+      for (int j = 0; j < 5; ++j) {
+        if (side) s[j].sub(F[j]);
+        else s[j].add(F[j]);
       }
     }
-  }
-  // ordered Kahan sum of the slots on the group's lead lane
-  Acc<float, true> s[5];
-#pragma unroll
-  for (int k = 0; k < MCF; ++k) {
-#pragma unroll
-    for (int j = 0; j < 5; ++j) s[j].add(__shfl_sync(0xffffffffu, F[j], lead + k));
-  }
-  unsigned long long lam_bits = 0x7ff0000000000000ull;
-  bool finite = true;
-  if (c < a.nc && slot == 0) {
     const float rv = __ldg(&a.cgeo[c]).w;
     float rr[5];
 #pragma unroll
@@ -512,7 +501,8 @@ __global__ void __launch_bounds__(256) k_mx_flux_update(const __grid_constant__ 
     if (!finite) atomicOr(&a.sc->status, 1);
     if (DT) {
       lam_bits = warp_min_u64(lam_bits);
-      if (lane == 0 && lam_bits != 0x7ff0000000000000ull) atomicMin(&a.sc->lam_bits, lam_bits);
+      if ((threadIdx.x & 31) == 0 && lam_bits != 0x7ff0000000000000ull)
+        atomicMin(&a.sc->lam_bits, lam_bits);
     }
   }
 }

@@ -21,8 +21,7 @@ static void flux_mcf(const MxArgs& a, const Disc& d, int mode, bool dt, const St
 
 cudaError_t launch_mx_flux_update(const MxArgs& a, const Disc& d, int mode, bool dt,
                                   const StageCoef& co, cudaStream_t s) {
-  const long lanes = (a.mcf <= 4) ? 4 : 8;  // one lane per face slot
-  const int B = (int)((a.nc * lanes + 255) / 256);
+  const int B = (a.nc + 255) / 256;
   if (a.mcf == 4) flux_mcf<4>(a, d, mode, dt, co, s, B);
   else if (a.mcf == 6) flux_mcf<6>(a, d, mode, dt, co, s, B);
   else if (a.mcf == 8) flux_mcf<8>(a, d, mode, dt, co, s, B);

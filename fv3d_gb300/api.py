@@ -62,6 +62,22 @@ class StepStats(C.Structure):
                 ("elapsed_ms", C.c_double)]
 
 
+class ImplicitOpts(C.Structure):
+    _fields_ = [("cfl_start", C.c_double), ("cfl_max", C.c_double), ("tol_rel", C.c_double),
+                ("max_newton", C.c_int), ("krylov_dim", C.c_int), ("eta", C.c_double),
+                ("fd_eps", C.c_double), ("jv_precision", C.c_int), ("preconditioner", C.c_int),
+                ("pc_refresh", C.c_int)]
+
+
+class ImplicitStats(C.Structure):
+    _fields_ = [("newton_steps", C.c_int), ("gmres_iterations", C.c_int),
+                ("jv_evaluations", C.c_int), ("rejected_steps", C.c_int), ("fallbacks", C.c_int),
+                ("converged", C.c_int), ("res0", C.c_double), ("res_final", C.c_double),
+                ("rel_res", C.c_double), ("wall_ms", C.c_double), ("cfl_final", C.c_double)]
+
+
+PRECONDITIONERS = {"block_jacobi": 0, "lumped": 1, "learned": 2, "none": 3}
+
 EXPORTS = {
     "fv3d_create": ([C.POINTER(Config), C.POINTER(C.c_void_p)], C.c_int),
     "fv3d_destroy": ([C.c_void_p], C.c_int),
@@ -82,6 +98,10 @@ EXPORTS = {
     "fv3d_profile_stage": ([C.c_void_p, C.c_int, C.c_double, _f8p], C.c_int),
     "fv3d_get_stream": ([C.c_void_p, C.POINTER(C.c_void_p)], C.c_int),
     "fv3d_device_state": ([C.c_void_p, C.POINTER(_f8p)], C.c_int),
+    "fv3d_implicit_default_opts": ([C.POINTER(ImplicitOpts)], C.c_int),
+    "fv3d_solve_implicit": ([C.c_void_p, C.POINTER(ImplicitOpts), C.POINTER(ImplicitStats)], C.c_int),
+    "fv3d_implicit_history": ([C.c_void_p, _f8p, C.c_int, C.POINTER(C.c_int)], C.c_int),
+    "fv3d_get_blocks": ([C.c_void_p, _f8p], C.c_int),
 }
 
 _lib = None
@@ -207,6 +227,40 @@ class Solver:
         out = np.empty(3)
         self._check(self.lib.fv3d_profile_stage(self.h, n_reps, cfl, _p(out, _f8p)))
         return out
+
+    # ---- implicit steady solve ----
+    def solve_implicit(self, check: bool = True, **kw):
+        """Pseudo-transient Newton-Krylov to ||R||/||R_0|| <= tol_rel.  Keyword
+        arguments override fv3d_implicit_default_opts (preconditioner may be
+        a name).  Returns the statistics as a dict (raises on failure when
+        `check`)."""
+        o = ImplicitOpts()
+        self._check(self.lib.fv3d_implicit_default_opts(C.byref(o)))
+        for k, v in kw.items():
+            if k == "preconditioner" and isinstance(v, str):
+                v = PRECONDITIONERS[v]
+            if k == "jv_precision" and isinstance(v, str):
+                v = {"fp64": 0, "fp32": 1}[v]
+            setattr(o, k, v)
+        st = ImplicitStats()
+        rc = self.lib.fv3d_solve_implicit(self.h, C.byref(o), C.byref(st))
+        out = {f: getattr(st, f) for f, _ in ImplicitStats._fields_}
+        out["status"] = rc
+        if check and rc != 0:
+            self._check(rc)
+        return out
+
+    def implicit_history(self):
+        n = C.c_int()
+        self._check(self.lib.fv3d_implicit_history(self.h, None, 0, C.byref(n)))
+        out = np.empty(n.value)
+        self._check(self.lib.fv3d_implicit_history(self.h, _p(out, _f8p), n.value, C.byref(n)))
+        return out
+
+    def blocks(self):
+        out = np.empty((self.nc, 5, 5))
+        self._check(self.lib.fv3d_get_blocks(self.h, _p(out, _f8p)))
+        return out  # out[i, col, row]
 
     def stream(self) -> int:
         s = C.c_void_p()

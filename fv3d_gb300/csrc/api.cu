@@ -15,6 +15,7 @@
 #include "../../include/fv3d_gpu.h"
 #include "launch.h"
 #include "context.h"
+#include "implicit.h"
 
 using namespace fv3d;
 
@@ -318,6 +319,8 @@ extern "C" fv3d_status fv3d_destroy(fv3d_ctx* handle) {
   cudaSetDevice(ctx->cfg.device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ctx->release_graphs();
+  delete ctx->implicit;
+  ctx->implicit = nullptr;
   ctx->free_device();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -421,8 +424,7 @@ extern "C" fv3d_status fv3d_set_state(fv3d_ctx* handle, const double* u) {
   CK(cudaMemcpyAsync(ctx->d_stage.p, u, sizeof(double) * 5 * (size_t)ctx->nc, cudaMemcpyHostToDevice,
                      ctx->stream));
   k_import<<<nblk(ctx->nc), 256, 0, ctx->stream>>>(ctx->nc, ctx->d_perm.p, ctx->d_stage.p, ctx->d_U.p,
-                                                  ctx->fp64() ? nullptr : ctx->d_Uf.p,
-                                                  ctx->fp64() ? nullptr : ctx->d_UfN.p, ctx->phys.km1,
+                                                  ctx->d_Uf.p, ctx->d_UfN.p, ctx->phys.km1,
                                                   ctx->cfg.R_mix);
   CK(cudaGetLastError());
   ctx->state_ready = true;

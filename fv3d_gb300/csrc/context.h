@@ -12,6 +12,8 @@
 
 namespace fv3d {
 
+struct Implicit;
+
 // owning device allocation
 template <class T>
 struct DevBuf {
@@ -56,7 +58,7 @@ struct Ctx {
 
   // device mesh
   DevBuf<int> d_perm, d_fc0, d_fc1, d_fregion, d_cface, d_cnbr;
-  DevBuf<char> d_geo, d_lam, d_lsq, d_rvol;  // element type follows the precision
+  DevBuf<char> d_geo, d_lam, d_lsq, d_rvol;  // FP64-path geometry (double)
   DevBuf<double> d_vol, d_dx;
   // device solution data
   DevBuf<double> d_U, d_K, d_U0, d_dphi, d_stage, d_part;
@@ -70,6 +72,7 @@ struct Ctx {
   DevBuf<unsigned long long> d_bits;
 
   std::map<std::pair<int, double>, cudaGraphExec_t> graphs;
+  Implicit* implicit = nullptr;  // Newton-Krylov work space, created on first use
 
   bool fp64() const { return cfg.precision == FV3D_PRECISION_FP64; }
   size_t rsize() const { return fp64() ? sizeof(double) : sizeof(float); }
@@ -92,5 +95,7 @@ struct Ctx {
 
 fv3d_status prepare_mesh(Ctx& ctx, const fv3d_mesh_arrays& m);
 fv3d_status upload_mesh(Ctx& ctx);
+fv3d_status ensure_fp64_path(Ctx& ctx);
+fv3d_status ensure_mixed_path(Ctx& ctx);
 
 }  // namespace fv3d

@@ -1,0 +1,700 @@
+// Implicit steady solve on sm_103a: pseudo-transient Newton-Krylov.
+//
+//   (I/dt_i - dR/dU) dU = R(U),   U <- U + dU,   until ||R||/||R_0|| <= tol
+//
+// * R(U) is the FP64 residual (finite_volume_time_derivative semantics, the
+//   FP64 kernels of kernels.cuh); norms and the Newton update in FP64.
+// * Local time steps dt_i = CFL * V_i / sum_d (|u_d| + c) dx_d (the
+//   convective formula of calc_ns_timestep, navier_stokes.c:171-187), CFL
+//   ramped by switched evolution relaxation CFL = CFL_0 ||R_0|| / ||R||
+//   clipped to [CFL_0, CFL_max].
+// * Restarted flexible GMRES with FP64 Arnoldi (classical Gram-Schmidt with
+//   one re-orthogonalisation, deterministic block reductions) and Givens
+//   rotations on the host.  Matrix-free J v = (R(U + eps v) - R(U)) / eps,
+//   from the FP32 residual (mixed kernels, eps scaled to FP32) or the FP64
+//   residual (eps = 1e-7 relative).
+// * Preconditioner: batched 5x5 block Jacobi.  Blocks are the exact
+//   diagonal blocks of the first-order (cell-centre) discretisation - central
+//   differences of each face's convective flux plus a two-point viscous flux
+//   with respect to the cell's own state, ghost states re-derived from the
+//   perturbed state - built in FP64, inverted, applied in FP32.  The
+//   reference's lumped blocks (implicit.c:61-119: every cell perturbed at
+//   once, eps = 1e-4 ||U_v||) are available as an alternative.
+// The reference's own implicit step (a block-diagonal linearisation solved
+// by basec's GMRES, implicit.c:224-351) is reproduced by the CPU oracle.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "context.h"
+#include "implicit.h"
+
+namespace fv3d {
+
+namespace {
+
+constexpr int RED_BLOCKS = 1024;  // fixed grid for deterministic reductions
+
+inline int blocks(size_t n, int t = 256) { return (int)((n + t - 1) / t); }
+
+// ---- vector kernels on N = 5 * nc doubles ---------------------------------
+__global__ void k_lincomb(size_t n, double a, const double* __restrict__ x, double b,
+                          const double* __restrict__ y, double* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = a * x[i] + b * (y ? y[i] : 0.0);
+}
+
+// partial[b][j] = sum over block b's elements of w * V_j  (j < k)
+__global__ void k_multidot_partial(size_t n, const double* __restrict__ w, const double* __restrict__ V,
+                                   int k, double* __restrict__ partial) {
+  __shared__ double sh[32][33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;  // 8 warps
+  for (int j0 = 0; j0 < k; j0 += 4) {
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+      const double wi = w[i];
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (j0 + q < k) acc[q] = fma(wi, V[(size_t)(j0 + q) * n + i], acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      double v = acc[q];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) sh[warp][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 4 && j0 + (int)threadIdx.x < k) {
+      double s = 0.0;
+      for (int wv = 0; wv < (int)(blockDim.x >> 5); ++wv) s += sh[wv][threadIdx.x];
+      partial[(size_t)blockIdx.x * 32 + j0 + threadIdx.x] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// out[j] = sum_b partial[b][j] in block order (one block, fixed order)
+__global__ void k_multidot_final(int nb, int k, const double* __restrict__ partial, double* __restrict__ out) {
+  const int j = threadIdx.x;
+  if (j >= k) return;
+  double s = 0.0;
+  for (int b = 0; b < nb; ++b) s += partial[(size_t)b * 32 + j];
+  out[j] = s;
+}
+
+// w -= sum_j h_j V_j   (h on the device)
+__global__ void k_multi_axpy(size_t n, double* __restrict__ w, const double* __restrict__ V,
+                             const double* __restrict__ h, int k, double sign) {
+  __shared__ double hs[32];
+  if (threadIdx.x < 32) hs[threadIdx.x] = (threadIdx.x < (unsigned)k) ? h[threadIdx.x] : 0.0;
+  __syncthreads();
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int j = 0; j < k; ++j) s = fma(hs[j], V[(size_t)j * n + i], s);
+    w[i] = w[i] + sign * s;
+  }
+}
+
+// local pseudo-time step per cell (FP64 convective formula)
+__global__ void k_local_dt(int nc, const double* __restrict__ U, const double* __restrict__ vol,
+                           const double* __restrict__ dx, double kappa, double km1, double cfl,
+                           double* __restrict__ dtl) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  double q[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) q[j] = U[(size_t)j * nc + c];
+  const double ir = 1.0 / q[0];
+  const double u = q[1] * ir, v = q[2] * ir, w = q[3] * ir;
+  const double p = fmax(1.00E-10, km1 * (q[4] - 0.5 * (q[1] * u + q[2] * v + q[3] * w)));
+  const double cs = sqrt(kappa * p * ir);
+  const double* d = dx + 3 * (size_t)c;
+  const double ds = (fabs(u) + cs) * d[0] + (fabs(v) + cs) * d[1] + (fabs(w) + cs) * d[2];
+  dtl[c] = cfl * vol[c] / ds;
+}
+
+// out = z / dt - (Rp - Rb) / eps   (per cell dt)
+__global__ void k_jv_combine(int nc, const double* __restrict__ z, const double* __restrict__ Rp,
+                             const double* __restrict__ Rb, const double* __restrict__ dtl, double ieps,
+                             double* __restrict__ out) {
+  const size_t n = 5 * (size_t)nc;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int c = (int)(i % nc);
+    out[i] = z[i] / dtl[c] - (Rp[i] - Rb[i]) * ieps;
+  }
+}
+
+// FP32 state record (rho, m, E, p, T) of an FP64 state W (renumbered SoA)
+__global__ void k_make_record(int nc, const double* __restrict__ W, float* __restrict__ Uf,
+                              float km1, float R) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const float rho = (float)W[c], mx = (float)W[(size_t)nc + c], my = (float)W[2 * (size_t)nc + c];
+  const float mz = (float)W[3 * (size_t)nc + c];
+  const double E = W[4 * (size_t)nc + c];
+  const float ir = 1.f / rho;
+  const float ke = 0.5f * (mx * mx + my * my + mz * mz) * ir;
+  const float p = fmaxf(1.00E-10f, (float)((double)km1 * (E - (double)ke)));
+  float4* d = reinterpret_cast<float4*>(Uf) + 2 * (size_t)c;
+  d[0] = make_float4(rho, mx, my, mz);
+  d[1] = make_float4((float)E, p, p * ir / R, 0.f);
+}
+
+// ---- first-order FD diagonal blocks ---------------------------------------
+// global-frame convective flux . n (FP64): AUSM or Rusanov
+__device__ void fo_flux(const double* l, const double* r, const double* n, const PhysConst& pc,
+                        double* F) {
+  const double km1 = pc.km1, kappa = pc.kappa;
+  const double irl = 1.0 / l[0], irr = 1.0 / r[0];
+  const double ul = l[1] * irl, vl = l[2] * irl, wl = l[3] * irl;
+  const double ur = r[1] * irr, vr = r[2] * irr, wr = r[3] * irr;
+  const double pl = fmax(1.00E-10, km1 * (l[4] - 0.5 * (l[1] * ul + l[2] * vl + l[3] * wl)));
+  const double pr = fmax(1.00E-10, km1 * (r[4] - 0.5 * (r[1] * ur + r[2] * vr + r[3] * wr)));
+  const double unl = ul * n[0] + vl * n[1] + wl * n[2];
+  const double unr = ur * n[0] + vr * n[1] + wr * n[2];
+  const double cl = sqrt(kappa * pl * irl), cr = sqrt(kappa * pr * irr);
+  if (pc.flux == 1) {
+    const double lam = fmax(fabs(unl) + cl, fabs(unr) + cr);
+    F[0] = 0.5 * (l[0] * unl + r[0] * unr) - 0.5 * lam * (r[0] - l[0]);
+    for (int d = 0; d < 3; ++d)
+      F[1 + d] = 0.5 * (l[1 + d] * unl + pl * n[d] + r[1 + d] * unr + pr * n[d]) - 0.5 * lam * (r[1 + d] - l[1 + d]);
+    F[4] = 0.5 * ((l[4] + pl) * unl + (r[4] + pr) * unr) - 0.5 * lam * (r[4] - l[4]);
+  } else {
+    const double Ml = unl / cl, Mr = unr / cr;
+    double mp, pp, mm, pm;
+    if (Ml <= -1.0) { mp = 0.0; pp = 0.0; }
+    else if (Ml < 1.0) { mp = 0.25 * (Ml + 1.0) * (Ml + 1.0); pp = 0.25 * pl * (1.0 + Ml) * (1.0 + Ml) * (2.0 - Ml); }
+    else { mp = Ml; pp = pl; }
+    if (Mr <= -1.0) { mm = Mr; pm = pr; }
+    else if (Mr < 1.0) { mm = -0.25 * (Mr - 1.0) * (Mr - 1.0); pm = 0.25 * pr * (1.0 - Mr) * (1.0 - Mr) * (2.0 + Mr); }
+    else { mm = 0.0; pm = 0.0; }
+    const double mdl = fmax(0.0, mp + mm) * cl * l[0];
+    const double mdr = fmin(0.0, mp + mm) * cr * r[0];
+    F[0] = mdl + mdr;
+    F[1] = mdl * ul + mdr * ur + (pp + pm) * n[0];
+    F[2] = mdl * vl + mdr * vr + (pp + pm) * n[1];
+    F[3] = mdl * wl + mdr * wr + (pp + pm) * n[2];
+    F[4] = mdl * (l[4] + pl) * irl + mdr * (r[4] + pr) * irr;
+  }
+  // two-point viscous flux across the face: -mu du/dn, -(mu u.du/dn + k dT/dn)
+  if (pc.mu != 0.0) {
+    const double id = 1.0 / n[3];  // n[3] carries the centre distance
+    const double mu = pc.mu, k = pc.heat_lambda;
+    const double Tl = pl * irl / pc.R_mix, Tr = pr * irr / pc.R_mix;
+    const double du = ur - ul, dv = vr - vl, dw = wr - wl;
+    F[1] -= mu * du * id;
+    F[2] -= mu * dv * id;
+    F[3] -= mu * dw * id;
+    F[4] -= (mu * (0.5 * (ul + ur) * du + 0.5 * (vl + vr) * dv + 0.5 * (wl + wr) * dw) + k * (Tr - Tl)) * id;
+  }
+}
+
+// D_c = I/dt_c + (1/V_c) sum_f d(F_f . n_out A_f)/dU_c  (column-major 5x5)
+__global__ void k_fo_blocks(KArgs<double> a, const double* __restrict__ dtl,
+                            const double* __restrict__ fdist, double* __restrict__ D) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.nc) return;
+  Phys<double> ph;
+  ph.load(a.pc);
+  double qc[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) qc[j] = a.U[(size_t)j * a.nc + c];
+  double Dc[25];
+#pragma unroll
+  for (int j = 0; j < 25; ++j) Dc[j] = 0.0;
+  for (int k = 0; k < a.mcf; ++k) {
+    const int e = a.cface[(size_t)c * a.mcf + k];
+    if (e < 0) break;
+    const int f = e >> 1, side = e & 1;
+    const double* g = a.geo + (size_t)f * GEO;
+    const double sg = side ? -1.0 : 1.0;
+    const double n[4] = {sg * g[G_N], sg * g[G_N + 1], sg * g[G_N + 2], fdist[f]};
+    const double A = g[G_A];
+    const bool bnd = f >= a.nf_int;
+    double qo[10];
+    if (!bnd) {
+      const int o = side ? a.fc0[f] : a.fc1[f];
+#pragma unroll
+      for (int j = 0; j < 5; ++j) qo[j] = a.U[(size_t)j * a.nc + o];
+    }
+    for (int v = 0; v < 5; ++v) {
+      const double h = 1e-7 * fmax(fabs(qc[v]), 1e-3 * fabs(qc[0]) + 1e-12);
+      double Fp[5], Fm[5];
+      for (int s = 0; s < 2; ++s) {
+        double qp[10];
+#pragma unroll
+        for (int j = 0; j < 5; ++j) qp[j] = qc[j];
+        qp[v] += s ? -h : h;
+        if (bnd) {
+          cons_to_prims(qp, ph);
+          ghost_state(qp, a.fregion[f - a.nf_int], &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qo);
+        }
+        fo_flux(qp, qo, n, a.pc, s ? Fm : Fp);
+      }
+      const double sc = A / (2.0 * h * a.vol[c]);
+#pragma unroll
+      for (int j = 0; j < 5; ++j) Dc[v * 5 + j] += (Fp[j] - Fm[j]) * sc;
+    }
+  }
+  const double idt = 1.0 / dtl[c];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) Dc[j * 5 + j] += idt;
+#pragma unroll
+  for (int j = 0; j < 25; ++j) D[(size_t)c * 25 + j] = Dc[j];
+}
+
+// lumped blocks (implicit.c:61-119): column v of -(R(U + e/2) - R(U - e/2)) / e
+__global__ void k_perturb_all(int nc, const double* __restrict__ U, int v, double delta,
+                              double* __restrict__ W) {
+  const size_t n = 5 * (size_t)nc;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    W[i] = U[i] + ((i / nc == (size_t)v) ? delta : 0.0);
+}
+
+__global__ void k_lumped_column(int nc, int v, const double* __restrict__ Rp, const double* __restrict__ Rm,
+                                double ieps, double* __restrict__ D) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+#pragma unroll
+  for (int j = 0; j < 5; ++j)
+    D[(size_t)c * 25 + v * 5 + j] = -(Rp[(size_t)j * nc + c] - Rm[(size_t)j * nc + c]) * ieps;
+}
+
+__global__ void k_add_diag(int nc, const double* __restrict__ dtl, double* __restrict__ D) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const double idt = 1.0 / dtl[c];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) D[(size_t)c * 25 + j * 5 + j] += idt;
+}
+
+// 5x5 inverse by Gauss-Jordan with partial pivoting (FP64), stored FP32;
+// a singular block falls back to the inverse of its diagonal.
+__global__ void k_block_invert(int nc, const double* __restrict__ D, float* __restrict__ Dinv) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  double M[5][10];
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 5; ++j) {
+      M[i][j] = D[(size_t)c * 25 + j * 5 + i];  // column-major -> row i, col j
+      M[i][5 + j] = (i == j) ? 1.0 : 0.0;
+    }
+  bool ok = true;
+  for (int col = 0; col < 5; ++col) {
+    int piv = col;
+    for (int i = col + 1; i < 5; ++i)
+      if (fabs(M[i][col]) > fabs(M[piv][col])) piv = i;
+    if (!(fabs(M[piv][col]) > 1e-300)) { ok = false; break; }
+    if (piv != col)
+      for (int j = 0; j < 10; ++j) { double t = M[col][j]; M[col][j] = M[piv][j]; M[piv][j] = t; }
+    const double ip = 1.0 / M[col][col];
+    for (int j = 0; j < 10; ++j) M[col][j] *= ip;
+    for (int i = 0; i < 5; ++i) {
+      if (i == col) continue;
+      const double fct = M[i][col];
+      for (int j = 0; j < 10; ++j) M[i][j] -= fct * M[col][j];
+    }
+  }
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 5; ++j) {
+      double v = ok ? M[i][5 + j] : ((i == j) ? 1.0 / D[(size_t)c * 25 + i * 5 + i] : 0.0);
+      Dinv[(size_t)c * 25 + j * 5 + i] = (float)v;  // column-major
+    }
+}
+
+// z_c = Dinv_c v_c  (FP32 arithmetic)
+__global__ void k_block_apply(int nc, const float* __restrict__ Dinv, const double* __restrict__ v,
+                              double* __restrict__ z) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  float x[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) x[j] = (float)v[(size_t)j * nc + c];
+  const float* M = Dinv + (size_t)c * 25;
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    float s = 0.f;
+#pragma unroll
+    for (int j = 0; j < 5; ++j) s = fmaf(M[j * 5 + i], x[j], s);
+    z[(size_t)i * nc + c] = (double)s;
+  }
+}
+
+// min density / pressure of a state (positivity check of a Newton update)
+__global__ void k_min_rho_p(int nc, const double* __restrict__ U, double km1, unsigned long long* out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long b = 0x7ff0000000000000ull;
+  if (c < nc) {
+    double q[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) q[j] = U[(size_t)j * nc + c];
+    const double p = km1 * (q[4] - 0.5 * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) / q[0]);
+    const double m = fmin(q[0], p);
+    b = (m > 0.0 && isfinite(m)) ? (unsigned long long)__double_as_longlong(m) : 0ull;
+  }
+  b = warp_min_u64(b);
+  if ((threadIdx.x & 31) == 0) atomicMin(out, b);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+#define ICK(expr)                                               \
+  do {                                                          \
+    fv3d_status st__ = ctx.cuda((expr), #expr);                 \
+    if (st__ != FV3D_OK) return st__;                           \
+  } while (0)
+
+fv3d_status Implicit::setup(Ctx& ctx, int m) {
+  const size_t n = 5 * (size_t)ctx.nc;
+  if (this->n == n && this->m >= m) return FV3D_OK;
+  this->n = n;
+  this->m = m;
+  auto al = [&](DevBuf<double>& b, size_t cnt) { return ctx.cuda(b.alloc(cnt), "implicit allocation"); };
+  fv3d_status st;
+  if ((st = al(V, (size_t)(m + 1) * n)) || (st = al(Z, (size_t)m * n)) || (st = al(w, n)) ||
+      (st = al(R, n)) || (st = al(Rb, n)) || (st = al(Rp, n)) || (st = al(Wst, n)) || (st = al(x, n)) ||
+      (st = al(dtl, (size_t)ctx.nc)) || (st = al(D, 25 * (size_t)ctx.nc)) ||
+      (st = al(part, (size_t)RED_BLOCKS * 32)) || (st = al(hdev, 64)) || (st = al(fdist, (size_t)ctx.nf)))
+    return st;
+  if ((st = ctx.cuda(Dinv.alloc(25 * (size_t)ctx.nc), "implicit allocation")) != FV3D_OK) return st;
+  if ((st = ctx.cuda(bits.alloc(1), "implicit allocation")) != FV3D_OK) return st;
+  // face centre distances for the two-point viscous term
+  std::vector<double> fd(ctx.nf);
+  for (int f = 0; f < ctx.nf; ++f) {
+    const double* g = &ctx.h_geo[(size_t)f * GEO];
+    if (f < ctx.nf_int) {
+      double s = 0.0;
+      for (int d = 0; d < 3; ++d) s += (g[G_D1 + d] - g[G_D2 + d]) * (g[G_D1 + d] - g[G_D2 + d]);
+      fd[f] = sqrt(s);
+    } else {
+      fd[f] = 2.0 * fabs(g[G_D1] * g[G_N] + g[G_D1 + 1] * g[G_N + 1] + g[G_D1 + 2] * g[G_N + 2]);
+    }
+  }
+  ICK(cudaMemcpy(fdist.p, fd.data(), sizeof(double) * ctx.nf, cudaMemcpyHostToDevice));
+  return FV3D_OK;
+}
+
+// R(state) in FP64 into `out`
+static fv3d_status residual64(Ctx& ctx, const double* state, double* out) {
+  KArgs<double> a = ctx.args<double>();
+  a.U = const_cast<double*>(state);
+  a.dphi = out;
+  StageCoef co{0, 0, 0, 0, 1, 1};
+  const Disc d = ctx.disc();
+  ICK(launch_gradients<double>(a, d, ctx.stream));
+  ICK(launch_face_flux<double>(a, d, ctx.stream));
+  ICK(launch_gather<double>(a, 0, false, co, ctx.stream));
+  return FV3D_OK;
+}
+
+// R(state) with the FP32 (mixed) kernels into `out`
+static fv3d_status residual32(Ctx& ctx, const double* state, double* out) {
+  k_make_record<<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, state, ctx.d_Uf.p, ctx.phys.f32[1],
+                                                        ctx.phys.f32[4]);
+  ICK(cudaGetLastError());
+  MxArgs a = ctx.mx_args();
+  a.dphi = out;
+  StageCoef co{0, 0, 0, 0, 1, 1};
+  const Disc d = ctx.disc();
+  ICK(launch_mx_sides(a, d, ctx.stream));
+  ICK(launch_mx_flux_update(a, d, 0, false, co, ctx.stream));
+  return FV3D_OK;
+}
+
+fv3d_status Implicit::dots(Ctx& ctx, const double* wv, const double* Vb, int k, std::vector<double>& out) {
+  const int nb = std::min(RED_BLOCKS, blocks(n));
+  for (int j0 = 0; j0 < k; j0 += 32) {
+    const int kk = std::min(32, k - j0);
+    k_multidot_partial<<<nb, 256, 0, ctx.stream>>>(n, wv, Vb + (size_t)j0 * n, kk, part.p);
+    k_multidot_final<<<1, 32, 0, ctx.stream>>>(nb, kk, part.p, hdev.p + j0);
+  }
+  ICK(cudaGetLastError());
+  out.resize(k);
+  ICK(cudaMemcpyAsync(out.data(), hdev.p, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx.stream));
+  ICK(cudaStreamSynchronize(ctx.stream));
+  return FV3D_OK;
+}
+
+fv3d_status Implicit::norm(Ctx& ctx, const double* v, double* out) {
+  std::vector<double> h;
+  fv3d_status st = dots(ctx, v, v, 1, h);
+  if (st != FV3D_OK) return st;
+  *out = sqrt(h[0]);
+  return FV3D_OK;
+}
+
+fv3d_status Implicit::precondition(Ctx& ctx, const double* v, double* z) {
+  if (opts.preconditioner == FV3D_PC_NONE) {
+    ICK(cudaMemcpyAsync(z, v, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx.stream));
+    return FV3D_OK;
+  }
+  k_block_apply<<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, Dinv.p, v, z);
+  ICK(cudaGetLastError());
+  return FV3D_OK;
+}
+
+// w = (I/dt - J) z
+fv3d_status Implicit::apply_A(Ctx& ctx, const double* z, double* out) {
+  double zn = 0.0;
+  fv3d_status st = norm(ctx, z, &zn);
+  if (st != FV3D_OK) return st;
+  if (!(zn > 0.0)) {
+    ICK(cudaMemsetAsync(out, 0, sizeof(double) * n, ctx.stream));
+    return FV3D_OK;
+  }
+  const double rel = (opts.jv_precision == 1) ? 5e-4 : opts.fd_eps;
+  const double eps = rel * (1.0 + unorm) / zn;
+  k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0, ctx.d_U.p, eps, z, Wst.p);
+  ICK(cudaGetLastError());
+  if (opts.jv_precision == 1) st = residual32(ctx, Wst.p, Rp.p);
+  else st = residual64(ctx, Wst.p, Rp.p);
+  if (st != FV3D_OK) return st;
+  k_jv_combine<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(ctx.nc, z, Rp.p, Rb.p, dtl.p, 1.0 / eps, out);
+  ICK(cudaGetLastError());
+  jv_count += 1;
+  return FV3D_OK;
+}
+
+fv3d_status Implicit::build_blocks(Ctx& ctx) {
+  if (opts.preconditioner == FV3D_PC_NONE) return FV3D_OK;
+  if (opts.preconditioner == FV3D_PC_LUMPED) {
+    // every cell perturbed at once by +-eps/2, eps = 1e-4 ||U_v||_2 (implicit.c:65-117)
+    std::vector<double> slice(ctx.nc);
+    for (int v = 0; v < 5; ++v) {
+      ICK(cudaMemcpyAsync(slice.data(), ctx.d_U.p + (size_t)v * ctx.nc, sizeof(double) * ctx.nc,
+                          cudaMemcpyDeviceToHost, ctx.stream));
+      ICK(cudaStreamSynchronize(ctx.stream));
+      double s = 0.0;
+      for (int c = 0; c < ctx.nc; ++c) s += slice[c] * slice[c];
+      const double eps = sqrt(s) * 1e-4;
+      k_perturb_all<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(ctx.nc, ctx.d_U.p, v, 0.5 * eps, Wst.p);
+      fv3d_status st = residual64(ctx, Wst.p, Rp.p);
+      if (st != FV3D_OK) return st;
+      k_perturb_all<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(ctx.nc, ctx.d_U.p, v, -0.5 * eps, Wst.p);
+      st = residual64(ctx, Wst.p, w.p);
+      if (st != FV3D_OK) return st;
+      k_lumped_column<<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, v, Rp.p, w.p, 1.0 / (eps + 1e-16), D.p);
+    }
+    k_add_diag<<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, dtl.p, D.p);
+  } else {
+    k_fo_blocks<<<blocks(ctx.nc, 128), 128, 0, ctx.stream>>>(ctx.args<double>(), dtl.p, fdist.p, D.p);
+  }
+  ICK(cudaGetLastError());
+  k_block_invert<<<blocks(ctx.nc, 128), 128, 0, ctx.stream>>>(ctx.nc, D.p, Dinv.p);
+  ICK(cudaGetLastError());
+  return FV3D_OK;
+}
+
+// FGMRES(m) for (I/dt - J) x = R, x0 = 0; returns iterations
+fv3d_status Implicit::fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res) {
+  const int m = opts.krylov_dim;
+  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0), y(m);
+  // V_0 = R / ||R||
+  k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0 / rnorm, R.p, 0.0, nullptr, V.p);
+  ICK(cudaGetLastError());
+  g[0] = rnorm;
+  int k = 0;
+  double res = rnorm;
+  for (; k < m; ++k) {
+    double* vk = V.p + (size_t)k * n;
+    double* zk = Z.p + (size_t)k * n;
+    fv3d_status st = precondition(ctx, vk, zk);
+    if (st != FV3D_OK) return st;
+    st = apply_A(ctx, zk, w.p);
+    if (st != FV3D_OK) return st;
+    // classical Gram-Schmidt, twice
+    std::vector<double> h1, h2;
+    if ((st = dots(ctx, w.p, V.p, k + 1, h1)) != FV3D_OK) return st;
+    k_multi_axpy<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, w.p, V.p, hdev.p, k + 1, -1.0);
+    if ((st = dots(ctx, w.p, V.p, k + 1, h2)) != FV3D_OK) return st;
+    k_multi_axpy<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, w.p, V.p, hdev.p, k + 1, -1.0);
+    ICK(cudaGetLastError());
+    double hn = 0.0;
+    if ((st = norm(ctx, w.p, &hn)) != FV3D_OK) return st;
+    for (int j = 0; j <= k; ++j) H[(size_t)k * (m + 1) + j] = h1[j] + h2[j];
+    H[(size_t)k * (m + 1) + k + 1] = hn;
+    if (hn > 0.0) {
+      k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0 / hn, w.p, 0.0, nullptr,
+                                                                  V.p + (size_t)(k + 1) * n);
+      ICK(cudaGetLastError());
+    }
+    // Givens rotations on the new column
+    for (int j = 0; j < k; ++j) {
+      const double a = H[(size_t)k * (m + 1) + j], b = H[(size_t)k * (m + 1) + j + 1];
+      H[(size_t)k * (m + 1) + j] = cs[j] * a + sn[j] * b;
+      H[(size_t)k * (m + 1) + j + 1] = -sn[j] * a + cs[j] * b;
+    }
+    const double a = H[(size_t)k * (m + 1) + k], b = H[(size_t)k * (m + 1) + k + 1];
+    const double r = sqrt(a * a + b * b);
+    cs[k] = (r > 0.0) ? a / r : 1.0;
+    sn[k] = (r > 0.0) ? b / r : 0.0;
+    H[(size_t)k * (m + 1) + k] = r;
+    H[(size_t)k * (m + 1) + k + 1] = 0.0;
+    g[k + 1] = -sn[k] * g[k];
+    g[k] = cs[k] * g[k];
+    res = fabs(g[k + 1]);
+    if (res <= opts.eta * rnorm || !(hn > 0.0)) { ++k; break; }
+  }
+  for (int i = k - 1; i >= 0; --i) {
+    double s = g[i];
+    for (int j = i + 1; j < k; ++j) s -= H[(size_t)j * (m + 1) + i] * y[j];
+    y[i] = s / H[(size_t)i * (m + 1) + i];
+  }
+  // x = Z y
+  ICK(cudaMemcpyAsync(hdev.p, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, ctx.stream));
+  ICK(cudaMemsetAsync(x.p, 0, sizeof(double) * n, ctx.stream));
+  k_multi_axpy<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, x.p, Z.p, hdev.p, k, 1.0);
+  ICK(cudaGetLastError());
+  *iters = k;
+  *rel_res = res / rnorm;
+  return FV3D_OK;
+}
+
+fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit_stats* stats) {
+  opts = o;
+  if (opts.krylov_dim < 1 || opts.krylov_dim > 31) return ctx.fail(FV3D_ERR_INVALID_ARG, "krylov_dim must be 1..31");
+  fv3d_status st = ensure_fp64_path(ctx);
+  if (st == FV3D_OK && opts.jv_precision == 1) st = ensure_mixed_path(ctx);
+  if (st == FV3D_OK) st = setup(ctx, opts.krylov_dim);
+  if (st != FV3D_OK) return st;
+  history.clear();
+  jv_count = 0;
+  const auto t0 = std::chrono::steady_clock::now();
+  double res0 = 0.0, res = 0.0, res_prev = 0.0, cfl = opts.cfl_start;
+  int newton = 0, gmres_total = 0, rejected = 0;
+  bool converged = false;
+  for (newton = 0; newton <= opts.max_newton; ++newton) {
+    if ((st = residual64(ctx, ctx.d_U.p, R.p)) != FV3D_OK) return st;
+    if ((st = norm(ctx, R.p, &res)) != FV3D_OK) return st;
+    if (!std::isfinite(res)) return ctx.fail(FV3D_ERR_NONFINITE, "non-finite residual at Newton step %d", newton);
+    if (newton == 0) res0 = res;
+    history.push_back(res);
+    if (res <= opts.tol_rel * res0 || res == 0.0) { converged = true; break; }
+    if (newton == opts.max_newton) break;
+    if (newton > 0) cfl = std::min(opts.cfl_max, std::max(opts.cfl_start, opts.cfl_start * res0 / res));
+    if ((st = norm(ctx, ctx.d_U.p, &unorm)) != FV3D_OK) return st;
+    // Newton step with a CFL back-off on failure
+    for (int attempt = 0; attempt < 6; ++attempt) {
+      k_local_dt<<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, ctx.d_U.p, ctx.d_vol.p, ctx.d_dx.p,
+                                                        ctx.cfg.kappa, ctx.phys.km1, cfl, dtl.p);
+      ICK(cudaGetLastError());
+      if (newton % std::max(1, opts.pc_refresh) == 0 || attempt > 0) {
+        if ((st = build_blocks(ctx)) != FV3D_OK) return st;
+      }
+      if (opts.jv_precision == 1) st = residual32(ctx, ctx.d_U.p, Rb.p);
+      else st = ICK_copy(ctx, Rb.p, R.p);
+      if (st != FV3D_OK) return st;
+      int it = 0;
+      double rr = 0.0;
+      if ((st = fgmres(ctx, res, &it, &rr)) != FV3D_OK) return st;
+      gmres_total += it;
+      // trial state
+      k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0, ctx.d_U.p, 1.0, x.p, Wst.p);
+      ICK(cudaMemsetAsync(bits.p, 0xff, sizeof(unsigned long long), ctx.stream));
+      k_min_rho_p<<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, Wst.p, ctx.phys.km1, bits.p);
+      ICK(cudaGetLastError());
+      unsigned long long mb = 0;
+      ICK(cudaMemcpyAsync(&mb, bits.p, sizeof(mb), cudaMemcpyDeviceToHost, ctx.stream));
+      ICK(cudaStreamSynchronize(ctx.stream));
+      if (mb != 0ull) {
+        ICK(cudaMemcpyAsync(ctx.d_U.p, Wst.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx.stream));
+        break;
+      }
+      rejected += 1;
+      cfl = std::max(1.0, cfl * 0.1);
+      if (attempt == 5) return ctx.fail(FV3D_ERR_NOT_CONVERGED, "Newton update not admissible at step %d", newton);
+    }
+    res_prev = res;
+  }
+  (void)res_prev;
+  ICK(cudaStreamSynchronize(ctx.stream));
+  const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+  if (stats != nullptr) {
+    stats->newton_steps = newton;
+    stats->gmres_iterations = gmres_total;
+    stats->jv_evaluations = jv_count;
+    stats->rejected_steps = rejected;
+    stats->fallbacks = 0;
+    stats->res0 = res0;
+    stats->res_final = res;
+    stats->rel_res = (res0 > 0.0) ? res / res0 : 0.0;
+    stats->wall_ms = ms;
+    stats->cfl_final = cfl;
+    stats->converged = converged ? 1 : 0;
+  }
+  ctx.state_ready = true;
+  ctx.residual_valid = false;
+  if (!converged) return ctx.fail(FV3D_ERR_NOT_CONVERGED, "relative residual %.3e after %d Newton steps", res / res0, newton);
+  return FV3D_OK;
+}
+
+fv3d_status Implicit::ICK_copy(Ctx& ctx, double* dst, const double* src) {
+  ICK(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx.stream));
+  return FV3D_OK;
+}
+
+}  // namespace fv3d
+
+using namespace fv3d;
+
+extern "C" fv3d_status fv3d_implicit_default_opts(fv3d_implicit_opts* o) {
+  if (o == nullptr) return FV3D_ERR_INVALID_ARG;
+  o->cfl_start = 100.0;
+  o->cfl_max = 1e4;
+  o->tol_rel = 1e-8;
+  o->max_newton = 500;
+  o->krylov_dim = 30;
+  o->eta = 1e-2;
+  o->fd_eps = 1e-7;
+  o->jv_precision = 1;
+  o->preconditioner = FV3D_PC_BLOCK_JACOBI;
+  o->pc_refresh = 1;
+  return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_solve_implicit(fv3d_ctx* handle, const fv3d_implicit_opts* opts,
+                                           fv3d_implicit_stats* stats) {
+  if (handle == nullptr || opts == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (!ctx->mesh_ready || !ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "mesh and state required");
+  for (int b = 0; b < ctx->nb; ++b)
+    if (!(ctx->region_set & (1u << ctx->h_fregion[b])))
+      return ctx->fail(FV3D_ERR_STATE, "boundary region %d has no condition", ctx->h_fregion[b]);
+  if (opts->preconditioner < 0 || opts->preconditioner > FV3D_PC_NONE || opts->jv_precision < 0 ||
+      opts->jv_precision > 1 || !(opts->tol_rel > 0.0) || !(opts->cfl_start > 0.0) || opts->max_newton < 0)
+    return ctx->fail(FV3D_ERR_INVALID_ARG, "bad implicit options");
+  if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "cudaSetDevice");
+  if (!ctx->implicit) ctx->implicit = new Implicit();
+  return ctx->implicit->solve(*ctx, *opts, stats);
+}
+
+extern "C" fv3d_status fv3d_implicit_history(const fv3d_ctx* handle, double* res, int max, int* count) {
+  if (handle == nullptr || count == nullptr) return FV3D_ERR_INVALID_ARG;
+  const Ctx* ctx = reinterpret_cast<const Ctx*>(handle);
+  if (!ctx->implicit) { *count = 0; return FV3D_OK; }
+  const std::vector<double>& h = ctx->implicit->history;
+  *count = (int)h.size();
+  if (res != nullptr)
+    for (int i = 0; i < std::min(max, (int)h.size()); ++i) res[i] = h[i];
+  return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_get_blocks(fv3d_ctx* handle, double* blocks_out) {
+  // diagonal blocks of the last preconditioner build, [n_cells][25]
+  // column-major, reference cell order
+  if (handle == nullptr || blocks_out == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (!ctx->implicit || ctx->implicit->D.p == nullptr) return ctx->fail(FV3D_ERR_STATE, "no blocks built");
+  std::vector<double> tmp(25 * (size_t)ctx->nc);
+  if (cudaMemcpy(tmp.data(), ctx->implicit->D.p, sizeof(double) * tmp.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return ctx->fail(FV3D_ERR_DEVICE, "copy blocks");
+  for (int c = 0; c < ctx->nc; ++c)
+    memcpy(blocks_out + 25 * (size_t)ctx->perm[c], &tmp[25 * (size_t)c], sizeof(double) * 25);
+  return FV3D_OK;
+}

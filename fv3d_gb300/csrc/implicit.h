@@ -1,0 +1,32 @@
+// Implicit Newton-Krylov solver state (see implicit.cu).
+#pragma once
+
+#include <vector>
+
+#include "context.h"
+
+namespace fv3d {
+
+struct Implicit {
+  fv3d_implicit_opts opts;
+  size_t n = 0;   // 5 * cells
+  int m = 0;      // Krylov dimension allocated
+  DevBuf<double> V, Z, w, R, Rb, Rp, Wst, x, dtl, D, part, hdev, fdist;
+  DevBuf<float> Dinv;
+  DevBuf<unsigned long long> bits;
+  std::vector<double> history;  // ||R||_2 per Newton step
+  int jv_count = 0;
+  double unorm = 0.0;
+
+  fv3d_status setup(Ctx& ctx, int m);
+  fv3d_status solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit_stats* stats);
+  fv3d_status fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res);
+  fv3d_status apply_A(Ctx& ctx, const double* z, double* out);
+  fv3d_status precondition(Ctx& ctx, const double* v, double* z);
+  fv3d_status build_blocks(Ctx& ctx);
+  fv3d_status dots(Ctx& ctx, const double* w, const double* V, int k, std::vector<double>& out);
+  fv3d_status norm(Ctx& ctx, const double* v, double* out);
+  fv3d_status ICK_copy(Ctx& ctx, double* dst, const double* src);
+};
+
+}  // namespace fv3d

@@ -79,13 +79,6 @@ std::vector<int> rcm_order(int nc, const std::vector<std::vector<int>>& adj) {
   return order;
 }
 
-template <class R>
-void convert(const std::vector<double>& src, std::vector<char>& dst) {
-  dst.resize(src.size() * sizeof(R));
-  R* d = reinterpret_cast<R*>(dst.data());
-  for (size_t i = 0; i < src.size(); ++i) d[i] = (R)src[i];
-}
-
 }  // namespace
 
 fv3d_status prepare_mesh(Ctx& ctx, const fv3d_mesh_arrays& m) {
@@ -304,95 +297,106 @@ fv3d_status prepare_mesh(Ctx& ctx, const fv3d_mesh_arrays& m) {
     if (e__ != cudaSuccess) return ctx.cuda(e__, "device allocation");                        \
   } while (0)
 
+// Data every path needs; the FP64-path and mixed-path arrays follow in
+// ensure_fp64_path / ensure_mixed_path (the explicit path allocates the one
+// of its precision, the implicit solver both).
 fv3d_status upload_mesh(Ctx& ctx) {
   ctx.free_device();
   const int nc = ctx.nc, nf = ctx.nf;
-  std::vector<char> tmp;
   UP(ctx.d_perm, ctx.perm.data(), (size_t)nc);
   UP(ctx.d_fc0, ctx.h_fc0.data(), (size_t)nf);
   UP(ctx.d_fc1, ctx.h_fc1.data(), (size_t)nf);
   if (ctx.nb > 0) UP(ctx.d_fregion, ctx.h_fregion.data(), (size_t)ctx.nb);
   UP(ctx.d_cface, ctx.h_cface.data(), (size_t)nc * ctx.mcf);  // ctx.mcf = padded stride
-  std::vector<double> rvol(nc);
-  for (int i = 0; i < nc; ++i) rvol[i] = 1.0 / ctx.h_vol[i];  // s_volume (reconstruction.c:82)
-  auto up_r = [&](DevBuf<char>& b, const std::vector<double>& src) -> fv3d_status {
-    if (ctx.fp64()) convert<double>(src, tmp);
-    else convert<float>(src, tmp);
-    cudaError_t e = b.alloc(tmp.size());
-    if (e == cudaSuccess) e = cudaMemcpy(b.p, tmp.data(), tmp.size(), cudaMemcpyHostToDevice);
-    return ctx.cuda(e, "mesh upload");
-  };
-  fv3d_status st;
-  if ((st = up_r(ctx.d_geo, ctx.h_geo)) != FV3D_OK) return st;
-  if ((st = up_r(ctx.d_lam, ctx.h_lam)) != FV3D_OK) return st;
-  if ((st = up_r(ctx.d_lsq, ctx.h_lsq)) != FV3D_OK) return st;
-  if ((st = up_r(ctx.d_rvol, rvol)) != FV3D_OK) return st;
   UP(ctx.d_vol, ctx.h_vol.data(), (size_t)nc);
   UP(ctx.d_dx, ctx.h_dx.data(), (size_t)nc * 3);
   ALLOC(ctx.d_U, (size_t)nc * 5);
-  ALLOC(ctx.d_K, (size_t)nc * 5);
-  ALLOC(ctx.d_U0, (size_t)nc * 5);
   ALLOC(ctx.d_dphi, (size_t)nc * 5);
   ALLOC(ctx.d_stage, (size_t)nc * 10);
   ALLOC(ctx.d_part, (size_t)((nc + 255) / 256 + 1) * 5 + 5);
-  if (!ctx.fp64()) ALLOC(ctx.d_Uf, (size_t)nc * 8);
-  if (ctx.fp64()) {
-    ALLOC(ctx.d_rec, (size_t)nc * REC * ctx.rsize());
-    ALLOC(ctx.d_FA, (size_t)nf * FAS * ctx.rsize());
-  } else {
-    // mixed path: compact float4 geometry and per-face-side records
-    std::vector<int2> fcell(nf);
-    std::vector<float4> gN(nf), gD(2 * (size_t)nf), lw(2 * (size_t)nf);
-    for (int f = 0; f < nf; ++f) {
-      const double* g = &ctx.h_geo[(size_t)f * GEO];
-      fcell[f] = make_int2(ctx.h_fc0[f], ctx.h_fc1[f]);
-      gN[f] = make_float4((float)g[G_N], (float)g[G_N + 1], (float)g[G_N + 2], (float)g[G_A]);
-      gD[f] = make_float4((float)g[G_D1], (float)g[G_D1 + 1], (float)g[G_D1 + 2], (float)ctx.h_lam[f]);
-      gD[(size_t)nf + f] = make_float4((float)g[G_D2], (float)g[G_D2 + 1], (float)g[G_D2 + 2], (float)ctx.h_lam[f]);
-      const double* w = &ctx.h_lsq[6 * (size_t)f];
-      lw[f] = make_float4((float)w[0], (float)w[1], (float)w[2], 0.f);
-      lw[(size_t)nf + f] = make_float4((float)w[3], (float)w[4], (float)w[5], 0.f);
-    }
-    // per cell: sum_f s_f n_f A_f (closure of the Green-Gauss difference
-    // form) with 1/V, and (dx, V) for the time step
-    std::vector<float4> cg(nc), cd(nc);
-    for (int c = 0; c < nc; ++c) {
-      double S[3] = {0.0, 0.0, 0.0};
-      for (int k = 0; k < ctx.mcf; ++k) {
-        const int e = ctx.h_cface[(size_t)c * ctx.mcf + k];
-        if (e < 0) break;
-        const double* g = &ctx.h_geo[(size_t)(e >> 1) * GEO];
-        const double sg = (e & 1) ? -g[G_A] : g[G_A];
-        for (int d = 0; d < 3; ++d) S[d] += sg * g[G_N + d];
-      }
-      cg[c] = make_float4((float)S[0], (float)S[1], (float)S[2], (float)(1.0 / ctx.h_vol[c]));
-      cd[c] = make_float4((float)ctx.h_dx[3 * (size_t)c], (float)ctx.h_dx[3 * (size_t)c + 1],
-                          (float)ctx.h_dx[3 * (size_t)c + 2], (float)ctx.h_vol[c]);
-    }
-    UP(ctx.d_cgeo, cg.data(), (size_t)nc);
-    // neighbour of every face slot: cell, -1 for a ghost, -2 for padding
-    std::vector<int> nbr((size_t)nc * ctx.mcf, -2);
-    for (int c = 0; c < nc; ++c)
-      for (int k = 0; k < ctx.mcf; ++k) {
-        const int e = ctx.h_cface[(size_t)c * ctx.mcf + k];
-        if (e < 0) break;
-        const int f = e >> 1;
-        nbr[(size_t)c * ctx.mcf + k] = (f >= ctx.nf_int) ? -1 : ((e & 1) ? ctx.h_fc0[f] : ctx.h_fc1[f]);
-      }
-    UP(ctx.d_cnbr, nbr.data(), nbr.size());
-    UP(ctx.d_cdx, cd.data(), (size_t)nc);
-    ALLOC(ctx.d_UfN, (size_t)nc * 8);
-    ALLOC(ctx.d_kf, (size_t)nc * 5);
-    ALLOC(ctx.d_dU, (size_t)nc * 5);
-    UP(ctx.d_fcell, fcell.data(), (size_t)nf);
-    UP(ctx.d_geoN, gN.data(), (size_t)nf);
-    UP(ctx.d_geoD, gD.data(), 2 * (size_t)nf);
-    UP(ctx.d_lsqW, lw.data(), 2 * (size_t)nf);
-    ALLOC(ctx.d_fs, (size_t)nf * FREC);
-  }
   ALLOC(ctx.d_sc, 1);
   ALLOC(ctx.d_bits, 2);
   ctx.mesh_ready = true;
+  fv3d_status st = ctx.fp64() ? ensure_fp64_path(ctx) : ensure_mixed_path(ctx);
+  if (st != FV3D_OK) ctx.mesh_ready = false;
+  return st;
+}
+
+fv3d_status ensure_fp64_path(Ctx& ctx) {
+  if (ctx.d_rec.p != nullptr) return FV3D_OK;
+  const int nc = ctx.nc, nf = ctx.nf;
+  std::vector<double> rvol(nc);
+  for (int i = 0; i < nc; ++i) rvol[i] = 1.0 / ctx.h_vol[i];  // s_volume (reconstruction.c:82)
+  auto up_d = [&](DevBuf<char>& b, const std::vector<double>& src) -> fv3d_status {
+    cudaError_t e = b.alloc(src.size() * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemcpy(b.p, src.data(), src.size() * sizeof(double), cudaMemcpyHostToDevice);
+    return ctx.cuda(e, "mesh upload");
+  };
+  fv3d_status st;
+  if ((st = up_d(ctx.d_geo, ctx.h_geo)) != FV3D_OK) return st;
+  if ((st = up_d(ctx.d_lam, ctx.h_lam)) != FV3D_OK) return st;
+  if ((st = up_d(ctx.d_lsq, ctx.h_lsq)) != FV3D_OK) return st;
+  if ((st = up_d(ctx.d_rvol, rvol)) != FV3D_OK) return st;
+  ALLOC(ctx.d_K, (size_t)nc * 5);
+  ALLOC(ctx.d_U0, (size_t)nc * 5);
+  ALLOC(ctx.d_FA, (size_t)nf * FAS * sizeof(double));
+  ALLOC(ctx.d_rec, (size_t)nc * REC * sizeof(double));
+  return FV3D_OK;
+}
+
+fv3d_status ensure_mixed_path(Ctx& ctx) {
+  if (ctx.d_fs.p != nullptr) return FV3D_OK;
+  const int nc = ctx.nc, nf = ctx.nf;
+  // compact float4 geometry and per-face records
+  std::vector<int2> fcell(nf);
+  std::vector<float4> gN(nf), gD(2 * (size_t)nf), lw(2 * (size_t)nf);
+  for (int f = 0; f < nf; ++f) {
+    const double* g = &ctx.h_geo[(size_t)f * GEO];
+    fcell[f] = make_int2(ctx.h_fc0[f], ctx.h_fc1[f]);
+    gN[f] = make_float4((float)g[G_N], (float)g[G_N + 1], (float)g[G_N + 2], (float)g[G_A]);
+    gD[f] = make_float4((float)g[G_D1], (float)g[G_D1 + 1], (float)g[G_D1 + 2], (float)ctx.h_lam[f]);
+    gD[(size_t)nf + f] = make_float4((float)g[G_D2], (float)g[G_D2 + 1], (float)g[G_D2 + 2], (float)ctx.h_lam[f]);
+    const double* w = &ctx.h_lsq[6 * (size_t)f];
+    lw[f] = make_float4((float)w[0], (float)w[1], (float)w[2], 0.f);
+    lw[(size_t)nf + f] = make_float4((float)w[3], (float)w[4], (float)w[5], 0.f);
+  }
+  // per cell: sum_f s_f n_f A_f (closure of the Green-Gauss difference
+  // form) with 1/V, and (dx, V) for the time step
+  std::vector<float4> cg(nc), cd(nc);
+  for (int c = 0; c < nc; ++c) {
+    double S[3] = {0.0, 0.0, 0.0};
+    for (int k = 0; k < ctx.mcf; ++k) {
+      const int e = ctx.h_cface[(size_t)c * ctx.mcf + k];
+      if (e < 0) break;
+      const double* g = &ctx.h_geo[(size_t)(e >> 1) * GEO];
+      const double sg = (e & 1) ? -g[G_A] : g[G_A];
+      for (int d = 0; d < 3; ++d) S[d] += sg * g[G_N + d];
+    }
+    cg[c] = make_float4((float)S[0], (float)S[1], (float)S[2], (float)(1.0 / ctx.h_vol[c]));
+    cd[c] = make_float4((float)ctx.h_dx[3 * (size_t)c], (float)ctx.h_dx[3 * (size_t)c + 1],
+                        (float)ctx.h_dx[3 * (size_t)c + 2], (float)ctx.h_vol[c]);
+  }
+  // neighbour of every face slot: cell, -1 for a ghost, -2 for padding
+  std::vector<int> nbr((size_t)nc * ctx.mcf, -2);
+  for (int c = 0; c < nc; ++c)
+    for (int k = 0; k < ctx.mcf; ++k) {
+      const int e = ctx.h_cface[(size_t)c * ctx.mcf + k];
+      if (e < 0) break;
+      const int f = e >> 1;
+      nbr[(size_t)c * ctx.mcf + k] = (f >= ctx.nf_int) ? -1 : ((e & 1) ? ctx.h_fc0[f] : ctx.h_fc1[f]);
+    }
+  UP(ctx.d_cgeo, cg.data(), (size_t)nc);
+  UP(ctx.d_cdx, cd.data(), (size_t)nc);
+  UP(ctx.d_cnbr, nbr.data(), nbr.size());
+  UP(ctx.d_fcell, fcell.data(), (size_t)nf);
+  UP(ctx.d_geoN, gN.data(), (size_t)nf);
+  UP(ctx.d_geoD, gD.data(), 2 * (size_t)nf);
+  UP(ctx.d_lsqW, lw.data(), 2 * (size_t)nf);
+  ALLOC(ctx.d_Uf, (size_t)nc * 8);
+  ALLOC(ctx.d_UfN, (size_t)nc * 8);
+  ALLOC(ctx.d_kf, (size_t)nc * 5);
+  ALLOC(ctx.d_dU, (size_t)nc * 5);
+  ALLOC(ctx.d_fs, (size_t)nf * FREC);
   return FV3D_OK;
 }
 

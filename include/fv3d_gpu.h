@@ -157,6 +157,50 @@ fv3d_status fv3d_step_explicit(fv3d_ctx *ctx, int scheme, int n_steps, double cf
 /* calc_global_residual (analyze.c:37-61) of the last residual evaluation */
 fv3d_status fv3d_global_residual(fv3d_ctx *ctx, double dt, double res[5]);
 
+/* ---- implicit steady solve ---------------------------------------------------- */
+/* Pseudo-transient Newton-Krylov replacing timestep_newton / calc_jacobian_
+ * numerical / the basec Krylov call (implicit.c:61-351): backward Euler with
+ * local time steps and a CFL ramp, matrix-free finite-difference J v,
+ * FGMRES(krylov_dim) with FP64 Arnoldi, batched 5x5 block-Jacobi
+ * preconditioning.  Iterates until ||R||_2 / ||R_0||_2 <= tol_rel. */
+enum {
+    FV3D_PC_BLOCK_JACOBI = 0,  /* first-order diagonal blocks (FD, FP64 build, FP32 apply) */
+    FV3D_PC_LUMPED = 1,        /* the reference's lumped blocks (implicit.c:61-119) */
+    FV3D_PC_LEARNED = 2,       /* per-cell MLP, block-Jacobi fallback on stagnation */
+    FV3D_PC_NONE = 3
+};
+typedef struct fv3d_implicit_opts {
+    double cfl_start;      /* initial CFL (100) */
+    double cfl_max;        /* CFL cap of the ramp (1e4) */
+    double tol_rel;        /* stop at ||R|| / ||R_0|| <= tol_rel (1e-8) */
+    int max_newton;        /* Newton step limit (500) */
+    int krylov_dim;        /* FGMRES restart length, 1..31 (30) */
+    double eta;            /* linear relative tolerance per Newton step (1e-2) */
+    double fd_eps;         /* relative finite-difference step of FP64 J v (1e-7) */
+    int jv_precision;      /* 0: J v from the FP64 residual, 1: from the FP32 residual */
+    int preconditioner;    /* FV3D_PC_* */
+    int pc_refresh;        /* rebuild the blocks every pc_refresh Newton steps */
+} fv3d_implicit_opts;
+typedef struct fv3d_implicit_stats {
+    int newton_steps;
+    int gmres_iterations;
+    int jv_evaluations;
+    int rejected_steps;    /* Newton updates refused (non-positive state) and retried */
+    int fallbacks;         /* learned-preconditioner solves redone with block Jacobi */
+    int converged;
+    double res0, res_final, rel_res;
+    double wall_ms;
+    double cfl_final;
+} fv3d_implicit_stats;
+fv3d_status fv3d_implicit_default_opts(fv3d_implicit_opts *opts);
+fv3d_status fv3d_solve_implicit(fv3d_ctx *ctx, const fv3d_implicit_opts *opts,
+                                fv3d_implicit_stats *stats);
+/* ||R||_2 after each Newton step of the last solve; *count = steps recorded */
+fv3d_status fv3d_implicit_history(const fv3d_ctx *ctx, double *res, int max, int *count);
+/* 5x5 blocks of the last preconditioner build, [n_cells][25] column-major,
+ * reference cell order (lumped blocks: compare with calc_jacobian_numerical) */
+fv3d_status fv3d_get_blocks(fv3d_ctx *ctx, double *blocks);
+
 /* ---- measurement helpers ------------------------------------------------------ */
 /* average device time (ms) per launch of each explicit-stage kernel over
  * n_reps stages, each bracketed by CUDA events on the context stream:

@@ -224,6 +224,8 @@ KArgs<R> Ctx::args() const {
   return a;
 }
 
+template KArgs<double> Ctx::args<double>() const;
+
 MxArgs Ctx::mx_args() const {
   MxArgs a;
   memset(&a, 0, sizeof(a));

@@ -57,14 +57,16 @@ def test_fp32_and_fp64_jv_reach_the_same_steady_state():
     assert (np.abs(sols[0] - sols[1]).max(axis=0) / scale).max() < 1e-6
 
 
-def test_block_jacobi_reduces_krylov_work():
+def test_block_jacobi_reduces_work():
+    """Krylov iterations (= J v products) to reach 1e-6 with the block-Jacobi
+    preconditioner versus none."""
     c = small_channel()
-    its = {}
+    work = {}
     for pc in ("block_jacobi", "none"):
         with api.from_case(c, "fp64") as s:
-            st = s.solve_implicit(preconditioner=pc, tol_rel=1e-4, max_newton=60, check=False)
-            its[pc] = st["gmres_iterations"] / max(1, st["newton_steps"])
-    assert its["block_jacobi"] < its["none"]
+            st = s.solve_implicit(preconditioner=pc, tol_rel=1e-6, max_newton=300, check=False)
+            work[pc] = st["jv_evaluations"] if st["converged"] else 10 ** 9
+    assert work["block_jacobi"] < work["none"]
 
 
 def test_lumped_blocks_available():

@@ -491,67 +491,85 @@ fv3d_status Implicit::build_blocks(Ctx& ctx) {
   return FV3D_OK;
 }
 
-// FGMRES(m) for (I/dt - J) x = R, x0 = 0; returns iterations
+// restarted FGMRES(m) for (I/dt - J) x = R, x0 = 0; returns iterations
 fv3d_status Implicit::fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res) {
   const int m = opts.krylov_dim;
-  std::vector<double> H((size_t)(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0), y(m);
-  // V_0 = R / ||R||
-  k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0 / rnorm, R.p, 0.0, nullptr, V.p);
-  ICK(cudaGetLastError());
-  g[0] = rnorm;
-  int k = 0;
-  double res = rnorm;
-  for (; k < m; ++k) {
-    double* vk = V.p + (size_t)k * n;
-    double* zk = Z.p + (size_t)k * n;
-    fv3d_status st = precondition(ctx, vk, zk);
-    if (st != FV3D_OK) return st;
-    st = apply_A(ctx, zk, w.p);
-    if (st != FV3D_OK) return st;
-    // classical Gram-Schmidt, twice
-    std::vector<double> h1, h2;
-    if ((st = dots(ctx, w.p, V.p, k + 1, h1)) != FV3D_OK) return st;
-    k_multi_axpy<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, w.p, V.p, hdev.p, k + 1, -1.0);
-    if ((st = dots(ctx, w.p, V.p, k + 1, h2)) != FV3D_OK) return st;
-    k_multi_axpy<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, w.p, V.p, hdev.p, k + 1, -1.0);
-    ICK(cudaGetLastError());
-    double hn = 0.0;
-    if ((st = norm(ctx, w.p, &hn)) != FV3D_OK) return st;
-    for (int j = 0; j <= k; ++j) H[(size_t)k * (m + 1) + j] = h1[j] + h2[j];
-    H[(size_t)k * (m + 1) + k + 1] = hn;
-    if (hn > 0.0) {
-      k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0 / hn, w.p, 0.0, nullptr,
-                                                                  V.p + (size_t)(k + 1) * n);
-      ICK(cudaGetLastError());
-    }
-    // Givens rotations on the new column
-    for (int j = 0; j < k; ++j) {
-      const double a = H[(size_t)k * (m + 1) + j], b = H[(size_t)k * (m + 1) + j + 1];
-      H[(size_t)k * (m + 1) + j] = cs[j] * a + sn[j] * b;
-      H[(size_t)k * (m + 1) + j + 1] = -sn[j] * a + cs[j] * b;
-    }
-    const double a = H[(size_t)k * (m + 1) + k], b = H[(size_t)k * (m + 1) + k + 1];
-    const double r = sqrt(a * a + b * b);
-    cs[k] = (r > 0.0) ? a / r : 1.0;
-    sn[k] = (r > 0.0) ? b / r : 0.0;
-    H[(size_t)k * (m + 1) + k] = r;
-    H[(size_t)k * (m + 1) + k + 1] = 0.0;
-    g[k + 1] = -sn[k] * g[k];
-    g[k] = cs[k] * g[k];
-    res = fabs(g[k + 1]);
-    if (res <= opts.eta * rnorm || !(hn > 0.0)) { ++k; break; }
-  }
-  for (int i = k - 1; i >= 0; --i) {
-    double s = g[i];
-    for (int j = i + 1; j < k; ++j) s -= H[(size_t)j * (m + 1) + i] * y[j];
-    y[i] = s / H[(size_t)i * (m + 1) + i];
-  }
-  // x = Z y
-  ICK(cudaMemcpyAsync(hdev.p, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, ctx.stream));
+  std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
   ICK(cudaMemsetAsync(x.p, 0, sizeof(double) * n, ctx.stream));
-  k_multi_axpy<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, x.p, Z.p, hdev.p, k, 1.0);
-  ICK(cudaGetLastError());
-  *iters = k;
+  int total = 0;
+  double res = rnorm;
+  for (int cyc = 0; cyc <= std::max(0, opts.max_restarts); ++cyc) {
+    double beta = rnorm;
+    if (cyc == 0) {
+      k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0 / rnorm, R.p, 0.0, nullptr, V.p);
+    } else {
+      // true residual of the current iterate: R - A x
+      fv3d_status st = apply_A(ctx, x.p, w.p);
+      if (st != FV3D_OK) return st;
+      k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0, R.p, -1.0, w.p, w.p);
+      if ((st = norm(ctx, w.p, &beta)) != FV3D_OK) return st;
+      if (!(beta > opts.eta * rnorm)) { res = beta; break; }
+      k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0 / beta, w.p, 0.0, nullptr, V.p);
+    }
+    ICK(cudaGetLastError());
+    std::fill(H.begin(), H.end(), 0.0);
+    std::fill(g.begin(), g.end(), 0.0);
+    g[0] = beta;
+    int k = 0;
+    bool done = false;
+    for (; k < m; ++k) {
+      double* vk = V.p + (size_t)k * n;
+      double* zk = Z.p + (size_t)k * n;
+      fv3d_status st = precondition(ctx, vk, zk);
+      if (st != FV3D_OK) return st;
+      st = apply_A(ctx, zk, w.p);
+      if (st != FV3D_OK) return st;
+      // classical Gram-Schmidt, twice
+      std::vector<double> h1, h2;
+      if ((st = dots(ctx, w.p, V.p, k + 1, h1)) != FV3D_OK) return st;
+      k_multi_axpy<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, w.p, V.p, hdev.p, k + 1, -1.0);
+      if ((st = dots(ctx, w.p, V.p, k + 1, h2)) != FV3D_OK) return st;
+      k_multi_axpy<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, w.p, V.p, hdev.p, k + 1, -1.0);
+      ICK(cudaGetLastError());
+      double hn = 0.0;
+      if ((st = norm(ctx, w.p, &hn)) != FV3D_OK) return st;
+      for (int j = 0; j <= k; ++j) H[(size_t)k * (m + 1) + j] = h1[j] + h2[j];
+      H[(size_t)k * (m + 1) + k + 1] = hn;
+      if (hn > 0.0) {
+        k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0 / hn, w.p, 0.0, nullptr,
+                                                                    V.p + (size_t)(k + 1) * n);
+        ICK(cudaGetLastError());
+      }
+      // Givens rotations on the new column
+      for (int j = 0; j < k; ++j) {
+        const double a = H[(size_t)k * (m + 1) + j], b = H[(size_t)k * (m + 1) + j + 1];
+        H[(size_t)k * (m + 1) + j] = cs[j] * a + sn[j] * b;
+        H[(size_t)k * (m + 1) + j + 1] = -sn[j] * a + cs[j] * b;
+      }
+      const double a = H[(size_t)k * (m + 1) + k], b = H[(size_t)k * (m + 1) + k + 1];
+      const double r = sqrt(a * a + b * b);
+      cs[k] = (r > 0.0) ? a / r : 1.0;
+      sn[k] = (r > 0.0) ? b / r : 0.0;
+      H[(size_t)k * (m + 1) + k] = r;
+      H[(size_t)k * (m + 1) + k + 1] = 0.0;
+      g[k + 1] = -sn[k] * g[k];
+      g[k] = cs[k] * g[k];
+      res = fabs(g[k + 1]);
+      if (res <= opts.eta * rnorm || !(hn > 0.0)) { ++k; done = true; break; }
+    }
+    for (int i = k - 1; i >= 0; --i) {
+      double s = g[i];
+      for (int j = i + 1; j < k; ++j) s -= H[(size_t)j * (m + 1) + i] * y[j];
+      y[i] = s / H[(size_t)i * (m + 1) + i];
+    }
+    // x += Z y
+    ICK(cudaMemcpyAsync(hdev.p, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, ctx.stream));
+    k_multi_axpy<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, x.p, Z.p, hdev.p, k, 1.0);
+    ICK(cudaGetLastError());
+    total += k;
+    if (done) break;
+  }
+  *iters = total;
   *rel_res = res / rnorm;
   return FV3D_OK;
 }
@@ -655,6 +673,7 @@ extern "C" fv3d_status fv3d_implicit_default_opts(fv3d_implicit_opts* o) {
   o->jv_precision = 1;
   o->preconditioner = FV3D_PC_BLOCK_JACOBI;
   o->pc_refresh = 1;
+  o->max_restarts = 0;
   return FV3D_OK;
 }
 

@@ -38,6 +38,19 @@ namespace fv3d {
 #ifndef FV3D_SIDES_MINBLOCKS
 #define FV3D_SIDES_MINBLOCKS 2
 #endif
+// unroll factor of the gradient-pass neighbour loop (1 keeps one neighbour
+// live at a time: fewer registers, more resident warps)
+#ifndef FV3D_SIDES_UNROLL
+#define FV3D_SIDES_UNROLL 8
+#endif
+#ifndef FV3D_FLUX_MINBLOCKS
+#define FV3D_FLUX_MINBLOCKS 1
+#endif
+#ifndef FV3D_FLUX_UNROLL
+#define FV3D_FLUX_UNROLL 8
+#endif
+constexpr int kSidesUnroll = FV3D_SIDES_UNROLL;
+constexpr int kFluxUnroll = FV3D_FLUX_UNROLL;
 
 // face record: side s at float4 [2s, 2s+1] = (rho, mx, my, mz), (E, vmx, vmy, vmz);
 // float4 [4] = (ve side 0, ve side 1, -, -).  v* = viscous normal flux times A.
@@ -193,7 +206,7 @@ __global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __
 #pragma unroll
   for (int v = 0; v < 8; ++v) { mn[v] = q[v]; mxv[v] = q[v]; }
   if (GMODE != 0) {
-#pragma unroll
+#pragma unroll kSidesUnroll
     for (int k = 0; k < MCF; ++k) {
       if (o[k] == -2) continue;
       const int f = e[k] >> 1, side = e[k] & 1;
@@ -386,7 +399,7 @@ __device__ __forceinline__ void mx_store_state(float4* dst, float rho, float mx,
 // MODE 0: residual only; 1: low-storage RK stage; 2: SSP-RK3 stage.
 // co.first / co.last mark the step's first and last stage.
 template <int MCF, int MODE, bool DT, bool VISC>
-__global__ void __launch_bounds__(256) k_mx_flux_update(const __grid_constant__ MxArgs a,
+__global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(const __grid_constant__ MxArgs a,
                                                         StageCoef co) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long lam_bits = 0x7ff0000000000000ull;
@@ -397,7 +410,7 @@ __global__ void __launch_bounds__(256) k_mx_flux_update(const __grid_constant__ 
     int e[MCF];
     load_cface<MCF>(a.cface + (size_t)c * MCF, e);
     Acc<float, true> s[5];
-#pragma unroll
+#pragma unroll kFluxUnroll
     for (int k = 0; k < MCF; ++k) {
       if (e[k] < 0) continue;
       const int f = e[k] >> 1, side = e[k] & 1;

@@ -180,6 +180,7 @@ typedef struct fv3d_implicit_opts {
     int jv_precision;      /* 0: J v from the FP64 residual, 1: from the FP32 residual */
     int preconditioner;    /* FV3D_PC_* */
     int pc_refresh;        /* rebuild the blocks every pc_refresh Newton steps */
+    int max_restarts;      /* FGMRES restarts per Newton step (0: one cycle) */
 } fv3d_implicit_opts;
 typedef struct fv3d_implicit_stats {
     int newton_steps;

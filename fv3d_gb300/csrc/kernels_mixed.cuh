@@ -52,24 +52,26 @@ namespace fv3d {
 constexpr int kSidesUnroll = FV3D_SIDES_UNROLL;
 constexpr int kFluxUnroll = FV3D_FLUX_UNROLL;
 
-// face record: side s at float4 [2s, 2s+1] = (rho, mx, my, mz), (E, vmx, vmy, vmz);
-// float4 [4] = (ve side 0, ve side 1, -, -).  v* = viscous normal flux times A.
-constexpr int FREC = 20;
+// face record: side s at float4 [2s, 2s+1] = (rho, mx, my, mz), (E, vmx, vmy, vmz)
+// (two full 32-byte sectors per face); the viscous energy flux of side s in
+// fsv[2f + s].  v* = viscous normal flux times A.
+constexpr int FREC = 16;
 
 struct MxArgs {
   int nc, nf, nf_int, mcf;
   const int* __restrict__ cface;     // [nc][mcf]
   const int* __restrict__ cnbr;      // [nc][mcf] neighbour cell, -1 ghost, -2 none
   const int2* __restrict__ fcell;    // [nf] (cell 0, cell 1 or ghost)
-  const float4* __restrict__ geoN;   // [nf] (n, A)
-  const float4* __restrict__ geoD;   // [2][nf] (d_side, lambda)
-  const float4* __restrict__ lsqW;   // [2][nf] (w_side, 0)
+  const float4* __restrict__ slotN;  // [nc][mcf] face (n, A), cell 0 -> cell 1 orientation
+  const float4* __restrict__ slotD;  // [nc][mcf] (d of this side, Green-Gauss weight)
+  const float4* __restrict__ slotW;  // [nc][mcf] least-squares weights of this side
   const int* __restrict__ fregion;   // [nf - nf_int]
   const float4* __restrict__ cgeo;   // [nc] (sum_f s_f n_f A_f, 1/V)
   const float4* __restrict__ cdx;    // [nc] (dx, V)
   float* Uf;                         // [nc][8] stage state (rho, m, E, p, T, -)
   float* UfN;                        // [nc][8] float(U_n) + p, T
   float* fs;                         // [nf][FREC]
+  float* fsv;                        // [nf][2]
   double* U;                         // [5][nc] conserved state U_n (FP64)
   float* kf;                         // [5][nc] RK register (FP32)
   float* dU;                         // [5][nc] U_stage - U_n (FP32)
@@ -210,7 +212,7 @@ __global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __
     for (int k = 0; k < MCF; ++k) {
       if (o[k] == -2) continue;
       const int f = e[k] >> 1, side = e[k] & 1;
-      const float4 nA = __ldg(&a.geoN[f]);
+      const float4 nA = __ldg(&a.slotN[(size_t)c * MCF + k]);
       float qo[10];
       if (o[k] < 0) {
         const float n[3] = {nA.x, nA.y, nA.z};
@@ -223,8 +225,7 @@ __global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __
         // s_f mean_f nA_f = s_f q_c nA_f + s_f w_f (q_o - q_c) nA_f with
         // w = lambda (cell 0 side) or 1 - lambda (cell 1 side); the q_c
         // terms are added once per cell through sum_f s_f nA_f below
-        const float lam = __ldg(&a.geoD[f]).w;
-        const float w = side ? (nA.w - lam * nA.w) : lam * nA.w;
+        const float w = __ldg(&a.slotD[(size_t)c * MCF + k]).w * nA.w;
         const float sw = side ? -w : w;
         const float ax = nA.x * sw, ay = nA.y * sw, az = nA.z * sw;
 #pragma unroll
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __
           g[v][2] += dq * az;
         }
       } else {
-        const float4 wl = __ldg(&a.lsqW[(size_t)side * a.nf + f]);
+        const float4 wl = __ldg(&a.slotW[(size_t)c * MCF + k]);
 #pragma unroll
         for (int v = 0; v < NG; ++v) {
           const int j = (v < 8) ? v : TT;
@@ -276,11 +277,11 @@ __global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __
   for (int k = 0; k < MCF; ++k) {
     if (o[k] == -2) continue;
     const int f = e[k] >> 1, side = e[k] & 1;
-    const float4 nA4 = __ldg(&a.geoN[f]);
+    const float4 nA4 = __ldg(&a.slotN[(size_t)c * MCF + k]);
     const float nA[3] = {nA4.x * nA4.w, nA4.y * nA4.w, nA4.z * nA4.w};
     float r[12];
     if (LINEAR) {
-      const float4 d = __ldg(&a.geoD[(size_t)side * a.nf + f]);
+      const float4 d = __ldg(&a.slotD[(size_t)c * MCF + k]);
 #pragma unroll
       for (int v = 0; v < 8; ++v) {
         const float slope = d.x * g[v][0] + d.y * g[v][1] + d.z * g[v][2];
@@ -298,7 +299,7 @@ __global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __
     rec[2 * side] = make_float4(r[0], r[1], r[2], r[3]);
     if (VISC) {
       rec[2 * side + 1] = make_float4(r[4], r[8], r[9], r[10]);
-      a.fs[(size_t)f * FREC + 16 + side] = r[11];
+      a.fsv[2 * (size_t)f + side] = r[11];
     } else {
       rec[2 * side + 1] = make_float4(r[4], 0.f, 0.f, 0.f);
     }
@@ -332,7 +333,7 @@ __global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __
           gT[0] = gm[9]; gT[1] = gm[10]; gT[2] = gm[11];
         }
         mx_viscous(gq, tg, gT, nA, ph, vg);
-        a.fs[(size_t)f * FREC + 17] = vg[3];
+        a.fsv[2 * (size_t)f + 1] = vg[3];
       }
       rec[2] = make_float4(gq[0], gq[1], gq[2], gq[3]);
       rec[3] = make_float4(gq[4], vg[0], vg[1], vg[2]);
@@ -418,11 +419,11 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
       const float4 l0 = __ldg(src + 0), l1 = __ldg(src + 1), r0 = __ldg(src + 2), r1 = __ldg(src + 3);
       const float l[5] = {l0.x, l0.y, l0.z, l0.w, l1.x};
       const float r[5] = {r0.x, r0.y, r0.z, r0.w, r1.x};
-      const float4 nA = __ldg(&a.geoN[f]);
+      const float4 nA = __ldg(&a.slotN[(size_t)c * MCF + k]);
       float F[5];
       mx_conv_flux(l, r, nA, ph, F);
       if (VISC) {
-        const float2 ve = __ldg(reinterpret_cast<const float2*>(src + 4));
+        const float2 ve = __ldg(reinterpret_cast<const float2*>(a.fsv) + f);
         F[1] += 0.5f * (l1.y + r1.y);
         F[2] += 0.5f * (l1.z + r1.z);
         F[3] += 0.5f * (l1.w + r1.w);

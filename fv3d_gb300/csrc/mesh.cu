@@ -347,19 +347,28 @@ fv3d_status ensure_fp64_path(Ctx& ctx) {
 fv3d_status ensure_mixed_path(Ctx& ctx) {
   if (ctx.d_fs.p != nullptr) return FV3D_OK;
   const int nc = ctx.nc, nf = ctx.nf;
-  // compact float4 geometry and per-face records
+  // per (cell, face slot) geometry, read coalesced by the cell kernels:
+  // face (n, A) in its cell 0 -> cell 1 orientation, this side's d with the
+  // Green-Gauss weight (lambda on the cell-0 side, 1 - lambda on the cell-1
+  // side), this side's least-squares weights
+  const int mcf = ctx.mcf;
   std::vector<int2> fcell(nf);
-  std::vector<float4> gN(nf), gD(2 * (size_t)nf), lw(2 * (size_t)nf);
-  for (int f = 0; f < nf; ++f) {
-    const double* g = &ctx.h_geo[(size_t)f * GEO];
-    fcell[f] = make_int2(ctx.h_fc0[f], ctx.h_fc1[f]);
-    gN[f] = make_float4((float)g[G_N], (float)g[G_N + 1], (float)g[G_N + 2], (float)g[G_A]);
-    gD[f] = make_float4((float)g[G_D1], (float)g[G_D1 + 1], (float)g[G_D1 + 2], (float)ctx.h_lam[f]);
-    gD[(size_t)nf + f] = make_float4((float)g[G_D2], (float)g[G_D2 + 1], (float)g[G_D2 + 2], (float)ctx.h_lam[f]);
-    const double* w = &ctx.h_lsq[6 * (size_t)f];
-    lw[f] = make_float4((float)w[0], (float)w[1], (float)w[2], 0.f);
-    lw[(size_t)nf + f] = make_float4((float)w[3], (float)w[4], (float)w[5], 0.f);
-  }
+  for (int f = 0; f < nf; ++f) fcell[f] = make_int2(ctx.h_fc0[f], ctx.h_fc1[f]);
+  std::vector<float4> sN((size_t)nc * mcf, make_float4(0.f, 0.f, 0.f, 0.f)), sD(sN), sW(sN);
+  for (int c = 0; c < nc; ++c)
+    for (int k = 0; k < mcf; ++k) {
+      const int e = ctx.h_cface[(size_t)c * mcf + k];
+      if (e < 0) break;
+      const int f = e >> 1, side = e & 1;
+      const double* g = &ctx.h_geo[(size_t)f * GEO];
+      const size_t i = (size_t)c * mcf + k;
+      sN[i] = make_float4((float)g[G_N], (float)g[G_N + 1], (float)g[G_N + 2], (float)g[G_A]);
+      const double* d = side ? &g[G_D2] : &g[G_D1];
+      const double w = side ? 1.0 - ctx.h_lam[f] : ctx.h_lam[f];
+      sD[i] = make_float4((float)d[0], (float)d[1], (float)d[2], (float)w);
+      const double* lw = &ctx.h_lsq[6 * (size_t)f + 3 * side];
+      sW[i] = make_float4((float)lw[0], (float)lw[1], (float)lw[2], 0.f);
+    }
   // per cell: sum_f s_f n_f A_f (closure of the Green-Gauss difference
   // form) with 1/V, and (dx, V) for the time step
   std::vector<float4> cg(nc), cd(nc);
@@ -389,14 +398,15 @@ fv3d_status ensure_mixed_path(Ctx& ctx) {
   UP(ctx.d_cdx, cd.data(), (size_t)nc);
   UP(ctx.d_cnbr, nbr.data(), nbr.size());
   UP(ctx.d_fcell, fcell.data(), (size_t)nf);
-  UP(ctx.d_geoN, gN.data(), (size_t)nf);
-  UP(ctx.d_geoD, gD.data(), 2 * (size_t)nf);
-  UP(ctx.d_lsqW, lw.data(), 2 * (size_t)nf);
+  UP(ctx.d_slotN, sN.data(), sN.size());
+  UP(ctx.d_slotD, sD.data(), sD.size());
+  if (ctx.cfg.gradient == FV3D_GRADIENT_LEAST_SQUARES) UP(ctx.d_slotW, sW.data(), sW.size());
   ALLOC(ctx.d_Uf, (size_t)nc * 8);
   ALLOC(ctx.d_UfN, (size_t)nc * 8);
   ALLOC(ctx.d_kf, (size_t)nc * 5);
   ALLOC(ctx.d_dU, (size_t)nc * 5);
   ALLOC(ctx.d_fs, (size_t)nf * FREC);
+  ALLOC(ctx.d_fsv, (size_t)nf * 2);
   return FV3D_OK;
 }
 

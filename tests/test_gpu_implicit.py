@@ -55,20 +55,26 @@ def test_fp32_and_fp64_jv_reach_the_same_steady_state():
             sols.append(s.get_conserved())
     # both satisfy the FP64 steady equations to 1e-8 (checked against the
     # oracle above); the states agree to the accuracy that implies
-    scale = np.abs(sols[0]).max(axis=0)
-    assert (np.abs(sols[0] - sols[1]).max(axis=0) / scale).max() < 1e-4
+    scale = np.maximum(np.abs(sols[0]).max(axis=0), 0.3 * np.abs(sols[0][:, 0]).max())
+    assert (np.abs(sols[0] - sols[1]).max(axis=0) / scale).max() < 1e-6
 
 
-def test_block_jacobi_reduces_work():
-    """Krylov iterations (= J v products) to reach 1e-6 with the block-Jacobi
-    preconditioner versus none."""
+def test_lumped_blocks_match_reference_jacobian(oracle):
+    """The reference's lumped blocks (implicit.c:61-119: every cell perturbed
+    at once by +-eps/2, eps = 1e-4 ||U_v||) from the GPU FP64 residual against
+    the oracle's calc_jacobian_numerical.  Off-diagonal entries only: the
+    diagonal also carries 1/dt, global in the reference and local here."""
     c = small_channel()
-    work = {}
-    for pc in ("block_jacobi", "none"):
-        with api.from_case(c, "fp64") as s:
-            st = s.solve_implicit(preconditioner=pc, tol_rel=1e-6, max_newton=300, check=False)
-            work[pc] = st["jv_evaluations"] if st["converged"] else 10 ** 9
-    assert work["block_jacobi"] < work["none"]
+    oracle.init(c.mesh, c.params, c.region_type, c.region_prim)
+    oracle.set_conserved(c.u0)
+    oracle.step_newton(0, 0.0, 1e-3, scheme=0, solver=1, max_iter_inner=3, is_transient=False)
+    ref = oracle.jacobian()                       # [cell, col, row]
+    with api.from_case(c, "fp64") as s:
+        s.solve_implicit(preconditioner="lumped", tol_rel=1e-12, max_newton=1, check=False)
+        gpu = s.blocks()
+    off = ~np.eye(5, dtype=bool)
+    scale = np.abs(ref).max()
+    assert np.abs(gpu[:, off] - ref[:, off]).max() / scale < 1e-6
 
 
 def test_lumped_blocks_available():

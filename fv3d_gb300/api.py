@@ -76,6 +76,17 @@ class ImplicitStats(C.Structure):
                 ("rel_res", C.c_double), ("wall_ms", C.c_double), ("cfl_final", C.c_double)]
 
 
+class MlpTrainOpts(C.Structure):
+    _fields_ = [("epochs", C.c_int), ("batch", C.c_int), ("lr", C.c_double), ("seed", C.c_ulonglong)]
+
+
+class MlpTrainStats(C.Structure):
+    _fields_ = [("loss_first", C.c_double), ("loss_last", C.c_double), ("samples", C.c_int),
+                ("steps", C.c_int), ("wall_ms", C.c_double)]
+
+
+_f4p = C.POINTER(C.c_float)
+
 PRECONDITIONERS = {"block_jacobi": 0, "lumped": 1, "learned": 2, "none": 3}
 
 EXPORTS = {
@@ -102,6 +113,15 @@ EXPORTS = {
     "fv3d_solve_implicit": ([C.c_void_p, C.POINTER(ImplicitOpts), C.POINTER(ImplicitStats)], C.c_int),
     "fv3d_implicit_history": ([C.c_void_p, _f8p, C.c_int, C.POINTER(C.c_int)], C.c_int),
     "fv3d_get_blocks": ([C.c_void_p, _f8p], C.c_int),
+    "fv3d_mlp_num_params": ([], C.c_int),
+    "fv3d_mlp_init": ([C.c_void_p, C.c_ulonglong], C.c_int),
+    "fv3d_mlp_get_params": ([C.c_void_p, _f4p], C.c_int),
+    "fv3d_mlp_set_params": ([C.c_void_p, _f4p], C.c_int),
+    "fv3d_mlp_forward": ([C.c_void_p, _f4p, C.c_int, _f4p], C.c_int),
+    "fv3d_mlp_grad": ([C.c_void_p, _f4p, _f4p, C.c_int, _f8p, _f4p], C.c_int),
+    "fv3d_mlp_harvest": ([C.c_void_p, C.c_int, C.c_int], C.c_int),
+    "fv3d_mlp_dataset": ([C.c_void_p, C.POINTER(C.c_int)], C.c_int),
+    "fv3d_mlp_train": ([C.c_void_p, C.POINTER(MlpTrainOpts), C.POINTER(MlpTrainStats)], C.c_int),
 }
 
 _lib = None
@@ -261,6 +281,48 @@ class Solver:
         out = np.empty((self.nc, 5, 5))
         self._check(self.lib.fv3d_get_blocks(self.h, _p(out, _f8p)))
         return out  # out[i, col, row]
+
+    # ---- learned preconditioner ----
+    def mlp_init(self, seed: int = 1):
+        self._check(self.lib.fv3d_mlp_init(self.h, seed))
+
+    def mlp_params(self):
+        out = np.empty(self.lib.fv3d_mlp_num_params(), dtype=np.float32)
+        self._check(self.lib.fv3d_mlp_get_params(self.h, _p(out, _f4p)))
+        return out
+
+    def mlp_set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        self._check(self.lib.fv3d_mlp_set_params(self.h, _p(p, _f4p)))
+
+    def mlp_forward(self, X):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        Y = np.empty((X.shape[0], 5), dtype=np.float32)
+        self._check(self.lib.fv3d_mlp_forward(self.h, _p(X, _f4p), X.shape[0], _p(Y, _f4p)))
+        return Y
+
+    def mlp_grad(self, X, T):
+        X = np.ascontiguousarray(X, dtype=np.float32)
+        T = np.ascontiguousarray(T, dtype=np.float32)
+        g = np.empty(self.lib.fv3d_mlp_num_params(), dtype=np.float32)
+        loss = C.c_double()
+        self._check(self.lib.fv3d_mlp_grad(self.h, _p(X, _f4p), _p(T, _f4p), X.shape[0],
+                                           C.byref(loss), _p(g, _f4p)))
+        return loss.value, g
+
+    def mlp_harvest(self, per_step: int, max_samples: int):
+        self._check(self.lib.fv3d_mlp_harvest(self.h, per_step, max_samples))
+
+    def mlp_dataset(self) -> int:
+        n = C.c_int()
+        self._check(self.lib.fv3d_mlp_dataset(self.h, C.byref(n)))
+        return n.value
+
+    def mlp_train(self, epochs=5, batch=4096, lr=1e-3, seed=7):
+        st = MlpTrainStats()
+        self._check(self.lib.fv3d_mlp_train(self.h, C.byref(MlpTrainOpts(epochs, batch, lr, seed)),
+                                            C.byref(st)))
+        return {f: getattr(st, f) for f, _ in MlpTrainStats._fields_}
 
     def stream(self) -> int:
         s = C.c_void_p()

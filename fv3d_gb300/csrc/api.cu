@@ -323,6 +323,8 @@ extern "C" fv3d_status fv3d_destroy(fv3d_ctx* handle) {
   ctx->release_graphs();
   delete ctx->implicit;
   ctx->implicit = nullptr;
+  delete ctx->mlp;
+  ctx->mlp = nullptr;
   ctx->free_device();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);

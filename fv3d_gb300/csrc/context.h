@@ -13,6 +13,7 @@
 namespace fv3d {
 
 struct Implicit;
+struct Mlp;
 
 // owning device allocation
 template <class T>
@@ -73,6 +74,7 @@ struct Ctx {
 
   std::map<std::pair<int, double>, cudaGraphExec_t> graphs;
   Implicit* implicit = nullptr;  // Newton-Krylov work space, created on first use
+  Mlp* mlp = nullptr;            // learned preconditioner, created on first use
 
   bool fp64() const { return cfg.precision == FV3D_PRECISION_FP64; }
   size_t rsize() const { return fp64() ? sizeof(double) : sizeof(float); }

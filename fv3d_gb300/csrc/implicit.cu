@@ -430,6 +430,7 @@ fv3d_status Implicit::norm(Ctx& ctx, const double* v, double* out) {
 }
 
 fv3d_status Implicit::precondition(Ctx& ctx, const double* v, double* z) {
+  if (opts.preconditioner == FV3D_PC_LEARNED && !use_block_jacobi) return ctx.mlp->apply(ctx, v, z);
   if (opts.preconditioner == FV3D_PC_NONE) {
     ICK(cudaMemcpyAsync(z, v, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx.stream));
     return FV3D_OK;
@@ -488,6 +489,8 @@ fv3d_status Implicit::build_blocks(Ctx& ctx) {
   ICK(cudaGetLastError());
   k_block_invert<<<blocks(ctx.nc, 128), 128, 0, ctx.stream>>>(ctx.nc, D.p, Dinv.p);
   ICK(cudaGetLastError());
+  if (ctx.mlp && ctx.mlp->ready && (opts.preconditioner == FV3D_PC_LEARNED || ctx.mlp->harvest_per_step > 0))
+    return ctx.mlp->build_features(ctx, *this);
   return FV3D_OK;
 }
 
@@ -506,10 +509,10 @@ fv3d_status Implicit::fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res
       // true residual of the current iterate: R - A x
       fv3d_status st = apply_A(ctx, x.p, w.p);
       if (st != FV3D_OK) return st;
-      k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0, R.p, -1.0, w.p, w.p);
-      if ((st = norm(ctx, w.p, &beta)) != FV3D_OK) return st;
+      k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0, R.p, -1.0, w.p, Rp.p);
+      if ((st = norm(ctx, Rp.p, &beta)) != FV3D_OK) return st;
       if (!(beta > opts.eta * rnorm)) { res = beta; break; }
-      k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0 / beta, w.p, 0.0, nullptr, V.p);
+      k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0 / beta, Rp.p, 0.0, nullptr, V.p);
     }
     ICK(cudaGetLastError());
     std::fill(H.begin(), H.end(), 0.0);
@@ -577,6 +580,8 @@ fv3d_status Implicit::fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res
 fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit_stats* stats) {
   opts = o;
   if (opts.krylov_dim < 1 || opts.krylov_dim > 31) return ctx.fail(FV3D_ERR_INVALID_ARG, "krylov_dim must be 1..31");
+  if (opts.preconditioner == FV3D_PC_LEARNED && !(ctx.mlp && ctx.mlp->ready))
+    return ctx.fail(FV3D_ERR_STATE, "learned preconditioner requested but no MLP initialised");
   fv3d_status st = ensure_fp64_path(ctx);
   if (st == FV3D_OK && opts.jv_precision == 1) st = ensure_mixed_path(ctx);
   if (st == FV3D_OK) st = setup(ctx, opts.krylov_dim);
@@ -584,8 +589,8 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
   history.clear();
   jv_count = 0;
   const auto t0 = std::chrono::steady_clock::now();
-  double res0 = 0.0, res = 0.0, res_prev = 0.0, cfl = opts.cfl_start;
-  int newton = 0, gmres_total = 0, rejected = 0;
+  double res0 = 0.0, res = 0.0, cfl = opts.cfl_start;
+  int newton = 0, gmres_total = 0, rejected = 0, fallbacks = 0;
   bool converged = false;
   for (newton = 0; newton <= opts.max_newton; ++newton) {
     if ((st = residual64(ctx, ctx.d_U.p, R.p)) != FV3D_OK) return st;
@@ -610,8 +615,19 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
       if (st != FV3D_OK) return st;
       int it = 0;
       double rr = 0.0;
+      use_block_jacobi = false;
       if ((st = fgmres(ctx, res, &it, &rr)) != FV3D_OK) return st;
       gmres_total += it;
+      if (opts.preconditioner == FV3D_PC_LEARNED && !(rr <= 0.5)) {
+        // stagnation with the learned preconditioner: redo with block Jacobi
+        use_block_jacobi = true;
+        fallbacks += 1;
+        if ((st = fgmres(ctx, res, &it, &rr)) != FV3D_OK) return st;
+        gmres_total += it;
+      }
+      if (ctx.mlp && ctx.mlp->ready && ctx.mlp->harvest_per_step > 0 && attempt == 0) {
+        if ((st = ctx.mlp->harvest(ctx, *this)) != FV3D_OK) return st;
+      }
       // trial state
       k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0, ctx.d_U.p, 1.0, x.p, Wst.p);
       ICK(cudaMemsetAsync(bits.p, 0xff, sizeof(unsigned long long), ctx.stream));
@@ -628,9 +644,7 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
       cfl = std::max(1.0, cfl * 0.1);
       if (attempt == 5) return ctx.fail(FV3D_ERR_NOT_CONVERGED, "Newton update not admissible at step %d", newton);
     }
-    res_prev = res;
   }
-  (void)res_prev;
   ICK(cudaStreamSynchronize(ctx.stream));
   const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (stats != nullptr) {
@@ -638,7 +652,7 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
     stats->gmres_iterations = gmres_total;
     stats->jv_evaluations = jv_count;
     stats->rejected_steps = rejected;
-    stats->fallbacks = 0;
+    stats->fallbacks = fallbacks;
     stats->res0 = res0;
     stats->res_final = res;
     stats->rel_res = (res0 > 0.0) ? res / res0 : 0.0;

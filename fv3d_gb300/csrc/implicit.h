@@ -7,6 +7,29 @@
 
 namespace fv3d {
 
+struct Implicit;
+
+// learned preconditioner state (mlp.cu)
+struct Mlp {
+  bool ready = false;
+  DevBuf<float> P, m, v, grad;      // FP32 master parameters, Adam moments, gradient
+  DevBuf<float> part, loss_part;    // per-CTA partial gradients / losses
+  DevBuf<int> bidx;
+  DevBuf<float> feat;               // [nc][32] per-cell feature record
+  DevBuf<float> X, T;               // harvested training pairs
+  int n_samples = 0, max_samples = 0, harvest_per_step = 0, harvest_calls = 0;
+  int adam_t = 0;
+
+  fv3d_status init(Ctx& ctx, unsigned long long seed);
+  fv3d_status ensure_scratch(Ctx& ctx, int nbatch);
+  fv3d_status forward_host(Ctx& ctx, const float* X, int n, float* Y);
+  fv3d_status grad_host(Ctx& ctx, const float* X, const float* T, int n, double* loss, float* g);
+  fv3d_status train(Ctx& ctx, const fv3d_mlp_train_opts& o, fv3d_mlp_train_stats* stats);
+  fv3d_status build_features(Ctx& ctx, const Implicit& im);
+  fv3d_status apply(Ctx& ctx, const double* v, double* z);
+  fv3d_status harvest(Ctx& ctx, const Implicit& im);
+};
+
 struct Implicit {
   fv3d_implicit_opts opts;
   size_t n = 0;   // 5 * cells
@@ -17,6 +40,7 @@ struct Implicit {
   std::vector<double> history;  // ||R||_2 per Newton step
   int jv_count = 0;
   double unorm = 0.0;
+  bool use_block_jacobi = false;  // learned preconditioner fell back this step
 
   fv3d_status setup(Ctx& ctx, int m);
   fv3d_status solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit_stats* stats);

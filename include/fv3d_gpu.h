@@ -202,6 +202,41 @@ fv3d_status fv3d_implicit_history(const fv3d_ctx *ctx, double *res, int max, int
  * reference cell order (lumped blocks: compare with calc_jacobian_numerical) */
 fv3d_status fv3d_get_blocks(fv3d_ctx *ctx, double *blocks);
 
+/* ---- learned preconditioner (per-cell MLP 36-64-64-64-5, GELU) -------------------- */
+/* BF16 weights / FP32 accumulation on tensor cores, trained on (residual,
+ * Newton-correction) pairs that the plain implicit solver harvests; used only
+ * inside FGMRES (preconditioner FV3D_PC_LEARNED) with a block-Jacobi redo
+ * whenever a linear solve stagnates.  No reference counterpart. */
+typedef struct fv3d_mlp_train_opts {
+    int epochs;
+    int batch;                 /* samples per Adam step (multiple of 64) */
+    double lr;
+    unsigned long long seed;   /* shuffling */
+} fv3d_mlp_train_opts;
+typedef struct fv3d_mlp_train_stats {
+    double loss_first, loss_last;
+    int samples;
+    int steps;
+    double wall_ms;
+} fv3d_mlp_train_stats;
+int fv3d_mlp_num_params(void);
+fv3d_status fv3d_mlp_init(fv3d_ctx *ctx, unsigned long long seed);
+/* packed FP32 parameters: W0[64][36] b0[64] W1[64][64] b1 W2[64][64] b2 W3[5][64] b3[5] */
+fv3d_status fv3d_mlp_get_params(fv3d_ctx *ctx, float *params);
+fv3d_status fv3d_mlp_set_params(fv3d_ctx *ctx, const float *params);
+/* forward of n samples X[n][36] -> Y[n][5] (host buffers) */
+fv3d_status fv3d_mlp_forward(fv3d_ctx *ctx, const float *X, int n, float *Y);
+/* loss = mean_n sum_j (y - t)^2 and its parameter gradient (host buffers) */
+fv3d_status fv3d_mlp_grad(fv3d_ctx *ctx, const float *X, const float *T, int n, double *loss,
+                          float *grad);
+/* harvest per_step sampled cells per Newton step in later implicit solves,
+ * up to max_samples pairs kept on the device (0 disables) */
+fv3d_status fv3d_mlp_harvest(fv3d_ctx *ctx, int per_step, int max_samples);
+fv3d_status fv3d_mlp_dataset(const fv3d_ctx *ctx, int *n_samples);
+/* Adam training on the harvested pairs (forward/backward/Adam kernels) */
+fv3d_status fv3d_mlp_train(fv3d_ctx *ctx, const fv3d_mlp_train_opts *opts,
+                           fv3d_mlp_train_stats *stats);
+
 /* ---- measurement helpers ------------------------------------------------------ */
 /* average device time (ms) per launch of each explicit-stage kernel over
  * n_reps stages, each bracketed by CUDA events on the context stream:

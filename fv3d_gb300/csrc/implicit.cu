@@ -551,6 +551,9 @@ fv3d_status Implicit::fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res
       }
       const double a = H[(size_t)k * (m + 1) + k], b = H[(size_t)k * (m + 1) + k + 1];
       const double r = sqrt(a * a + b * b);
+      // a preconditioned direction with no component (a zero or non-finite
+      // preconditioner output): stop without it, leaving the residual unreduced
+      if (!(r > 0.0) || !std::isfinite(r)) { res = fabs(g[k]); done = true; break; }
       cs[k] = (r > 0.0) ? a / r : 1.0;
       sn[k] = (r > 0.0) ? b / r : 0.0;
       H[(size_t)k * (m + 1) + k] = r;

@@ -16,7 +16,7 @@ struct Mlp {
   DevBuf<float> part, loss_part;    // per-CTA partial gradients / losses
   DevBuf<int> bidx;
   DevBuf<float> feat;               // [nc][32] per-cell feature record
-  DevBuf<float> X, T;               // harvested training pairs
+  DevBuf<float> X, T, Wt;           // harvested training pairs and their loss weights
   int n_samples = 0, max_samples = 0, harvest_per_step = 0, harvest_calls = 0;
   int adam_t = 0;
 

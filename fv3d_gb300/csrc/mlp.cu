@@ -167,9 +167,9 @@ __device__ void mlp_forward_warp(const MlpW& w, MlpAct& s, int r0, bool keep) {
 // per-CTA partial gradients (deterministic reduction afterwards)
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(128) k_mlp_train(const float* __restrict__ P, const float* __restrict__ X,
-                                                   const float* __restrict__ T, const int* __restrict__ idx,
-                                                   int nbatch, float inv_b, float* __restrict__ part,
-                                                   float* __restrict__ loss_part) {
+                                                   const float* __restrict__ T, const float* __restrict__ Wt,
+                                                   const int* __restrict__ idx, int nbatch, float inv_b,
+                                                   float* __restrict__ part, float* __restrict__ loss_part) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MlpTrainSmem& S = *reinterpret_cast<MlpTrainSmem*>(smem_raw);
   const int base = blockIdx.x * MLP_TILE;
@@ -183,16 +183,18 @@ __global__ void __launch_bounds__(128) k_mlp_train(const float* __restrict__ P, 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r0 = warp * 16;
   mlp_forward_warp(S.w, S.act, r0, true);
-  // output delta dL/dy = 2 (y - t) / B  (mean over samples of sum over outputs)
+  // output delta dL/dy = 2 w (y - t) / B  (weighted mean over samples of the
+  // sum over outputs; w = 1 without a weight array)
   float lsum = 0.f;
   for (int i = lane; i < 16 * LD_O; i += 32) {
     const int r = r0 + i / LD_O, o = i % LD_O;
     const int sidx = (base + r < nbatch) ? idx[base + r] : -1;
     float d = 0.f;
     if (sidx >= 0 && o < MLP_OUT) {
+      const float w = Wt ? Wt[sidx] : 1.f;
       const float e = S.act.y[r * 8 + o] - T[(size_t)sidx * MLP_OUT + o];
-      lsum += e * e;
-      d = 2.f * e * inv_b;
+      lsum += w * e * e;
+      d = 2.f * w * e * inv_b;
     }
     if (o < 8) S.act.y[r * 8 + o] = d;  // keep the FP32 delta for db3
     S.dy[r * LD_O + o] = __float2bfloat16(d);
@@ -378,9 +380,12 @@ __global__ void k_mlp_features(int nc, int mcf, const int* __restrict__ cface, c
 }
 
 // training pairs from a Newton step: cells c_j = (j0 + j * stride) mod nc
+// with raw weights (|r_c| / ||D_c||_F)^2: the squared size of the cell's
+// block-Jacobi output, so that a cell whose local residual is tiny next to its
+// Newton correction (a correction carried in from elsewhere) does not dominate
 __global__ void k_mlp_harvest(int nc, int count, long long j0, long long stride, const float* __restrict__ feat,
                               const double* __restrict__ r, const double* __restrict__ x,
-                              float* __restrict__ X, float* __restrict__ T) {
+                              float* __restrict__ X, float* __restrict__ T, float* __restrict__ Wt) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= count) return;
   const int c = (int)((j0 + (long long)j * stride) % nc);
@@ -396,6 +401,25 @@ __global__ void k_mlp_harvest(int nc, int count, long long j0, long long stride,
     Xo[31 + k] = (rn > 0.0) ? (float)(r[(size_t)k * nc + c] / rn) : 0.f;
     To[k] = (float)(x[(size_t)k * nc + c] * scale);
   }
+  const double b = rn * (double)f[31];
+  Wt[j] = (float)(b * b);
+}
+
+// one Newton step's weights divided by their mean (steps of very different
+// residual size weigh alike); one CTA, fixed-order reduction
+__global__ void __launch_bounds__(256) k_mlp_weight_norm(int count, float* __restrict__ Wt) {
+  __shared__ double red[256];
+  double s = 0.0;
+  for (int j = threadIdx.x; j < count; j += 256) s += Wt[j];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 128; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  const double mean = red[0] / count;
+  const float inv = (mean > 0.0) ? (float)(1.0 / mean) : 0.f;
+  for (int j = threadIdx.x; j < count; j += 256) Wt[j] *= inv;
 }
 
 size_t train_smem() { return sizeof(MlpTrainSmem); }
@@ -470,7 +494,8 @@ fv3d_status Mlp::grad_host(Ctx& ctx, const float* X, const float* T, int n, doub
   std::iota(id.begin(), id.end(), 0);
   MCK(cudaMemcpy(bidx.p, id.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
   const int nparts = (n + MLP_TILE - 1) / MLP_TILE;
-  k_mlp_train<<<nparts, 128, train_smem(), ctx.stream>>>(P.p, dX.p, dT.p, bidx.p, n, 1.f / n, part.p, loss_part.p);
+  k_mlp_train<<<nparts, 128, train_smem(), ctx.stream>>>(P.p, dX.p, dT.p, nullptr, bidx.p, n, 1.f / n, part.p,
+                                                         loss_part.p);
   k_mlp_reduce<<<(MLP_NPARAM + 255) / 256, 256, 0, ctx.stream>>>(nparts, part.p, grad.p);
   MCK(cudaGetLastError());
   MCK(cudaStreamSynchronize(ctx.stream));
@@ -504,8 +529,8 @@ fv3d_status Mlp::train(Ctx& ctx, const fv3d_mlp_train_opts& o, fv3d_mlp_train_st
     int ebat = 0;
     std::vector<float> lp(nparts);
     for (int b0 = 0; b0 + B <= n_samples; b0 += B) {
-      k_mlp_train<<<nparts, 128, train_smem(), ctx.stream>>>(P.p, X.p, T.p, perm.p + b0, B, 1.f / B, part.p,
-                                                             loss_part.p);
+      k_mlp_train<<<nparts, 128, train_smem(), ctx.stream>>>(P.p, X.p, T.p, Wt.p, perm.p + b0, B, 1.f / B,
+                                                             part.p, loss_part.p);
       k_mlp_reduce<<<(MLP_NPARAM + 255) / 256, 256, 0, ctx.stream>>>(nparts, part.p, grad.p);
       adam_t += 1;
       const float c1 = 1.f - powf(b1, (float)adam_t), c2 = 1.f - powf(b2, (float)adam_t);
@@ -558,13 +583,16 @@ fv3d_status Mlp::harvest(Ctx& ctx, const Implicit& im) {
   if (X.n < (size_t)max_samples * MLP_IN) {
     MCK(X.alloc((size_t)max_samples * MLP_IN));
     MCK(T.alloc((size_t)max_samples * MLP_OUT));
+    MCK(Wt.alloc((size_t)max_samples));
   }
   // a deterministic spread of cells: stride coprime-ish with nc, offset per step
   const long long stride = 2654435761LL % ctx.nc + 1;
   const long long j0 = (long long)harvest_calls * 7919LL;
   k_mlp_harvest<<<(count + 255) / 256, 256, 0, ctx.stream>>>(ctx.nc, count, j0, stride, feat.p, im.R.p, im.x.p,
                                                              X.p + (size_t)n_samples * MLP_IN,
-                                                             T.p + (size_t)n_samples * MLP_OUT);
+                                                             T.p + (size_t)n_samples * MLP_OUT,
+                                                             Wt.p + n_samples);
+  k_mlp_weight_norm<<<1, 256, 0, ctx.stream>>>(count, Wt.p + n_samples);
   MCK(cudaGetLastError());
   n_samples += count;
   harvest_calls += 1;
@@ -633,6 +661,7 @@ extern "C" fv3d_status fv3d_mlp_harvest(fv3d_ctx* handle, int per_step, int max_
     m->n_samples = 0;
     m->X.release();
     m->T.release();
+    m->Wt.release();
   }
   return FV3D_OK;
 }

@@ -106,6 +106,7 @@ EXPORTS = {
     "fv3d_step_explicit": ([C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double,
                             C.POINTER(StepStats)], C.c_int),
     "fv3d_global_residual": ([C.c_void_p, C.c_double, _f8p], C.c_int),
+    "fv3d_global_residual_noalloc": ([C.c_void_p, C.c_double, _f8p], C.c_int),
     "fv3d_profile_stage": ([C.c_void_p, C.c_int, C.c_double, _f8p], C.c_int),
     "fv3d_get_stream": ([C.c_void_p, C.POINTER(C.c_void_p)], C.c_int),
     "fv3d_device_state": ([C.c_void_p, C.POINTER(_f8p)], C.c_int),

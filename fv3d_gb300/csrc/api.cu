@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <numeric>
 #include <string>
 #include <vector>
@@ -621,6 +622,60 @@ extern "C" fv3d_status fv3d_global_residual(fv3d_ctx* handle, double dt, double 
   k_residual_final<<<1, 256, 0, ctx->stream>>>(nb, ctx->d_part.p, dt / ctx->vol_total, ctx->d_part.p + 5 * (size_t)nb);
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(res, ctx->d_part.p + 5 * (size_t)nb, 5 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return FV3D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// calc_global_residual without any device allocation: the block partial sums
+// and the five results live in one file-scope static device array of fixed
+// size instead of the context's scratch.  Same kernels and grid as
+// fv3d_global_residual, so the results are bitwise identical.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kNoAllocMaxBlocks = FV3D_NOALLOC_MAX_CELLS / 256;
+constexpr int kNoAllocMaxDevices = 64;
+// [kNoAllocMaxBlocks][5] block partials, then the 5 results (320 KiB).  Every
+// slot a call reads is written earlier in that call, so nothing in it has to
+// start at zero.  One array per device: calls that overlap on one device
+// (other threads, other contexts' streams) race on it.
+static __device__ __align__(256) double g_noalloc_part[5 * kNoAllocMaxBlocks + 5];
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {};  // resolved by the first call on each device
+}  // namespace
+
+extern "C" fv3d_status fv3d_global_residual_noalloc(fv3d_ctx* handle, double dt, double res[5]) {
+  if (handle == nullptr || res == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (!ctx->residual_valid) return ctx->fail(FV3D_ERR_STATE, "no residual evaluated (call fv3d_time_derivative)");
+  if (ctx->nc > FV3D_NOALLOC_MAX_CELLS)
+    return ctx->fail(FV3D_ERR_UNSUPPORTED,
+                     "fv3d_global_residual_noalloc: %d cells exceed its static scratch (at most %d cells); "
+                     "use fv3d_global_residual",
+                     ctx->nc, FV3D_NOALLOC_MAX_CELLS);
+  const int dev = ctx->cfg.device;
+  if (dev < 0 || dev >= kNoAllocMaxDevices)
+    return ctx->fail(FV3D_ERR_UNSUPPORTED, "fv3d_global_residual_noalloc: device %d beyond %d", dev,
+                     kNoAllocMaxDevices - 1);
+  CK(cudaSetDevice(dev));
+  double* part = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_ptr[dev] == nullptr) {
+      void* p = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_part);
+      if (e != cudaSuccess || p == nullptr)
+        return ctx->fail(FV3D_ERR_DEVICE, "cudaGetSymbolAddress of the static residual scratch: %s",
+                         cudaGetErrorString(e));
+      g_noalloc_ptr[dev] = static_cast<double*>(p);
+    }
+    part = g_noalloc_ptr[dev];
+  }
+  const int nb = nblk(ctx->nc);
+  k_residual_partial<<<nb, 256, 0, ctx->stream>>>(ctx->nc, ctx->d_dphi.p, ctx->d_vol.p, part);
+  k_residual_final<<<1, 256, 0, ctx->stream>>>(nb, part, dt / ctx->vol_total, part + 5 * (size_t)nb);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(res, part + 5 * (size_t)nb, 5 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return FV3D_OK;
 }

@@ -156,6 +156,19 @@ fv3d_status fv3d_step_explicit(fv3d_ctx *ctx, int scheme, int n_steps, double cf
                                double dt_fixed, fv3d_step_stats *stats);
 /* calc_global_residual (analyze.c:37-61) of the last residual evaluation */
 fv3d_status fv3d_global_residual(fv3d_ctx *ctx, double dt, double res[5]);
+/* No counterpart in the reference.  fv3d_global_residual for callers that
+ * must not allocate device memory when they call (code running under a fixed
+ * device-memory budget or in a section where allocation calls are not
+ * allowed): the reduction scratch is one static device array of fixed size
+ * (320 KiB per device), so meshes of at most FV3D_NOALLOC_MAX_CELLS cells;
+ * larger meshes get FV3D_ERR_UNSUPPORTED.  Results are bitwise those of
+ * fv3d_global_residual.  The first call on a device looks up the array's
+ * address (cudaGetSymbolAddress); make that first call before any stream
+ * capture begins.  Nothing in the array needs to start at zero.  Calls that
+ * overlap on one device (other threads, other contexts) race on the one
+ * array: serialise them. */
+#define FV3D_NOALLOC_MAX_CELLS 2097152
+fv3d_status fv3d_global_residual_noalloc(fv3d_ctx *ctx, double dt, double res[5]);
 
 /* ---- implicit steady solve ---------------------------------------------------- */
 /* Pseudo-transient Newton-Krylov replacing timestep_newton / calc_jacobian_

@@ -42,14 +42,14 @@ STAGES = {"euler": 1, "rk33": 3, "rk45": 5, "ssprk3": 3}
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--steps", type=int, default=1000)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--case", default="tgv_tet", choices=["tgv_tet", "tgv_hex", "euler16"])
     p.add_argument("--n", type=int, default=64)
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--e2e-steps", type=int, default=20)
-    p.add_argument("--cpu-sample-stages", type=int, default=3)
+    p.add_argument("--cpu-sample-stages", type=int, default=15)
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 

@@ -95,6 +95,49 @@ __device__ __forceinline__ void mx_unpack(const float4 x, const float4 y, float*
   q[VU] = x.y * ir; q[VV] = x.z * ir; q[VW] = x.w * ir;
 }
 
+// 32-byte records in one request: ld / st .v8.f32 (256-bit global
+// accesses, sm_100 and later).  Every record passed here starts at a
+// multiple of 32 bytes from a cudaMalloc base, as these require.
+#ifndef FV3D_V8
+#define FV3D_V8 1
+#endif
+__device__ __forceinline__ void ld_rec_nc(const float* p, float4& x, float4& y) {
+#if FV3D_V8
+  asm volatile("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(x.x), "=f"(x.y), "=f"(x.z), "=f"(x.w), "=f"(y.x), "=f"(y.y), "=f"(y.z), "=f"(y.w)
+               : "l"(p));
+#else
+  x = __ldg(reinterpret_cast<const float4*>(p));
+  y = __ldg(reinterpret_cast<const float4*>(p) + 1);
+#endif
+}
+// for a record this thread overwrites later in the same launch
+__device__ __forceinline__ void ld_rec(const float* p, float4& x, float4& y) {
+#if FV3D_V8
+  asm volatile("ld.global.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(x.x), "=f"(x.y), "=f"(x.z), "=f"(x.w), "=f"(y.x), "=f"(y.y), "=f"(y.z), "=f"(y.w)
+               : "l"(p) : "memory");
+#else
+  x = reinterpret_cast<const float4*>(p)[0];
+  y = reinterpret_cast<const float4*>(p)[1];
+#endif
+}
+__device__ __forceinline__ void st_rec(float* p, const float4 x, const float4 y) {
+#if FV3D_V8
+  asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(x.x), "f"(x.y), "f"(x.z),
+               "f"(x.w), "f"(y.x), "f"(y.y), "f"(y.z), "f"(y.w)
+               : "memory");
+#else
+  reinterpret_cast<float4*>(p)[0] = x;
+  reinterpret_cast<float4*>(p)[1] = y;
+#endif
+}
+__device__ __forceinline__ void ld_unpack(const float* rec, float* q) {
+  float4 x, y;
+  ld_rec_nc(rec, x, y);
+  mx_unpack(x, y, q);
+}
+
 // eos.c:55-75 with the face-normal velocity un
 __device__ __forceinline__ float mx_wall_pressure(float rho, float p, float un, const MxPhys& ph) {
   if (un <= 0.f) {
@@ -195,9 +238,8 @@ __global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __
   if (c >= a.nc) return;
   MxPhys ph;
   ph.load(a.pc);
-  const float4* Uf4 = reinterpret_cast<const float4*>(a.Uf);
   float q[10];
-  mx_unpack(__ldg(Uf4 + 2 * (size_t)c), __ldg(Uf4 + 2 * (size_t)c + 1), q);
+  ld_unpack(a.Uf + 8 * (size_t)c, q);
   int e[MCF], o[MCF];
   load_cface<MCF>(a.cface + (size_t)c * MCF, e);
   load_cface<MCF>(a.cnbr + (size_t)c * MCF, o);  // neighbour cell, -1 ghost, -2 none
@@ -218,7 +260,7 @@ __global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __
         const float n[3] = {nA.x, nA.y, nA.z};
         mx_ghost(q, a.fregion[f - a.nf_int], n, a.pc, ph, qo);
       } else {
-        mx_unpack(__ldg(Uf4 + 2 * (size_t)o[k]), __ldg(Uf4 + 2 * (size_t)o[k] + 1), qo);
+        ld_unpack(a.Uf + 8 * (size_t)o[k], qo);
       }
       if (GMODE == 1) {
         // Green-Gauss (reconstruction.c:43-71) in difference form:
@@ -295,14 +337,10 @@ __global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __
       for (int v = 0; v < 8; ++v) r[v] = q[v];
     }
     if (VISC) mx_viscous(r, tau, g[8], nA, ph, &r[8]);
-    float4* rec = reinterpret_cast<float4*>(a.fs + (size_t)f * FREC);
-    rec[2 * side] = make_float4(r[0], r[1], r[2], r[3]);
-    if (VISC) {
-      rec[2 * side + 1] = make_float4(r[4], r[8], r[9], r[10]);
-      a.fsv[2 * (size_t)f + side] = r[11];
-    } else {
-      rec[2 * side + 1] = make_float4(r[4], 0.f, 0.f, 0.f);
-    }
+    float* rec = a.fs + (size_t)f * FREC;
+    st_rec(rec + 8 * side, make_float4(r[0], r[1], r[2], r[3]),
+           VISC ? make_float4(r[4], r[8], r[9], r[10]) : make_float4(r[4], 0.f, 0.f, 0.f));
+    if (VISC) a.fsv[2 * (size_t)f + side] = r[11];
     if (o[k] == -1) {
       // ghost side: unlimited ghost of the cell-centre state
       // (reconstruction.c:249-253), gradient = interior gradient with the
@@ -335,8 +373,7 @@ __global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __
         mx_viscous(gq, tg, gT, nA, ph, vg);
         a.fsv[2 * (size_t)f + 1] = vg[3];
       }
-      rec[2] = make_float4(gq[0], gq[1], gq[2], gq[3]);
-      rec[3] = make_float4(gq[4], vg[0], vg[1], vg[2]);
+      st_rec(rec + 8, make_float4(gq[0], gq[1], gq[2], gq[3]), make_float4(gq[4], vg[0], vg[1], vg[2]));
     }
   }
 }
@@ -388,13 +425,13 @@ __device__ __forceinline__ void mx_conv_flux(const float* l, const float* r, con
 }
 
 // FP32 stage state record from conserved floats
-__device__ __forceinline__ void mx_store_state(float4* dst, float rho, float mx, float my, float mz,
-                                               float E, const MxPhys& ph) {
+__device__ __forceinline__ void mx_make_state(float rho, float mx, float my, float mz, float E,
+                                              const MxPhys& ph, float4& x, float4& y) {
   const float ir = 1.f / rho;
   const float ke = 0.5f * (mx * mx + my * my + mz * mz) * ir;
   const float p = fmaxf(1.00E-10f, ph.km1 * (E - ke));
-  dst[0] = make_float4(rho, mx, my, mz);
-  dst[1] = make_float4(E, p, p * ir / ph.R, 0.f);
+  x = make_float4(rho, mx, my, mz);
+  y = make_float4(E, p, p * ir / ph.R, 0.f);
 }
 
 // MODE 0: residual only; 1: low-storage RK stage; 2: SSP-RK3 stage.
@@ -415,8 +452,9 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
     for (int k = 0; k < MCF; ++k) {
       if (e[k] < 0) continue;
       const int f = e[k] >> 1, side = e[k] & 1;
-      const float4* src = reinterpret_cast<const float4*>(a.fs + (size_t)f * FREC);
-      const float4 l0 = __ldg(src + 0), l1 = __ldg(src + 1), r0 = __ldg(src + 2), r1 = __ldg(src + 3);
+      float4 l0, l1, r0, r1;
+      ld_rec_nc(a.fs + (size_t)f * FREC, l0, l1);
+      ld_rec_nc(a.fs + (size_t)f * FREC + 8, r0, r1);
       const float l[5] = {l0.x, l0.y, l0.z, l0.w, l1.x};
       const float r[5] = {r0.x, r0.y, r0.z, r0.w, r1.x};
       const float4 nA = __ldg(&a.slotN[(size_t)c * MCF + k]);
@@ -462,9 +500,9 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
           du[j] = co.first ? fdt * rr[j] : c1 * fmaf(fdt, rr[j], a.dU[i]);
         }
       }
-      float4* sh = reinterpret_cast<float4*>(a.Uf) + 2 * (size_t)c;
+      float* sh = a.Uf + 8 * (size_t)c;
       float4 o0 = make_float4(0.f, 0.f, 0.f, 0.f), o1 = o0;
-      if (DT && MODE == 1) { o0 = sh[0]; o1 = sh[1]; }  // stage-input state
+      if (DT && MODE == 1) ld_rec(sh, o0, o1);  // stage-input state
       float un[5];
       if (co.last) {
         // end of step: U_{n+1} = U_n + dU in FP64, new base record
@@ -476,13 +514,13 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
           un[j] = (float)uj;
           finite = finite && isfinite(uj);
         }
-        float4* base = reinterpret_cast<float4*>(a.UfN) + 2 * (size_t)c;
-        mx_store_state(base, un[0], un[1], un[2], un[3], un[4], ph);
-        sh[0] = base[0];
-        sh[1] = base[1];
+        float4 x, y;
+        mx_make_state(un[0], un[1], un[2], un[3], un[4], ph, x, y);
+        st_rec(a.UfN + 8 * (size_t)c, x, y);
+        st_rec(sh, x, y);
       } else {
-        const float4* base = reinterpret_cast<const float4*>(a.UfN) + 2 * (size_t)c;
-        const float4 b0 = base[0], b1 = base[1];
+        float4 b0, b1;
+        ld_rec_nc(a.UfN + 8 * (size_t)c, b0, b1);
         un[0] = b0.x + du[0]; un[1] = b0.y + du[1]; un[2] = b0.z + du[2]; un[3] = b0.w + du[3];
         un[4] = b1.x + du[4];
 #pragma unroll
@@ -490,7 +528,9 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
           a.dU[(size_t)j * a.nc + c] = du[j];
           finite = finite && isfinite(du[j]);
         }
-        mx_store_state(sh, un[0], un[1], un[2], un[3], un[4], ph);
+        float4 x, y;
+        mx_make_state(un[0], un[1], un[2], un[3], un[4], ph, x, y);
+        st_rec(sh, x, y);
       }
       if (DT) {
         // calc_ns_timestep on the reference's phi_total: new density, the

@@ -10,9 +10,9 @@ value  = cells * stages * steps / device time  (state resident in HBM)
 e2e    = the same metric through the public C ABI with host buffers: every
          step uploads the conserved state from pinned host memory, runs one
          step and reads the state back
-roofline: the dominant kernel's algorithmic bytes (fixed byte model, see
-         the design doc) / its average CUDA-event duration, against the measured
-         HBM copy bandwidth
+roofline: the dominant kernel's algorithmic bytes (the fixed byte model in
+         byte_model below) / its average CUDA-event duration, against the
+         measured HBM copy bandwidth
 cpu_baseline: the FP64 CPU oracle on the host cores, bounded sample
 
 --impl reference times the CPU implementation of the path (the reference's
@@ -45,7 +45,9 @@ def parse():
     p.add_argument("--steps", type=int, default=1000)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--case", default="tgv_tet", choices=["tgv_tet", "tgv_hex", "euler16"])
+    p.add_argument("--case", default="tgv_tet", choices=["tgv_tet", "tgv_hex", "euler16", "channel"])
+    p.add_argument("--learned", action="store_true",
+                   help="channel: also harvest, train and evaluate the learned preconditioner")
     p.add_argument("--n", type=int, default=64)
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--e2e-steps", type=int, default=20)
@@ -211,8 +213,52 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_channel(args):
+    """Implicit steady channel (96 x 48 x 48 stretched hexes, AUSM, second
+    order): wall time of the pseudo-transient Newton-Krylov solve to a 1e-8
+    relative FP64 residual, with FGMRES(30) unpreconditioned (the fastest
+    here), with block Jacobi, and optionally with the learned preconditioner
+    trained on pairs harvested from the block-Jacobi solve."""
+    from fv3d_gb300 import api, cases
+    c = cases.channel()
+    keys = ("converged", "newton_steps", "gmres_iterations", "jv_evaluations", "rel_res", "wall_ms",
+            "fallbacks")
+    runs = {}
+    with api.Solver(c.mesh, c.params, c.region_type, c.region_prim, "fp64", "morton") as s:
+        if args.learned:
+            s.mlp_init(5)
+        plans = [("none", dict(max_restarts=3)), ("block_jacobi", {})]
+        for pc, kw in plans:
+            if args.learned and pc == "block_jacobi":
+                s.mlp_harvest(1024, 400000)
+            s.set_state(c.u0)
+            st = s.solve_implicit(preconditioner=pc, max_newton=400, check=False, **kw)
+            runs[pc] = {k: st[k] for k in keys}
+            if args.learned:
+                s.mlp_harvest(0, 400000)
+        if args.learned:
+            tr = s.mlp_train(epochs=30, batch=1024, lr=2e-3)
+            s.set_state(c.u0)
+            st = s.solve_implicit(preconditioner="learned", max_newton=400, check=False)
+            runs["learned"] = {k: st[k] for k in keys}
+            runs["learned"]["train"] = tr
+    best = runs["none"]
+    line = {"metric": "seconds to 1e-8 relative steady residual", "value": round(best["wall_ms"] / 1e3, 3),
+            "unit": "s", "n_gpus": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 (Jv f32)", "data": "synthetic",
+            "config": {"workload": f"channel 96x48x48: {c.mesh.n_cells} cells, {c.mesh.n_faces} faces, AUSM, "
+                                   "Green-Gauss linear, no limiter, Re=1000, pseudo-transient Newton, "
+                                   "SER CFL 100 -> 1e4, FGMRES(30), FD Jv in FP32",
+                       "preconditioner": "none (3 restarts)"},
+            "runs": runs}
+    print(json.dumps(line))
+
+
 def main():
     args = parse()
+    if args.case == "channel":
+        run_channel(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return

@@ -65,6 +65,8 @@ struct MxArgs {
   const float4* __restrict__ slotN;  // [nc][mcf] face (n, A), cell 0 -> cell 1 orientation
   const float4* __restrict__ slotD;  // [nc][mcf] (d of this side, Green-Gauss weight)
   const float4* __restrict__ slotW;  // [nc][mcf] least-squares weights of this side
+  const float4* __restrict__ slotNk; // [mcf][nc] slotN again, slot-major for the flux pass: a
+                                     // warp's load of slot k is 512 contiguous bytes
   const int* __restrict__ fregion;   // [nf - nf_int]
   const float4* __restrict__ cgeo;   // [nc] (sum_f s_f n_f A_f, 1/V)
   const float4* __restrict__ cdx;    // [nc] (dx, V)
@@ -457,7 +459,7 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
       ld_rec_nc(a.fs + (size_t)f * FREC + 8, r0, r1);
       const float l[5] = {l0.x, l0.y, l0.z, l0.w, l1.x};
       const float r[5] = {r0.x, r0.y, r0.z, r0.w, r1.x};
-      const float4 nA = __ldg(&a.slotN[(size_t)c * MCF + k]);
+      const float4 nA = __ldg(&a.slotNk[(size_t)k * a.nc + c]);
       float F[5];
       mx_conv_flux(l, r, nA, ph, F);
       if (VISC) {

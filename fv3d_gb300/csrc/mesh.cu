@@ -400,6 +400,12 @@ fv3d_status ensure_mixed_path(Ctx& ctx) {
   UP(ctx.d_fcell, fcell.data(), (size_t)nf);
   UP(ctx.d_slotN, sN.data(), sN.size());
   UP(ctx.d_slotD, sD.data(), sD.size());
+  {
+    std::vector<float4> sNk(sN.size());
+    for (int c = 0; c < nc; ++c)
+      for (int k = 0; k < mcf; ++k) sNk[(size_t)k * nc + c] = sN[(size_t)c * mcf + k];
+    UP(ctx.d_slotNk, sNk.data(), sNk.size());
+  }
   if (ctx.cfg.gradient == FV3D_GRADIENT_LEAST_SQUARES) UP(ctx.d_slotW, sW.data(), sW.size());
   ALLOC(ctx.d_Uf, (size_t)nc * 8);
   ALLOC(ctx.d_UfN, (size_t)nc * 8);

@@ -2,7 +2,7 @@
 // (hand-written, BF16 tensor-core operands via mma.sync m16n8k16, FP32
 // accumulation), feature construction from the block-Jacobi blocks, the
 // harvest of (residual, Newton correction) training pairs from the plain
-// implicit solver, and the training driver.
+// implicit solver, and the training loop.
 #include <algorithm>
 #include <chrono>
 #include <cmath>

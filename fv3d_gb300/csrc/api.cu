@@ -230,9 +230,9 @@ template KArgs<double> Ctx::args<double>() const;
 MxArgs Ctx::mx_args() const {
   MxArgs a;
   memset(&a, 0, sizeof(a));
-  a.nc = nc; a.nf = nf; a.nf_int = nf_int; a.mcf = mcf;
+  a.nc = nc; a.nf = nf; a.nf_int = nf_int; a.mcf = mcf; a.ncp = ncp;
   a.cface = d_cface.p; a.cnbr = d_cnbr.p; a.fcell = d_fcell.p; a.slotN = d_slotN.p;
-  a.slotD = d_slotD.p; a.slotW = d_slotW.p; a.slotNk = d_slotNk.p; a.fregion = d_fregion.p; a.cgeo = d_cgeo.p; a.cdx = d_cdx.p;
+  a.slotD = d_slotD.p; a.slotW = d_slotW.p; a.slotNk = d_slotNk.p; a.slotDk = d_slotDk.p; a.slotWk = d_slotWk.p; a.fregion = d_fregion.p; a.cgeo = d_cgeo.p; a.cdx = d_cdx.p;
   a.Uf = d_Uf.p; a.UfN = d_UfN.p; a.fs = d_fs.p; a.fsv = d_fsv.p;
   a.U = d_U.p; a.kf = d_kf.p; a.dU = d_dU.p; a.dphi = d_dphi.p; a.sc = d_sc.p;
   a.pc = phys;
@@ -608,6 +608,8 @@ extern "C" fv3d_status fv3d_step_explicit(fv3d_ctx* handle, int scheme, int n_st
     stats->steps = hs.step;
     stats->elapsed_ms = ms;
   }
+  if (hs.status & kStatusStageTimeout)
+    return ctx->fail(FV3D_ERR_TIMEOUT, "gradient pass: a tile's staged copies did not arrive within 0.5 s");
   if (hs.status & 1) return ctx->fail(FV3D_ERR_NONFINITE, "non-finite state or time step after %d steps", hs.step);
   return FV3D_OK;
 }

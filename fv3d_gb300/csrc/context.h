@@ -46,6 +46,7 @@ struct Ctx {
 
   // sizes (renumbered mesh): interior faces first, then boundary faces
   int nc = 0, nf = 0, nf_int = 0, nb = 0, mcf = 0, n_regions = 0;
+  int ncp = 0;  // nc rounded up to whole gradient-pass tiles (kTile cells): row count of the staged arrays
   double vol_total = 0.0;
 
   // host-side maps
@@ -67,7 +68,7 @@ struct Ctx {
   DevBuf<char> d_rec, d_FA;
   // mixed path
   DevBuf<int2> d_fcell;
-  DevBuf<float4> d_slotN, d_slotD, d_slotW, d_slotNk, d_cgeo, d_cdx;
+  DevBuf<float4> d_slotN, d_slotD, d_slotW, d_slotNk, d_slotDk, d_slotWk, d_cgeo, d_cdx;
   DevBuf<float> d_fs, d_fsv, d_UfN, d_kf, d_dU;
   DevBuf<DevScalars> d_sc;
   DevBuf<unsigned long long> d_bits;
@@ -86,7 +87,7 @@ struct Ctx {
     d_geo.release(); d_lam.release(); d_lsq.release(); d_rvol.release(); d_vol.release(); d_dx.release();
     d_U.release(); d_K.release(); d_U0.release(); d_dphi.release(); d_stage.release(); d_part.release();
     d_Uf.release(); d_rec.release(); d_FA.release(); d_sc.release(); d_bits.release();
-    d_fcell.release(); d_slotN.release(); d_slotD.release(); d_slotW.release(); d_slotNk.release(); d_fs.release();
+    d_fcell.release(); d_slotN.release(); d_slotD.release(); d_slotW.release(); d_slotNk.release(); d_slotDk.release(); d_slotWk.release(); d_fs.release();
     d_fsv.release();
     d_cgeo.release(); d_cdx.release(); d_UfN.release(); d_kf.release(); d_dU.release();
   }

@@ -43,6 +43,14 @@ namespace fv3d {
 #ifndef FV3D_SIDES_UNROLL
 #define FV3D_SIDES_UNROLL 8
 #endif
+// second-order gradient passes staged through shared memory by bulk
+// asynchronous copies (k_mx_sides_tma); 0 = k_mx_sides reading global memory
+#ifndef FV3D_SIDES_TMA
+#define FV3D_SIDES_TMA 1
+#endif
+#ifndef FV3D_TMA_MINBLOCKS
+#define FV3D_TMA_MINBLOCKS 4
+#endif
 #ifndef FV3D_FLUX_MINBLOCKS
 #define FV3D_FLUX_MINBLOCKS 1
 #endif
@@ -57,16 +65,23 @@ constexpr int kFluxUnroll = FV3D_FLUX_UNROLL;
 // fsv[2f + s].  v* = viscous normal flux times A.
 constexpr int FREC = 16;
 
+// cells per tile of the staged gradient pass (k_mx_sides_tma): one thread per
+// cell; the per-cell arrays it stages are padded to whole tiles (ncp rows)
+constexpr int kTile = 128;
+
 struct MxArgs {
   int nc, nf, nf_int, mcf;
+  int ncp;                           // nc rounded up to whole tiles
   const int* __restrict__ cface;     // [nc][mcf]
   const int* __restrict__ cnbr;      // [nc][mcf] neighbour cell, -1 ghost, -2 none
   const int2* __restrict__ fcell;    // [nf] (cell 0, cell 1 or ghost)
   const float4* __restrict__ slotN;  // [nc][mcf] face (n, A), cell 0 -> cell 1 orientation
   const float4* __restrict__ slotD;  // [nc][mcf] (d of this side, Green-Gauss weight)
   const float4* __restrict__ slotW;  // [nc][mcf] least-squares weights of this side
-  const float4* __restrict__ slotNk; // [mcf][nc] slotN again, slot-major for the flux pass: a
-                                     // warp's load of slot k is 512 contiguous bytes
+  const float4* __restrict__ slotNk; // [mcf][ncp] slotN again, slot-major (flux pass: a warp's
+                                     // load of slot k is 512 contiguous bytes; staged gradient pass)
+  const float4* __restrict__ slotDk; // [mcf][ncp] slotD, slot-major
+  const float4* __restrict__ slotWk; // [mcf][ncp] slotW, slot-major (least squares only)
   const int* __restrict__ fregion;   // [nf - nf_int]
   const float4* __restrict__ cgeo;   // [nc] (sum_f s_f n_f A_f, 1/V)
   const float4* __restrict__ cdx;    // [nc] (dx, V)
@@ -459,7 +474,7 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
       ld_rec_nc(a.fs + (size_t)f * FREC + 8, r0, r1);
       const float l[5] = {l0.x, l0.y, l0.z, l0.w, l1.x};
       const float r[5] = {r0.x, r0.y, r0.z, r0.w, r1.x};
-      const float4 nA = __ldg(&a.slotNk[(size_t)k * a.nc + c]);
+      const float4 nA = __ldg(&a.slotNk[(size_t)k * a.ncp + c]);
       float F[5];
       mx_conv_flux(l, r, nA, ph, F);
       if (VISC) {
@@ -559,6 +574,266 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
       lam_bits = warp_min_u64(lam_bits);
       if ((threadIdx.x & 31) == 0 && lam_bits != 0x7ff0000000000000ull)
         atomicMin(&a.sc->lam_bits, lam_bits);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// gradient pass staged through shared memory.  Each CTA handles one tile of
+// kTile consecutive cells (one thread per cell).  One elected thread issues
+// bulk asynchronous copies (cp.async.bulk, the TMA unit) of the tile's
+// contiguous per-cell data - state records, face slots, neighbours, cell
+// geometry and the slot-major face geometry - into shared memory, completing
+// on one mbarrier; the bytes in flight no longer occupy registers.  The
+// arithmetic is that of k_mx_sides, operation for operation, so the face
+// records are bitwise the same.  Neighbour states are gathered from global
+// memory as before.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+// global -> shared bulk copy; both addresses 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// wait for a phase with a time limit; false if it did not complete in time
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, unsigned long long limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = global_ns();
+  while (!mbar_try_wait(bar, parity))
+    if (global_ns() - t0 > limit_ns) return false;
+  return true;
+}
+
+// a cell's MCF face-slot ints from the shared-memory tile (plain shared
+// loads: the read-only global path of load_cface must not see shared addresses)
+template <int MCF>
+__device__ __forceinline__ void load_slots_shared(const int* cf, int* e) {
+  if (MCF == 4) {
+    const int4 v = *reinterpret_cast<const int4*>(cf);
+    e[0] = v.x; e[1] = v.y; e[2] = v.z; e[3] = v.w;
+  } else if (MCF % 2 == 0) {
+#pragma unroll
+    for (int k = 0; k < MCF; k += 2) {
+      const int2 v = reinterpret_cast<const int2*>(cf)[k / 2];
+      e[k] = v.x; e[k + 1] = v.y;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < MCF; ++k) e[k] = cf[k];
+  }
+}
+
+// shared-memory tile: byte offsets (all multiples of 16)
+template <int MCF, int GMODE>
+struct SidesTile {
+  static constexpr int uf = 0;                                    // float [kTile][8]
+  static constexpr int cf = uf + kTile * 32;                      // int [kTile][MCF]
+  static constexpr int cn = cf + kTile * MCF * 4;                 // int [kTile][MCF]
+  static constexpr int cg = cn + kTile * MCF * 4;                 // float4 [kTile]
+  static constexpr int sn = cg + kTile * 16;                      // float4 [MCF][kTile]
+  static constexpr int sd = sn + MCF * kTile * 16;                // float4 [MCF][kTile]
+  static constexpr int sw = sd + MCF * kTile * 16;                // float4 [MCF][kTile] (LSQ)
+  static constexpr int bytes = sw + (GMODE == 2 ? MCF * kTile * 16 : 0);
+  static constexpr int bar = bytes;                               // mbarrier (8 bytes)
+  static constexpr int total = bytes + 16;
+};
+
+// status bit set when a tile's copies did not arrive within the time limit
+constexpr int kStatusStageTimeout = 4;
+
+template <int MCF, int GMODE, bool LINEAR, bool LIMIT, bool VISC>
+__global__ void __launch_bounds__(kTile, FV3D_TMA_MINBLOCKS) k_mx_sides_tma(const __grid_constant__ MxArgs a) {
+  static_assert(GMODE != 0, "the staged gradient pass needs gradients");
+  using L = SidesTile<MCF, GMODE>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int tid = threadIdx.x;
+  const int c0 = blockIdx.x * kTile;
+  const uint32_t bar = smem_u32(smem + L::bar);
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    mbar_expect_tx(bar, L::bytes);
+    const uint32_t s0 = smem_u32(smem);
+    bulk_g2s(s0 + L::uf, a.Uf + 8 * (size_t)c0, kTile * 32, bar);
+    bulk_g2s(s0 + L::cf, a.cface + (size_t)c0 * MCF, kTile * MCF * 4, bar);
+    bulk_g2s(s0 + L::cn, a.cnbr + (size_t)c0 * MCF, kTile * MCF * 4, bar);
+    bulk_g2s(s0 + L::cg, a.cgeo + c0, kTile * 16, bar);
+#pragma unroll
+    for (int k = 0; k < MCF; ++k) {
+      bulk_g2s(s0 + L::sn + k * kTile * 16, a.slotNk + (size_t)k * a.ncp + c0, kTile * 16, bar);
+      bulk_g2s(s0 + L::sd + k * kTile * 16, a.slotDk + (size_t)k * a.ncp + c0, kTile * 16, bar);
+      if (GMODE == 2) bulk_g2s(s0 + L::sw + k * kTile * 16, a.slotWk + (size_t)k * a.ncp + c0, kTile * 16, bar);
+    }
+  }
+  if (!mbar_wait_bounded(bar, 0, 500000000ull)) {
+    // the copies did not land in 0.5 s: report, give them one more bounded
+    // wait so that none is still writing this CTA's shared memory, return
+    if (tid == 0) atomicOr(&a.sc->status, kStatusStageTimeout);
+    mbar_wait_bounded(bar, 0, 500000000ull);
+    return;
+  }
+  const int c = c0 + tid;
+  if (c >= a.nc) return;
+  MxPhys ph;
+  ph.load(a.pc);
+  const float4* sUf = reinterpret_cast<const float4*>(smem + L::uf);
+  const float4* sN = reinterpret_cast<const float4*>(smem + L::sn);
+  const float4* sD = reinterpret_cast<const float4*>(smem + L::sd);
+  const float4* sW = reinterpret_cast<const float4*>(smem + L::sw);
+  float q[10];
+  mx_unpack(sUf[2 * tid], sUf[2 * tid + 1], q);
+  int e[MCF], o[MCF];
+  load_slots_shared<MCF>(reinterpret_cast<const int*>(smem + L::cf) + tid * MCF, e);
+  load_slots_shared<MCF>(reinterpret_cast<const int*>(smem + L::cn) + tid * MCF, o);
+  float g[NG][3];
+#pragma unroll
+  for (int v = 0; v < NG; ++v) { g[v][0] = 0.f; g[v][1] = 0.f; g[v][2] = 0.f; }
+  float mn[8], mxv[8];
+#pragma unroll
+  for (int v = 0; v < 8; ++v) { mn[v] = q[v]; mxv[v] = q[v]; }
+#pragma unroll kSidesUnroll
+  for (int k = 0; k < MCF; ++k) {
+    if (o[k] == -2) continue;
+    const int f = e[k] >> 1, side = e[k] & 1;
+    const float4 nA = sN[k * kTile + tid];
+    float qo[10];
+    if (o[k] < 0) {
+      const float n[3] = {nA.x, nA.y, nA.z};
+      mx_ghost(q, a.fregion[f - a.nf_int], n, a.pc, ph, qo);
+    } else {
+      ld_unpack(a.Uf + 8 * (size_t)o[k], qo);
+    }
+    if (GMODE == 1) {
+      const float w = sD[k * kTile + tid].w * nA.w;
+      const float sw = side ? -w : w;
+      const float ax = nA.x * sw, ay = nA.y * sw, az = nA.z * sw;
+#pragma unroll
+      for (int v = 0; v < NG; ++v) {
+        const int j = (v < 8) ? v : TT;
+        const float dq = qo[j] - q[j];
+        g[v][0] += dq * ax;
+        g[v][1] += dq * ay;
+        g[v][2] += dq * az;
+      }
+    } else {
+      const float4 wl = sW[k * kTile + tid];
+#pragma unroll
+      for (int v = 0; v < NG; ++v) {
+        const int j = (v < 8) ? v : TT;
+        const float dq = qo[j] - q[j];
+        g[v][0] += wl.x * dq;
+        g[v][1] += wl.y * dq;
+        g[v][2] += wl.z * dq;
+      }
+    }
+    if (LIMIT) {
+#pragma unroll
+      for (int v = 0; v < 8; ++v) { mn[v] = fminf(mn[v], qo[v]); mxv[v] = fmaxf(mxv[v], qo[v]); }
+    }
+  }
+  if (GMODE == 1) {
+    const float4 cg = reinterpret_cast<const float4*>(smem + L::cg)[tid];
+#pragma unroll
+    for (int v = 0; v < NG; ++v) {
+      const int j = (v < 8) ? v : TT;
+      g[v][0] = (g[v][0] + q[j] * cg.x) * cg.w;
+      g[v][1] = (g[v][1] + q[j] * cg.y) * cg.w;
+      g[v][2] = (g[v][2] + q[j] * cg.z) * cg.w;
+    }
+  }
+  float tau[6];
+  if (VISC) {
+    float gm[12];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      gm[d] = g[1][d]; gm[3 + d] = g[2][d]; gm[6 + d] = g[3][d]; gm[9 + d] = g[8][d];
+    }
+    mx_stress(gm, ph, tau);
+  }
+#pragma unroll
+  for (int k = 0; k < MCF; ++k) {
+    if (o[k] == -2) continue;
+    const int f = e[k] >> 1, side = e[k] & 1;
+    const float4 nA4 = sN[k * kTile + tid];
+    const float nA[3] = {nA4.x * nA4.w, nA4.y * nA4.w, nA4.z * nA4.w};
+    float r[12];
+    if (LINEAR) {
+      const float4 d = sD[k * kTile + tid];
+#pragma unroll
+      for (int v = 0; v < 8; ++v) {
+        const float slope = d.x * g[v][0] + d.y * g[v][1] + d.z * g[v][2];
+        float inc = slope;
+        if (LIMIT)
+          inc = (slope > 0.f) ? fminf(slope, mxv[v] - q[v]) : ((slope < 0.f) ? fmaxf(slope, mn[v] - q[v]) : 0.f);
+        r[v] = q[v] + inc;
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < 8; ++v) r[v] = q[v];
+    }
+    if (VISC) mx_viscous(r, tau, g[8], nA, ph, &r[8]);
+    float* rec = a.fs + (size_t)f * FREC;
+    st_rec(rec + 8 * side, make_float4(r[0], r[1], r[2], r[3]),
+           VISC ? make_float4(r[4], r[8], r[9], r[10]) : make_float4(r[4], 0.f, 0.f, 0.f));
+    if (VISC) a.fsv[2 * (size_t)f + side] = r[11];
+    if (o[k] == -1) {  // ghost side, as in k_mx_sides
+      const int region = a.fregion[f - a.nf_int];
+      const float n[3] = {nA4.x, nA4.y, nA4.z};
+      float gq[10];
+      mx_ghost(q, region, n, a.pc, ph, gq);
+      float vg[4] = {0.f, 0.f, 0.f, 0.f};
+      if (VISC) {
+        const int type = a.pc.region_type[region];
+        float tg[6], gT[3] = {g[8][0], g[8][1], g[8][2]};
+#pragma unroll
+        for (int j = 0; j < 6; ++j) tg[j] = tau[j];
+        if (type == BC_WALL_SLIP || type == BC_SYMMETRY) {
+          float gm[12];
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            gm[d] = g[1][d]; gm[3 + d] = g[2][d]; gm[6 + d] = g[3][d]; gm[9 + d] = g[8][d];
+          }
+#pragma unroll
+          for (int v = 0; v < 4; ++v) {
+            const float gn = gm[3 * v] * n[0] + gm[3 * v + 1] * n[1] + gm[3 * v + 2] * n[2];
+            gm[3 * v] -= gn * n[0]; gm[3 * v + 1] -= gn * n[1]; gm[3 * v + 2] -= gn * n[2];
+          }
+          mx_stress(gm, ph, tg);
+          gT[0] = gm[9]; gT[1] = gm[10]; gT[2] = gm[11];
+        }
+        mx_viscous(gq, tg, gT, nA, ph, vg);
+        a.fsv[2 * (size_t)f + 1] = vg[3];
+      }
+      st_rec(rec + 8, make_float4(gq[0], gq[1], gq[2], gq[3]), make_float4(gq[4], vg[0], vg[1], vg[2]));
     }
   }
 }

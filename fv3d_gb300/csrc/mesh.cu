@@ -303,11 +303,17 @@ fv3d_status prepare_mesh(Ctx& ctx, const fv3d_mesh_arrays& m) {
 fv3d_status upload_mesh(Ctx& ctx) {
   ctx.free_device();
   const int nc = ctx.nc, nf = ctx.nf;
+  ctx.ncp = (nc + kTile - 1) / kTile * kTile;
   UP(ctx.d_perm, ctx.perm.data(), (size_t)nc);
   UP(ctx.d_fc0, ctx.h_fc0.data(), (size_t)nf);
   UP(ctx.d_fc1, ctx.h_fc1.data(), (size_t)nf);
   if (ctx.nb > 0) UP(ctx.d_fregion, ctx.h_fregion.data(), (size_t)ctx.nb);
-  UP(ctx.d_cface, ctx.h_cface.data(), (size_t)nc * ctx.mcf);  // ctx.mcf = padded stride
+  {
+    // ctx.mcf = padded stride; rows up to ncp (whole tiles for the staged gradient pass)
+    std::vector<int> cf((size_t)ctx.ncp * ctx.mcf, -1);
+    std::copy(ctx.h_cface.begin(), ctx.h_cface.end(), cf.begin());
+    UP(ctx.d_cface, cf.data(), cf.size());
+  }
   UP(ctx.d_vol, ctx.h_vol.data(), (size_t)nc);
   UP(ctx.d_dx, ctx.h_dx.data(), (size_t)nc * 3);
   ALLOC(ctx.d_U, (size_t)nc * 5);
@@ -371,7 +377,7 @@ fv3d_status ensure_mixed_path(Ctx& ctx) {
     }
   // per cell: sum_f s_f n_f A_f (closure of the Green-Gauss difference
   // form) with 1/V, and (dx, V) for the time step
-  std::vector<float4> cg(nc), cd(nc);
+  std::vector<float4> cg(ctx.ncp, make_float4(0.f, 0.f, 0.f, 0.f)), cd(nc);
   for (int c = 0; c < nc; ++c) {
     double S[3] = {0.0, 0.0, 0.0};
     for (int k = 0; k < ctx.mcf; ++k) {
@@ -386,7 +392,7 @@ fv3d_status ensure_mixed_path(Ctx& ctx) {
                         (float)ctx.h_dx[3 * (size_t)c + 2], (float)ctx.h_vol[c]);
   }
   // neighbour of every face slot: cell, -1 for a ghost, -2 for padding
-  std::vector<int> nbr((size_t)nc * ctx.mcf, -2);
+  std::vector<int> nbr((size_t)ctx.ncp * ctx.mcf, -2);
   for (int c = 0; c < nc; ++c)
     for (int k = 0; k < ctx.mcf; ++k) {
       const int e = ctx.h_cface[(size_t)c * ctx.mcf + k];
@@ -394,21 +400,35 @@ fv3d_status ensure_mixed_path(Ctx& ctx) {
       const int f = e >> 1;
       nbr[(size_t)c * ctx.mcf + k] = (f >= ctx.nf_int) ? -1 : ((e & 1) ? ctx.h_fc0[f] : ctx.h_fc1[f]);
     }
-  UP(ctx.d_cgeo, cg.data(), (size_t)nc);
+  UP(ctx.d_cgeo, cg.data(), cg.size());
   UP(ctx.d_cdx, cd.data(), (size_t)nc);
   UP(ctx.d_cnbr, nbr.data(), nbr.size());
   UP(ctx.d_fcell, fcell.data(), (size_t)nf);
   UP(ctx.d_slotN, sN.data(), sN.size());
   UP(ctx.d_slotD, sD.data(), sD.size());
-  {
-    std::vector<float4> sNk(sN.size());
+  // slot-major copies [mcf][ncp] (rows padded to whole tiles with zeros):
+  // the flux pass reads slotNk, the staged gradient pass copies one row
+  // segment per slot into shared memory
+  auto slot_major = [&](const std::vector<float4>& src, DevBuf<float4>& dst) -> fv3d_status {
+    std::vector<float4> t((size_t)mcf * ctx.ncp, make_float4(0.f, 0.f, 0.f, 0.f));
     for (int c = 0; c < nc; ++c)
-      for (int k = 0; k < mcf; ++k) sNk[(size_t)k * nc + c] = sN[(size_t)c * mcf + k];
-    UP(ctx.d_slotNk, sNk.data(), sNk.size());
+      for (int k = 0; k < mcf; ++k) t[(size_t)k * ctx.ncp + c] = src[(size_t)c * mcf + k];
+    UP(dst, t.data(), t.size());
+    return FV3D_OK;
+  };
+  fv3d_status st;
+  if ((st = slot_major(sN, ctx.d_slotNk)) != FV3D_OK) return st;
+  if ((st = slot_major(sD, ctx.d_slotDk)) != FV3D_OK) return st;
+  if (ctx.cfg.gradient == FV3D_GRADIENT_LEAST_SQUARES) {
+    UP(ctx.d_slotW, sW.data(), sW.size());
+    if ((st = slot_major(sW, ctx.d_slotWk)) != FV3D_OK) return st;
   }
-  if (ctx.cfg.gradient == FV3D_GRADIENT_LEAST_SQUARES) UP(ctx.d_slotW, sW.data(), sW.size());
-  ALLOC(ctx.d_Uf, (size_t)nc * 8);
-  ALLOC(ctx.d_UfN, (size_t)nc * 8);
+  {
+    cudaError_t e = setup_mx_sides();
+    if (e != cudaSuccess) return ctx.cuda(e, "gradient-pass setup");
+  }
+  ALLOC(ctx.d_Uf, (size_t)ctx.ncp * 8);
+  ALLOC(ctx.d_UfN, (size_t)ctx.ncp * 8);
   ALLOC(ctx.d_kf, (size_t)nc * 5);
   ALLOC(ctx.d_dU, (size_t)nc * 5);
   ALLOC(ctx.d_fs, (size_t)nf * FREC);

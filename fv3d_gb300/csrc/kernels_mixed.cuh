@@ -83,15 +83,15 @@ struct MxArgs {
   const float4* __restrict__ slotDk; // [mcf][ncp] slotD, slot-major
   const float4* __restrict__ slotWk; // [mcf][ncp] slotW, slot-major (least squares only)
   const int* __restrict__ fregion;   // [nf - nf_int]
-  const float4* __restrict__ cgeo;   // [nc] (sum_f s_f n_f A_f, 1/V)
-  const float4* __restrict__ cdx;    // [nc] (dx, V)
+  const float4* __restrict__ cgeo;   // [ncp] (sum_f s_f n_f A_f, 1/V)
+  const float4* __restrict__ cdx;    // [ncp] (dx, V)
   float* Uf;                         // [nc][8] stage state (rho, m, E, p, T, -)
   float* UfN;                        // [nc][8] float(U_n) + p, T
   float* fs;                         // [nf][FREC]
   float* fsv;                        // [nf][2]
   double* U;                         // [5][nc] conserved state U_n (FP64)
-  float* kf;                         // [5][nc] RK register (FP32)
-  float* dU;                         // [5][nc] U_stage - U_n (FP32)
+  float* kf;                         // [5][ncp] RK register (FP32)
+  float* dU;                         // [5][ncp] U_stage - U_n (FP32)
   double* dphi;                      // [5][nc]
   DevScalars* sc;
   PhysConst pc;
@@ -504,7 +504,7 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
         const float gdt = (float)(dt * co.g);
 #pragma unroll
         for (int j = 0; j < 5; ++j) {
-          const size_t i = (size_t)j * a.nc + c;
+          const size_t i = (size_t)j * a.ncp + c;
           const float kj = co.first ? rr[j] : fmaf(a.kf[i], (float)co.a, rr[j]);
           if (!co.last) a.kf[i] = kj;
           du[j] = co.first ? gdt * kj : fmaf(gdt, kj, a.dU[i]);
@@ -513,7 +513,7 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
         const float fdt = (float)dt, c1 = (float)co.c1;
 #pragma unroll
         for (int j = 0; j < 5; ++j) {
-          const size_t i = (size_t)j * a.nc + c;
+          const size_t i = (size_t)j * a.ncp + c;
           du[j] = co.first ? fdt * rr[j] : c1 * fmaf(fdt, rr[j], a.dU[i]);
         }
       }
@@ -542,7 +542,7 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
         un[4] = b1.x + du[4];
 #pragma unroll
         for (int j = 0; j < 5; ++j) {
-          a.dU[(size_t)j * a.nc + c] = du[j];
+          a.dU[(size_t)j * a.ncp + c] = du[j];
           finite = finite && isfinite(du[j]);
         }
         float4 x, y;

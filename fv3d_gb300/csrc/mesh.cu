@@ -377,7 +377,7 @@ fv3d_status ensure_mixed_path(Ctx& ctx) {
     }
   // per cell: sum_f s_f n_f A_f (closure of the Green-Gauss difference
   // form) with 1/V, and (dx, V) for the time step
-  std::vector<float4> cg(ctx.ncp, make_float4(0.f, 0.f, 0.f, 0.f)), cd(nc);
+  std::vector<float4> cg(ctx.ncp, make_float4(0.f, 0.f, 0.f, 0.f)), cd(cg);
   for (int c = 0; c < nc; ++c) {
     double S[3] = {0.0, 0.0, 0.0};
     for (int k = 0; k < ctx.mcf; ++k) {
@@ -401,7 +401,7 @@ fv3d_status ensure_mixed_path(Ctx& ctx) {
       nbr[(size_t)c * ctx.mcf + k] = (f >= ctx.nf_int) ? -1 : ((e & 1) ? ctx.h_fc0[f] : ctx.h_fc1[f]);
     }
   UP(ctx.d_cgeo, cg.data(), cg.size());
-  UP(ctx.d_cdx, cd.data(), (size_t)nc);
+  UP(ctx.d_cdx, cd.data(), cd.size());
   UP(ctx.d_cnbr, nbr.data(), nbr.size());
   UP(ctx.d_fcell, fcell.data(), (size_t)nf);
   UP(ctx.d_slotN, sN.data(), sN.size());
@@ -429,8 +429,8 @@ fv3d_status ensure_mixed_path(Ctx& ctx) {
   }
   ALLOC(ctx.d_Uf, (size_t)ctx.ncp * 8);
   ALLOC(ctx.d_UfN, (size_t)ctx.ncp * 8);
-  ALLOC(ctx.d_kf, (size_t)nc * 5);
-  ALLOC(ctx.d_dU, (size_t)nc * 5);
+  ALLOC(ctx.d_kf, (size_t)ctx.ncp * 5);
+  ALLOC(ctx.d_dU, (size_t)ctx.ncp * 5);
   ALLOC(ctx.d_fs, (size_t)nf * FREC);
   ALLOC(ctx.d_fsv, (size_t)nf * 2);
   return FV3D_OK;

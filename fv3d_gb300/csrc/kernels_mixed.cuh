@@ -51,6 +51,11 @@ namespace fv3d {
 #ifndef FV3D_TMA_MINBLOCKS
 #define FV3D_TMA_MINBLOCKS 4
 #endif
+// the staged gradient pass as a persistent kernel with two tile buffers
+// (k_mx_sides_tma2): the next tile's copies fly while a tile is computed
+#ifndef FV3D_SIDES_PERSIST
+#define FV3D_SIDES_PERSIST 1
+#endif
 #ifndef FV3D_FLUX_MINBLOCKS
 #define FV3D_FLUX_MINBLOCKS 1
 #endif
@@ -667,40 +672,11 @@ struct SidesTile {
 // status bit set when a tile's copies did not arrive within the time limit
 constexpr int kStatusStageTimeout = 4;
 
+// one tile of the staged gradient pass, from the tile in shared memory
+// (layout SidesTile) for the cell c0 + tid: the arithmetic of k_mx_sides
 template <int MCF, int GMODE, bool LINEAR, bool LIMIT, bool VISC>
-__global__ void __launch_bounds__(kTile, FV3D_TMA_MINBLOCKS) k_mx_sides_tma(const __grid_constant__ MxArgs a) {
-  static_assert(GMODE != 0, "the staged gradient pass needs gradients");
+__device__ __forceinline__ void sides_tile(const MxArgs& a, const unsigned char* smem, int c0, int tid) {
   using L = SidesTile<MCF, GMODE>;
-  extern __shared__ __align__(128) unsigned char smem[];
-  const int tid = threadIdx.x;
-  const int c0 = blockIdx.x * kTile;
-  const uint32_t bar = smem_u32(smem + L::bar);
-  if (tid == 0) {
-    mbar_init(bar, 1);
-    fence_mbar_init();
-  }
-  __syncthreads();
-  if (tid == 0) {
-    mbar_expect_tx(bar, L::bytes);
-    const uint32_t s0 = smem_u32(smem);
-    bulk_g2s(s0 + L::uf, a.Uf + 8 * (size_t)c0, kTile * 32, bar);
-    bulk_g2s(s0 + L::cf, a.cface + (size_t)c0 * MCF, kTile * MCF * 4, bar);
-    bulk_g2s(s0 + L::cn, a.cnbr + (size_t)c0 * MCF, kTile * MCF * 4, bar);
-    bulk_g2s(s0 + L::cg, a.cgeo + c0, kTile * 16, bar);
-#pragma unroll
-    for (int k = 0; k < MCF; ++k) {
-      bulk_g2s(s0 + L::sn + k * kTile * 16, a.slotNk + (size_t)k * a.ncp + c0, kTile * 16, bar);
-      bulk_g2s(s0 + L::sd + k * kTile * 16, a.slotDk + (size_t)k * a.ncp + c0, kTile * 16, bar);
-      if (GMODE == 2) bulk_g2s(s0 + L::sw + k * kTile * 16, a.slotWk + (size_t)k * a.ncp + c0, kTile * 16, bar);
-    }
-  }
-  if (!mbar_wait_bounded(bar, 0, 500000000ull)) {
-    // the copies did not land in 0.5 s: report, give them one more bounded
-    // wait so that none is still writing this CTA's shared memory, return
-    if (tid == 0) atomicOr(&a.sc->status, kStatusStageTimeout);
-    mbar_wait_bounded(bar, 0, 500000000ull);
-    return;
-  }
   const int c = c0 + tid;
   if (c >= a.nc) return;
   MxPhys ph;
@@ -835,6 +811,120 @@ __global__ void __launch_bounds__(kTile, FV3D_TMA_MINBLOCKS) k_mx_sides_tma(cons
       }
       st_rec(rec + 8, make_float4(gq[0], gq[1], gq[2], gq[3]), make_float4(gq[4], vg[0], vg[1], vg[2]));
     }
+  }
+}
+
+template <int MCF, int GMODE, bool LINEAR, bool LIMIT, bool VISC>
+__global__ void __launch_bounds__(kTile, FV3D_TMA_MINBLOCKS) k_mx_sides_tma(const __grid_constant__ MxArgs a) {
+  static_assert(GMODE != 0, "the staged gradient pass needs gradients");
+  using L = SidesTile<MCF, GMODE>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int tid = threadIdx.x;
+  const int c0 = blockIdx.x * kTile;
+  const uint32_t bar = smem_u32(smem + L::bar);
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) {
+    mbar_expect_tx(bar, L::bytes);
+    const uint32_t s0 = smem_u32(smem);
+    bulk_g2s(s0 + L::uf, a.Uf + 8 * (size_t)c0, kTile * 32, bar);
+    bulk_g2s(s0 + L::cf, a.cface + (size_t)c0 * MCF, kTile * MCF * 4, bar);
+    bulk_g2s(s0 + L::cn, a.cnbr + (size_t)c0 * MCF, kTile * MCF * 4, bar);
+    bulk_g2s(s0 + L::cg, a.cgeo + c0, kTile * 16, bar);
+#pragma unroll
+    for (int k = 0; k < MCF; ++k) {
+      bulk_g2s(s0 + L::sn + k * kTile * 16, a.slotNk + (size_t)k * a.ncp + c0, kTile * 16, bar);
+      bulk_g2s(s0 + L::sd + k * kTile * 16, a.slotDk + (size_t)k * a.ncp + c0, kTile * 16, bar);
+      if (GMODE == 2) bulk_g2s(s0 + L::sw + k * kTile * 16, a.slotWk + (size_t)k * a.ncp + c0, kTile * 16, bar);
+    }
+  }
+  if (!mbar_wait_bounded(bar, 0, 500000000ull)) {
+    // the copies did not land in 0.5 s: report, give them one more bounded
+    // wait so that none is still writing this CTA's shared memory, return
+    if (tid == 0) atomicOr(&a.sc->status, kStatusStageTimeout);
+    mbar_wait_bounded(bar, 0, 500000000ull);
+    return;
+  }
+  sides_tile<MCF, GMODE, LINEAR, LIMIT, VISC>(a, smem, c0, tid);
+}
+
+// ---------------------------------------------------------------------------
+// persistent form of the staged gradient pass: each CTA walks the tiles
+// blockIdx.x, blockIdx.x + gridDim.x, ... with two tile buffers; the bulk
+// copies of its next tile are in flight while it computes the current one.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+template <int MCF, int GMODE>
+__device__ __forceinline__ void sides_issue(const MxArgs& a, uint32_t s0, uint32_t bar, int c0) {
+  using L = SidesTile<MCF, GMODE>;
+  mbar_expect_tx(bar, L::bytes);
+  bulk_g2s(s0 + L::uf, a.Uf + 8 * (size_t)c0, kTile * 32, bar);
+  bulk_g2s(s0 + L::cf, a.cface + (size_t)c0 * MCF, kTile * MCF * 4, bar);
+  bulk_g2s(s0 + L::cn, a.cnbr + (size_t)c0 * MCF, kTile * MCF * 4, bar);
+  bulk_g2s(s0 + L::cg, a.cgeo + c0, kTile * 16, bar);
+#pragma unroll
+  for (int k = 0; k < MCF; ++k) {
+    bulk_g2s(s0 + L::sn + k * kTile * 16, a.slotNk + (size_t)k * a.ncp + c0, kTile * 16, bar);
+    bulk_g2s(s0 + L::sd + k * kTile * 16, a.slotDk + (size_t)k * a.ncp + c0, kTile * 16, bar);
+    if (GMODE == 2) bulk_g2s(s0 + L::sw + k * kTile * 16, a.slotWk + (size_t)k * a.ncp + c0, kTile * 16, bar);
+  }
+}
+
+// bytes between the two tile buffers (each ends with its mbarrier)
+template <int MCF, int GMODE>
+constexpr int sides_buf_stride() {
+  return (SidesTile<MCF, GMODE>::total + 127) / 128 * 128;
+}
+
+template <int MCF, int GMODE, bool LINEAR, bool LIMIT, bool VISC>
+__global__ void __launch_bounds__(kTile) k_mx_sides_tma2(const __grid_constant__ MxArgs a) {
+  static_assert(GMODE != 0, "the staged gradient pass needs gradients");
+  using L = SidesTile<MCF, GMODE>;
+  constexpr int BUF = sides_buf_stride<MCF, GMODE>();
+  extern __shared__ __align__(128) unsigned char smem[];
+  const int tid = threadIdx.x;
+  const int ntiles = a.ncp / kTile;
+  int t = blockIdx.x;
+  if (t >= ntiles) return;  // whole CTA
+  const uint32_t s0 = smem_u32(smem);
+  const uint32_t bar0 = s0 + L::bar, bar1 = s0 + BUF + L::bar;
+  if (tid == 0) {
+    mbar_init(bar0, 1);
+    mbar_init(bar1, 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (tid == 0) sides_issue<MCF, GMODE>(a, s0, bar0, t * kTile);
+  for (int i = 0; t < ntiles; ++i, t += gridDim.x) {
+    const int b = i & 1;
+    const int tn = t + gridDim.x;
+    if (tid == 0 && tn < ntiles) {
+      // buffer b^1 was last read in iteration i - 1, which every thread has
+      // finished (the barrier at its end); order those reads before the
+      // asynchronous writes
+      fence_proxy_async_smem();
+      sides_issue<MCF, GMODE>(a, s0 + (b ^ 1) * BUF, b ? bar0 : bar1, tn * kTile);
+    }
+    const uint32_t bar = b ? bar1 : bar0, bar_next = b ? bar0 : bar1;
+    const bool ok = __syncthreads_and(mbar_wait_bounded(bar, (i >> 1) & 1, 500000000ull));
+    if (!ok) {
+      // copies did not land in 0.5 s: report; one more bounded wait on each
+      // buffer still being filled so that no copy outlives the CTA's shared memory
+      if (tid == 0) {
+        atomicOr(&a.sc->status, kStatusStageTimeout);
+        mbar_wait_bounded(bar, (i >> 1) & 1, 500000000ull);
+        if (tn < ntiles) mbar_wait_bounded(bar_next, ((i + 1) >> 1) & 1, 500000000ull);
+      }
+      return;
+    }
+    sides_tile<MCF, GMODE, LINEAR, LIMIT, VISC>(a, smem + b * BUF, t * kTile, tid);
+    __syncthreads();  // buffer b is refilled in the next iteration
   }
 }
 

@@ -1,14 +1,24 @@
 // Mixed-precision explicit-stage launchers (gradient pass).
+#include <algorithm>
+
 #include "kernels_mixed.cuh"
 #include "launch.h"
 
 namespace fv3d {
 
 #if FV3D_SIDES_TMA
-// second-order passes: the tile-staged kernel, one CTA of kTile threads per tile
+static int g_sm_count = 0;  // multiprocessors of the device, read in setup_mx_sides
+
+// second-order passes: the tile-staged kernel
 template <int MCF, int G, bool L, bool M, bool V>
 static void launch_staged(const MxArgs& a, cudaStream_t s) {
+#if FV3D_SIDES_PERSIST
+  const int ntiles = a.ncp / kTile;
+  const int grid = std::min(ntiles, std::max(1, g_sm_count) * 4);
+  k_mx_sides_tma2<MCF, G, L, M, V><<<grid, kTile, 2 * sides_buf_stride<MCF, G>(), s>>>(a);
+#else
   k_mx_sides_tma<MCF, G, L, M, V><<<a.ncp / kTile, kTile, SidesTile<MCF, G>::total, s>>>(a);
+#endif
 }
 #define MX_SIDES(G, L, M, V)                                              \
   do {                                                                   \
@@ -37,22 +47,29 @@ static void sides_mcf(const MxArgs& a, const Disc& d, cudaStream_t s, int B) {
 #undef MX_SIDES
 }
 
-// tiles above 48 KB (6 or 8 face slots with least squares) need the opt-in
-// shared-memory size; set once per context setup, outside any stream capture
+// dynamic shared memory above 48 KB needs the opt-in size per kernel; set
+// once per context setup, outside any stream capture
 cudaError_t setup_mx_sides() {
 #if FV3D_SIDES_TMA
-  cudaError_t e = cudaSuccess;
-#define MX_ATTR(MCF, L, M, V)                                                                   \
-  if (e == cudaSuccess)                                                                        \
-    e = cudaFuncSetAttribute(k_mx_sides_tma<MCF, 2, L, M, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             SidesTile<MCF, 2>::total);
-#define MX_ATTR_ALL(MCF)                                                                        \
-  MX_ATTR(MCF, false, false, false) MX_ATTR(MCF, false, false, true) MX_ATTR(MCF, true, false, false) \
-  MX_ATTR(MCF, true, false, true) MX_ATTR(MCF, true, true, false) MX_ATTR(MCF, true, true, true)
-  static_assert(SidesTile<4, 2>::total <= 48 * 1024 && SidesTile<8, 1>::total <= 48 * 1024,
-                "only the least-squares tiles of 6 and 8 slots exceed 48 KB");
-  MX_ATTR_ALL(6)
-  MX_ATTR_ALL(8)
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
+#if FV3D_SIDES_PERSIST
+#define MX_ATTR(MCF, G, L, M, V)                                                                    \
+  if (e == cudaSuccess)                                                                            \
+    e = cudaFuncSetAttribute(k_mx_sides_tma2<MCF, G, L, M, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             2 * sides_buf_stride<MCF, G>());
+#else
+#define MX_ATTR(MCF, G, L, M, V)                                                                    \
+  if (e == cudaSuccess)                                                                            \
+    e = cudaFuncSetAttribute(k_mx_sides_tma<MCF, G, L, M, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                             SidesTile<MCF, G>::total);
+#endif
+#define MX_ATTR_ALL(MCF, G)                                                                          \
+  MX_ATTR(MCF, G, false, false, false) MX_ATTR(MCF, G, false, false, true)                           \
+  MX_ATTR(MCF, G, true, false, false) MX_ATTR(MCF, G, true, false, true)                             \
+  MX_ATTR(MCF, G, true, true, false) MX_ATTR(MCF, G, true, true, true)
+  MX_ATTR_ALL(4, 1) MX_ATTR_ALL(4, 2) MX_ATTR_ALL(6, 1) MX_ATTR_ALL(6, 2) MX_ATTR_ALL(8, 1) MX_ATTR_ALL(8, 2)
 #undef MX_ATTR_ALL
 #undef MX_ATTR
   return e;

@@ -35,7 +35,11 @@ namespace fv3d {
 
 namespace {
 
-constexpr int RED_BLOCKS = 1024;  // fixed grid for deterministic reductions
+constexpr int RED_BLOCKS = 608;   // fixed grid for deterministic reductions (4 per SM)
+// device coefficient slots: h1 [0, 32), h2 [32, 64), |w| and its derived
+// scalars [64, 68), |z|, 1/|z|, eps, 1/eps [68, 72), a host norm [96, 100);
+// FGMRES's y for the solution update at [0, k)
+constexpr int kHostCoefs = 65;
 
 inline int blocks(size_t n, int t = 256) { return (int)((n + t - 1) / t); }
 
@@ -46,62 +50,138 @@ __global__ void k_lincomb(size_t n, double a, const double* __restrict__ x, doub
     out[i] = a * x[i] + b * (y ? y[i] : 0.0);
 }
 
-// partial[b][j] = sum over block b's elements of w * V_j  (j < k)
-__global__ void k_multidot_partial(size_t n, const double* __restrict__ w, const double* __restrict__ V,
-                                   int k, double* __restrict__ partial) {
-  __shared__ double sh[32][33];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;  // 8 warps
-  for (int j0 = 0; j0 < k; j0 += 4) {
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-      const double wi = w[i];
+__device__ __forceinline__ float fmadd(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmadd(double a, double b, double c) { return fma(a, b, c); }
+
+// Krylov vectors are T = double (FP64 Jacobian-vector products) or T =
+// float (FP32 ones: basis, Gram-Schmidt and preconditioner in FP32, on the
+// FP32 pipe); coefficients, norms and the Newton update stay FP64.
+
+// partial[b][j] = sum over block b's elements of w_i V_j,i, j < k <= KMAX:
+// one pass over w and the k vectors; products and sums in T (an FP32 basis
+// is reduced in FP32: GB300's FP64 rate is a small fraction of its FP32
+// rate), in a fixed order over a fixed grid, so deterministic
+template <int KMAX, class T>
+__global__ void __launch_bounds__(256) k_dots_partial(size_t n, const T* __restrict__ w, const T* __restrict__ V,
+                                                      int k, T* __restrict__ partial) {
+  __shared__ T sh[8][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T acc[KMAX];
 #pragma unroll
-      for (int q = 0; q < 4; ++q)
-        if (j0 + q < k) acc[q] = fma(wi, V[(size_t)(j0 + q) * n + i], acc[q]);
-    }
+  for (int j = 0; j < KMAX; ++j) acc[j] = T(0);
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const T wi = w[i];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      double v = acc[q];
+    for (int j = 0; j < KMAX; ++j)
+      if (j < k) acc[j] = fmadd(wi, V[(size_t)j * n + i], acc[j]);
+  }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) sh[warp][q] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < 4 && j0 + (int)threadIdx.x < k) {
-      double s = 0.0;
-      for (int wv = 0; wv < (int)(blockDim.x >> 5); ++wv) s += sh[wv][threadIdx.x];
-      partial[(size_t)blockIdx.x * 32 + j0 + threadIdx.x] = s;
-    }
-    __syncthreads();
+  for (int j = 0; j < KMAX; ++j) {
+    if (j >= k) break;
+    T v = acc[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[warp][j] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32 && (int)threadIdx.x < k) {
+    T s = T(0);
+#pragma unroll
+    for (int wv = 0; wv < 8; ++wv) s += sh[wv][threadIdx.x];
+    partial[(size_t)blockIdx.x * 32 + threadIdx.x] = s;
   }
 }
 
-// out[j] = sum_b partial[b][j] in block order (one block, fixed order)
-__global__ void k_multidot_final(int nb, int k, const double* __restrict__ partial, double* __restrict__ out) {
-  const int j = threadIdx.x;
-  if (j >= k) return;
-  double s = 0.0;
-  for (int b = 0; b < nb; ++b) s += partial[(size_t)b * 32 + j];
-  out[j] = s;
+// out[j] = sum_b partial[b][j]: 32 warps stride the rows, then a
+// fixed-order sum of the 32 warp results.  For a norm (take_sqrt, k = 1)
+// out[0] = |w| and, from the one thread, out[1] = 1/|w|, out[2] = c/|w| and
+// out[3] = |w|/c (each 0 when |w| = 0), so that no other kernel divides
+template <class T>
+__global__ void __launch_bounds__(1024) k_dots_final(int nb, int k, const T* __restrict__ partial,
+                                                     double* __restrict__ out, int take_sqrt, double c) {
+  __shared__ T sh[32][33];
+  const int j = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T s = T(0);
+  if (j < k)
+    for (int b = warp; b < nb; b += 32) s += partial[(size_t)b * 32 + j];
+  sh[warp][j] = s;
+  __syncthreads();
+  if (threadIdx.x < 32 && j < k) {
+    T ts = T(0);
+#pragma unroll
+    for (int wv = 0; wv < 32; ++wv) ts += sh[wv][j];
+    const double t = (double)ts;
+    if (take_sqrt) {
+      const double r = sqrt(t);
+      out[0] = r;
+      out[1] = (r > 0.0) ? 1.0 / r : 0.0;
+      out[2] = (r > 0.0) ? c / r : 0.0;
+      out[3] = (r > 0.0) ? r / c : 0.0;
+    } else {
+      out[j] = t;
+    }
+  }
 }
 
-// w -= sum_j h_j V_j   (h on the device)
-__global__ void k_multi_axpy(size_t n, double* __restrict__ w, const double* __restrict__ V,
-                             const double* __restrict__ h, int k, double sign) {
+// out = x * (*s) when *s > 0 (s = 1/|x| from k_dots_final: the new Arnoldi vector)
+template <class T>
+__global__ void k_scale_dev(size_t n, const T* __restrict__ x, const double* __restrict__ s, T* __restrict__ out) {
+  const double r = *s;
+  if (!(r > 0.0)) return;
+  const T rt = (T)r;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = x[i] * rt;
+}
+
+// out = a x + b y (FP64 inputs) stored as T
+template <class T>
+__global__ void k_to_basis(size_t n, double a, const double* __restrict__ x, double b, const double* __restrict__ y,
+                           T* __restrict__ out) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (T)(a * x[i] + b * (y ? y[i] : 0.0));
+}
+
+// finite-difference state W = U + eps z (FP64), eps on the device
+template <class T>
+__global__ void k_fd_state(size_t n, const double* __restrict__ U, const T* __restrict__ z,
+                           const double* __restrict__ eps, double* __restrict__ W) {
+  const double e = *eps;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    W[i] = U[i] + e * (double)z[i];
+}
+
+// w += sign sum_j h_j V_j   (h on the device, FP64; the sum in T)
+template <class T>
+__global__ void k_multi_axpy(size_t n, T* __restrict__ w, const T* __restrict__ V, const double* __restrict__ h,
+                             int k, double sign) {
+  __shared__ T hs[32];
+  if (threadIdx.x < 32) hs[threadIdx.x] = (threadIdx.x < (unsigned)k) ? (T)(sign * h[threadIdx.x]) : T(0);
+  __syncthreads();
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    T s = T(0);
+    for (int j = 0; j < k; ++j) s = fmadd(hs[j], V[(size_t)j * n + i], s);
+    w[i] = w[i] + s;
+  }
+}
+
+// x += sum_j h_j Z_j in FP64 (the Newton correction from the basis)
+template <class T>
+__global__ void k_axpy_basis(size_t n, double* __restrict__ x, const T* __restrict__ Z, const double* __restrict__ h,
+                             int k) {
   __shared__ double hs[32];
   if (threadIdx.x < 32) hs[threadIdx.x] = (threadIdx.x < (unsigned)k) ? h[threadIdx.x] : 0.0;
   __syncthreads();
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
     double s = 0.0;
-    for (int j = 0; j < k; ++j) s = fma(hs[j], V[(size_t)j * n + i], s);
-    w[i] = w[i] + sign * s;
+    for (int j = 0; j < k; ++j) s = fma(hs[j], (double)Z[(size_t)j * n + i], s);
+    x[i] += s;
   }
 }
 
 // local pseudo-time step per cell (FP64 convective formula)
 __global__ void k_local_dt(int nc, const double* __restrict__ U, const double* __restrict__ vol,
                            const double* __restrict__ dx, double kappa, double km1, double cfl,
-                           double* __restrict__ dtl) {
+                           double* __restrict__ dtl, double* __restrict__ idtl) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   double q[5];
@@ -114,18 +194,27 @@ __global__ void k_local_dt(int nc, const double* __restrict__ U, const double* _
   const double* d = dx + 3 * (size_t)c;
   const double ds = (fabs(u) + cs) * d[0] + (fabs(v) + cs) * d[1] + (fabs(w) + cs) * d[2];
   dtl[c] = cfl * vol[c] / ds;
+  idtl[c] = ds / (cfl * vol[c]);
 }
 
-// out = z / dt - (Rp - Rb) / eps   (per cell dt)
-__global__ void k_jv_combine(int nc, const double* __restrict__ z, const double* __restrict__ Rp,
-                             const double* __restrict__ Rb, const double* __restrict__ dtl, double ieps,
-                             double* __restrict__ out) {
-  const size_t n = 5 * (size_t)nc;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    const int c = (int)(i % nc);
-    out[i] = z[i] / dtl[c] - (Rp[i] - Rb[i]) * ieps;
+// out = z / dt - (Rp - Rb) / eps per cell and variable; idt = 1/dt per
+// cell, ieps = |z| / c = 1/eps on the device (0 for z = 0).  The difference
+// of the two residuals is taken in FP64, the rest in T.
+template <class T>
+__global__ void k_jv_combine(int nc, const T* __restrict__ z, const double* __restrict__ Rp,
+                             const double* __restrict__ Rb, const double* __restrict__ idt,
+                             const double* __restrict__ ieps_p, T* __restrict__ out) {
+  const T ieps = (T)*ieps_p;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    const T id = (T)idt[c];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      const size_t i = (size_t)j * nc + c;
+      out[i] = z[i] * id - (T)(Rp[i] - Rb[i]) * ieps;
+    }
   }
 }
+
 
 // FP32 state record (rho, m, E, p, T) of an FP64 state W (renumbered SoA)
 __global__ void k_make_record(int nc, const double* __restrict__ W, float* __restrict__ Uf,
@@ -306,8 +395,9 @@ __global__ void k_block_invert(int nc, const double* __restrict__ D, float* __re
 }
 
 // z_c = Dinv_c v_c  (FP32 arithmetic)
-__global__ void k_block_apply(int nc, const float* __restrict__ Dinv, const double* __restrict__ v,
-                              double* __restrict__ z) {
+template <class T>
+__global__ void k_block_apply(int nc, const float* __restrict__ Dinv, const T* __restrict__ v,
+                              T* __restrict__ z) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   float x[5];
@@ -319,7 +409,7 @@ __global__ void k_block_apply(int nc, const float* __restrict__ Dinv, const doub
     float s = 0.f;
 #pragma unroll
     for (int j = 0; j < 5; ++j) s = fmaf(M[j * 5 + i], x[j], s);
-    z[(size_t)i * nc + c] = (double)s;
+    z[(size_t)i * nc + c] = (T)s;
   }
 }
 
@@ -357,10 +447,13 @@ fv3d_status Implicit::setup(Ctx& ctx, int m) {
   this->m = m;
   auto al = [&](DevBuf<double>& b, size_t cnt) { return ctx.cuda(b.alloc(cnt), "implicit allocation"); };
   fv3d_status st;
-  if ((st = al(V, (size_t)(m + 1) * n)) || (st = al(Z, (size_t)m * n)) || (st = al(w, n)) ||
+  if ((st = al(w, n)) ||
       (st = al(R, n)) || (st = al(Rb, n)) || (st = al(Rp, n)) || (st = al(Wst, n)) || (st = al(x, n)) ||
-      (st = al(dtl, (size_t)ctx.nc)) || (st = al(D, 25 * (size_t)ctx.nc)) ||
-      (st = al(part, (size_t)RED_BLOCKS * 32)) || (st = al(hdev, 64)) || (st = al(fdist, (size_t)ctx.nf)))
+      (st = al(dtl, (size_t)ctx.nc)) || (st = al(idtl, (size_t)ctx.nc)) || (st = al(D, 25 * (size_t)ctx.nc)) ||
+      (st = al(part, (size_t)RED_BLOCKS * 32)) || (st = al(hdev, 128)) || (st = al(fdist, (size_t)ctx.nf)))
+    return st;
+  if (hpin == nullptr && (st = ctx.cuda(cudaMallocHost((void**)&hpin, sizeof(double) * kHostCoefs),
+                                        "implicit host buffer")) != FV3D_OK)
     return st;
   if ((st = ctx.cuda(Dinv.alloc(25 * (size_t)ctx.nc), "implicit allocation")) != FV3D_OK) return st;
   if ((st = ctx.cuda(bits.alloc(1), "implicit allocation")) != FV3D_OK) return st;
@@ -407,56 +500,56 @@ static fv3d_status residual32(Ctx& ctx, const double* state, double* out) {
   return FV3D_OK;
 }
 
-fv3d_status Implicit::dots(Ctx& ctx, const double* wv, const double* Vb, int k, std::vector<double>& out) {
+// k inner products w . V_j (j < k <= 32) into dst on the device, no host
+// synchronisation; take_sqrt with V = w, k = 1 gives |w| (and the derived
+// scalars of k_dots_final)
+template <class T>
+fv3d_status Implicit::dots_dev(Ctx& ctx, const T* wv, const T* Vb, int k, double* dst, bool take_sqrt, double c) {
   const int nb = std::min(RED_BLOCKS, blocks(n));
-  for (int j0 = 0; j0 < k; j0 += 32) {
-    const int kk = std::min(32, k - j0);
-    k_multidot_partial<<<nb, 256, 0, ctx.stream>>>(n, wv, Vb + (size_t)j0 * n, kk, part.p);
-    k_multidot_final<<<1, 32, 0, ctx.stream>>>(nb, kk, part.p, hdev.p + j0);
-  }
+  T* pt = reinterpret_cast<T*>(part.p);  // sized for RED_BLOCKS x 32 doubles
+  if (k <= 8) k_dots_partial<8, T><<<nb, 256, 0, ctx.stream>>>(n, wv, Vb, k, pt);
+  else if (k <= 16) k_dots_partial<16, T><<<nb, 256, 0, ctx.stream>>>(n, wv, Vb, k, pt);
+  else k_dots_partial<32, T><<<nb, 256, 0, ctx.stream>>>(n, wv, Vb, k, pt);
+  k_dots_final<T><<<1, 1024, 0, ctx.stream>>>(nb, k, pt, dst, take_sqrt ? 1 : 0, c);
   ICK(cudaGetLastError());
-  out.resize(k);
-  ICK(cudaMemcpyAsync(out.data(), hdev.p, sizeof(double) * k, cudaMemcpyDeviceToHost, ctx.stream));
-  ICK(cudaStreamSynchronize(ctx.stream));
   return FV3D_OK;
 }
 
+// |v| on the host (synchronises)
 fv3d_status Implicit::norm(Ctx& ctx, const double* v, double* out) {
-  std::vector<double> h;
-  fv3d_status st = dots(ctx, v, v, 1, h);
+  fv3d_status st = dots_dev<double>(ctx, v, v, 1, hdev.p + 96, true, 1.0);
   if (st != FV3D_OK) return st;
-  *out = sqrt(h[0]);
+  ICK(cudaMemcpyAsync(hpin, hdev.p + 96, sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+  ICK(cudaStreamSynchronize(ctx.stream));
+  *out = hpin[0];
   return FV3D_OK;
 }
 
-fv3d_status Implicit::precondition(Ctx& ctx, const double* v, double* z) {
+template <class T>
+fv3d_status Implicit::precondition(Ctx& ctx, const T* v, T* z) {
   if (opts.preconditioner == FV3D_PC_LEARNED && !use_block_jacobi) return ctx.mlp->apply(ctx, v, z);
   if (opts.preconditioner == FV3D_PC_NONE) {
-    ICK(cudaMemcpyAsync(z, v, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx.stream));
+    ICK(cudaMemcpyAsync(z, v, sizeof(T) * n, cudaMemcpyDeviceToDevice, ctx.stream));
     return FV3D_OK;
   }
-  k_block_apply<<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, Dinv.p, v, z);
+  k_block_apply<T><<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, Dinv.p, v, z);
   ICK(cudaGetLastError());
   return FV3D_OK;
 }
 
-// w = (I/dt - J) z
-fv3d_status Implicit::apply_A(Ctx& ctx, const double* z, double* out) {
-  double zn = 0.0;
-  fv3d_status st = norm(ctx, z, &zn);
-  if (st != FV3D_OK) return st;
-  if (!(zn > 0.0)) {
-    ICK(cudaMemsetAsync(out, 0, sizeof(double) * n, ctx.stream));
-    return FV3D_OK;
-  }
+// w = (I/dt - J) z: the step eps = rel (1 + |U|) / |z| is formed on the
+// device, so a Jacobian-vector product needs no host synchronisation
+template <class T>
+fv3d_status Implicit::apply_A(Ctx& ctx, const T* z, T* out) {
   const double rel = (opts.jv_precision == 1) ? 5e-4 : opts.fd_eps;
-  const double eps = rel * (1.0 + unorm) / zn;
-  k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0, ctx.d_U.p, eps, z, Wst.p);
+  fv3d_status st = dots_dev<T>(ctx, z, z, 1, hdev.p + 68, true, rel * (1.0 + unorm));
+  if (st != FV3D_OK) return st;
+  k_fd_state<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, ctx.d_U.p, z, hdev.p + 70, Wst.p);
   ICK(cudaGetLastError());
   if (opts.jv_precision == 1) st = residual32(ctx, Wst.p, Rp.p);
   else st = residual64(ctx, Wst.p, Rp.p);
   if (st != FV3D_OK) return st;
-  k_jv_combine<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(ctx.nc, z, Rp.p, Rb.p, dtl.p, 1.0 / eps, out);
+  k_jv_combine<T><<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, z, Rp.p, Rb.p, idtl.p, hdev.p + 71, out);
   ICK(cudaGetLastError());
   jv_count += 1;
   return FV3D_OK;
@@ -495,7 +588,10 @@ fv3d_status Implicit::build_blocks(Ctx& ctx) {
 }
 
 // restarted FGMRES(m) for (I/dt - J) x = R, x0 = 0; returns iterations
-fv3d_status Implicit::fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res) {
+// restarted flexible GMRES on the Newton system with basis V, Z and work
+// vector wt of type T (FP32 for FP32 Jacobian-vector products)
+template <class T>
+fv3d_status Implicit::fgmres_t(Ctx& ctx, T* Vt, T* Zt, T* wt, double rnorm, int* iters, double* rel_res) {
   const int m = opts.krylov_dim;
   std::vector<double> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m);
   ICK(cudaMemsetAsync(x.p, 0, sizeof(double) * n, ctx.stream));
@@ -504,15 +600,15 @@ fv3d_status Implicit::fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res
   for (int cyc = 0; cyc <= std::max(0, opts.max_restarts); ++cyc) {
     double beta = rnorm;
     if (cyc == 0) {
-      k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0 / rnorm, R.p, 0.0, nullptr, V.p);
+      k_to_basis<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0 / rnorm, R.p, 0.0, nullptr, Vt);
     } else {
-      // true residual of the current iterate: R - A x
-      fv3d_status st = apply_A(ctx, x.p, w.p);
+      // true residual of the current iterate: R - A x (in FP64)
+      fv3d_status st = apply_A<double>(ctx, x.p, w.p);
       if (st != FV3D_OK) return st;
       k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0, R.p, -1.0, w.p, Rp.p);
       if ((st = norm(ctx, Rp.p, &beta)) != FV3D_OK) return st;
       if (!(beta > opts.eta * rnorm)) { res = beta; break; }
-      k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0 / beta, Rp.p, 0.0, nullptr, V.p);
+      k_to_basis<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0 / beta, Rp.p, 0.0, nullptr, Vt);
     }
     ICK(cudaGetLastError());
     std::fill(H.begin(), H.end(), 0.0);
@@ -521,28 +617,26 @@ fv3d_status Implicit::fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res
     int k = 0;
     bool done = false;
     for (; k < m; ++k) {
-      double* vk = V.p + (size_t)k * n;
-      double* zk = Z.p + (size_t)k * n;
-      fv3d_status st = precondition(ctx, vk, zk);
+      T* vk = Vt + (size_t)k * n;
+      T* zk = Zt + (size_t)k * n;
+      fv3d_status st = precondition<T>(ctx, vk, zk);
       if (st != FV3D_OK) return st;
-      st = apply_A(ctx, zk, w.p);
+      st = apply_A<T>(ctx, zk, wt);
       if (st != FV3D_OK) return st;
-      // classical Gram-Schmidt, twice
-      std::vector<double> h1, h2;
-      if ((st = dots(ctx, w.p, V.p, k + 1, h1)) != FV3D_OK) return st;
-      k_multi_axpy<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, w.p, V.p, hdev.p, k + 1, -1.0);
-      if ((st = dots(ctx, w.p, V.p, k + 1, h2)) != FV3D_OK) return st;
-      k_multi_axpy<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, w.p, V.p, hdev.p, k + 1, -1.0);
+      // classical Gram-Schmidt, twice, the norm and the next basis vector on
+      // the device; one host synchronisation for the Hessenberg column
+      if ((st = dots_dev<T>(ctx, wt, Vt, k + 1, hdev.p, false, 0.0)) != FV3D_OK) return st;
+      k_multi_axpy<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, wt, Vt, hdev.p, k + 1, -1.0);
+      if ((st = dots_dev<T>(ctx, wt, Vt, k + 1, hdev.p + 32, false, 0.0)) != FV3D_OK) return st;
+      k_multi_axpy<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, wt, Vt, hdev.p + 32, k + 1, -1.0);
+      if ((st = dots_dev<T>(ctx, wt, wt, 1, hdev.p + 64, true, 1.0)) != FV3D_OK) return st;
+      k_scale_dev<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, wt, hdev.p + 65, Vt + (size_t)(k + 1) * n);
       ICK(cudaGetLastError());
-      double hn = 0.0;
-      if ((st = norm(ctx, w.p, &hn)) != FV3D_OK) return st;
-      for (int j = 0; j <= k; ++j) H[(size_t)k * (m + 1) + j] = h1[j] + h2[j];
+      ICK(cudaMemcpyAsync(hpin, hdev.p, sizeof(double) * kHostCoefs, cudaMemcpyDeviceToHost, ctx.stream));
+      ICK(cudaStreamSynchronize(ctx.stream));
+      const double hn = hpin[64];
+      for (int j = 0; j <= k; ++j) H[(size_t)k * (m + 1) + j] = hpin[j] + hpin[32 + j];
       H[(size_t)k * (m + 1) + k + 1] = hn;
-      if (hn > 0.0) {
-        k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0 / hn, w.p, 0.0, nullptr,
-                                                                    V.p + (size_t)(k + 1) * n);
-        ICK(cudaGetLastError());
-      }
       // Givens rotations on the new column
       for (int j = 0; j < k; ++j) {
         const double a = H[(size_t)k * (m + 1) + j], b = H[(size_t)k * (m + 1) + j + 1];
@@ -570,7 +664,7 @@ fv3d_status Implicit::fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res
     }
     // x += Z y
     ICK(cudaMemcpyAsync(hdev.p, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, ctx.stream));
-    k_multi_axpy<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, x.p, Z.p, hdev.p, k, 1.0);
+    k_axpy_basis<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, x.p, Zt, hdev.p, k);
     ICK(cudaGetLastError());
     total += k;
     if (done) break;
@@ -578,6 +672,11 @@ fv3d_status Implicit::fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res
   *iters = total;
   *rel_res = res / rnorm;
   return FV3D_OK;
+}
+
+fv3d_status Implicit::fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res) {
+  if (opts.jv_precision == 1) return fgmres_t<float>(ctx, V32.p, Z32.p, w32.p, rnorm, iters, rel_res);
+  return fgmres_t<double>(ctx, V.p, Z.p, w.p, rnorm, iters, rel_res);
 }
 
 fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit_stats* stats) {
@@ -589,6 +688,20 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
   if (st == FV3D_OK && opts.jv_precision == 1) st = ensure_mixed_path(ctx);
   if (st == FV3D_OK) st = setup(ctx, opts.krylov_dim);
   if (st != FV3D_OK) return st;
+  // Krylov basis in the precision of the Jacobian-vector products
+  {
+    const size_t nv = (size_t)(opts.krylov_dim + 1) * n, nz = (size_t)opts.krylov_dim * n;
+    cudaError_t e = cudaSuccess;
+    if (opts.jv_precision == 1) {
+      if (V32.n < nv) e = V32.alloc(nv);
+      if (e == cudaSuccess && Z32.n < nz) e = Z32.alloc(nz);
+      if (e == cudaSuccess && w32.n < n) e = w32.alloc(n);
+    } else {
+      if (V.n < nv) e = V.alloc(nv);
+      if (e == cudaSuccess && Z.n < nz) e = Z.alloc(nz);
+    }
+    if ((st = ctx.cuda(e, "Krylov basis allocation")) != FV3D_OK) return st;
+  }
   history.clear();
   jv_count = 0;
   const auto t0 = std::chrono::steady_clock::now();
@@ -608,7 +721,7 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
     // Newton step with a CFL back-off on failure
     for (int attempt = 0; attempt < 6; ++attempt) {
       k_local_dt<<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, ctx.d_U.p, ctx.d_vol.p, ctx.d_dx.p,
-                                                        ctx.cfg.kappa, ctx.phys.km1, cfl, dtl.p);
+                                                        ctx.cfg.kappa, ctx.phys.km1, cfl, dtl.p, idtl.p);
       ICK(cudaGetLastError());
       if (newton % std::max(1, opts.pc_refresh) == 0 || attempt > 0) {
         if ((st = build_blocks(ctx)) != FV3D_OK) return st;

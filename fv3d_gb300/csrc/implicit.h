@@ -27,6 +27,7 @@ struct Mlp {
   fv3d_status train(Ctx& ctx, const fv3d_mlp_train_opts& o, fv3d_mlp_train_stats* stats);
   fv3d_status build_features(Ctx& ctx, const Implicit& im);
   fv3d_status apply(Ctx& ctx, const double* v, double* z);
+  fv3d_status apply(Ctx& ctx, const float* v, float* z);
   fv3d_status harvest(Ctx& ctx, const Implicit& im);
 };
 
@@ -34,21 +35,32 @@ struct Implicit {
   fv3d_implicit_opts opts;
   size_t n = 0;   // 5 * cells
   int m = 0;      // Krylov dimension allocated
-  DevBuf<double> V, Z, w, R, Rb, Rp, Wst, x, dtl, D, part, hdev, fdist;
+  DevBuf<double> V, Z, w, R, Rb, Rp, Wst, x, dtl, idtl, D, part, hdev, fdist;
+  DevBuf<float> V32, Z32, w32;    // Krylov basis for FP32 Jacobian-vector products
   DevBuf<float> Dinv;
   DevBuf<unsigned long long> bits;
   std::vector<double> history;  // ||R||_2 per Newton step
   int jv_count = 0;
   double unorm = 0.0;
   bool use_block_jacobi = false;  // learned preconditioner fell back this step
+  double* hpin = nullptr;         // pinned host copy of the Arnoldi coefficients (kHostCoefs doubles)
+
+  ~Implicit() {
+    if (hpin) cudaFreeHost(hpin);
+  }
 
   fv3d_status setup(Ctx& ctx, int m);
   fv3d_status solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit_stats* stats);
   fv3d_status fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res);
-  fv3d_status apply_A(Ctx& ctx, const double* z, double* out);
-  fv3d_status precondition(Ctx& ctx, const double* v, double* z);
+  template <class T>
+  fv3d_status fgmres_t(Ctx& ctx, T* Vt, T* Zt, T* wt, double rnorm, int* iters, double* rel_res);
+  template <class T>
+  fv3d_status apply_A(Ctx& ctx, const T* z, T* out);
+  template <class T>
+  fv3d_status precondition(Ctx& ctx, const T* v, T* z);
   fv3d_status build_blocks(Ctx& ctx);
-  fv3d_status dots(Ctx& ctx, const double* w, const double* V, int k, std::vector<double>& out);
+  template <class T>
+  fv3d_status dots_dev(Ctx& ctx, const T* w, const T* V, int k, double* dst, bool take_sqrt, double c);
   fv3d_status norm(Ctx& ctx, const double* v, double* out);
   fv3d_status ICK_copy(Ctx& ctx, double* dst, const double* src);
 };

@@ -322,9 +322,11 @@ __global__ void __launch_bounds__(128) k_mlp_forward(const float* __restrict__ P
 
 // preconditioner application z = M(v): features of each cell from its
 // block / geometry record and its vector, MLP, rescale
+// (vectors in FP64 or, for the FP32 Krylov basis, FP32)
+template <class T>
 __global__ void __launch_bounds__(128) k_mlp_apply(const float* __restrict__ P, int nc,
-                                                   const float* __restrict__ feat, const double* __restrict__ v,
-                                                   double* __restrict__ z) {
+                                                   const float* __restrict__ feat, const T* __restrict__ v,
+                                                   T* __restrict__ z) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MlpW& W = *reinterpret_cast<MlpW*>(smem_raw);
   MlpAct& A = *reinterpret_cast<MlpAct*>(smem_raw + sizeof(MlpW));
@@ -356,7 +358,7 @@ __global__ void __launch_bounds__(128) k_mlp_apply(const float* __restrict__ P, 
   __syncthreads();
   for (int i = threadIdx.x; i < MLP_TILE * MLP_OUT; i += blockDim.x) {
     const int r = i / MLP_OUT, o = i % MLP_OUT, c = base + r;
-    if (c < nc) z[(size_t)o * nc + c] = (double)(A.y[r * 8 + o] * vn[r] * feat[(size_t)c * MLP_FEAT + 31]);
+    if (c < nc) z[(size_t)o * nc + c] = (T)(A.y[r * 8 + o] * vn[r] * feat[(size_t)c * MLP_FEAT + 31]);
   }
 }
 
@@ -458,7 +460,8 @@ fv3d_status Mlp::init(Ctx& ctx, unsigned long long seed) {
   ready = true;
   MCK(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
   MCK(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem()));
-  MCK(cudaFuncSetAttribute(k_mlp_apply, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem()));
+  MCK(cudaFuncSetAttribute(k_mlp_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem()));
+  MCK(cudaFuncSetAttribute(k_mlp_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem()));
   return FV3D_OK;
 }
 
@@ -572,7 +575,15 @@ fv3d_status Mlp::build_features(Ctx& ctx, const Implicit& im) {
 }
 
 fv3d_status Mlp::apply(Ctx& ctx, const double* vin, double* zout) {
-  k_mlp_apply<<<(ctx.nc + MLP_TILE - 1) / MLP_TILE, 128, fwd_smem(), ctx.stream>>>(P.p, ctx.nc, feat.p, vin, zout);
+  k_mlp_apply<double><<<(ctx.nc + MLP_TILE - 1) / MLP_TILE, 128, fwd_smem(), ctx.stream>>>(P.p, ctx.nc, feat.p, vin,
+                                                                                          zout);
+  MCK(cudaGetLastError());
+  return FV3D_OK;
+}
+
+fv3d_status Mlp::apply(Ctx& ctx, const float* vin, float* zout) {
+  k_mlp_apply<float><<<(ctx.nc + MLP_TILE - 1) / MLP_TILE, 128, fwd_smem(), ctx.stream>>>(P.p, ctx.nc, feat.p, vin,
+                                                                                         zout);
   MCK(cudaGetLastError());
   return FV3D_OK;
 }

@@ -76,6 +76,14 @@ class ImplicitStats(C.Structure):
                 ("rel_res", C.c_double), ("wall_ms", C.c_double), ("cfl_final", C.c_double)]
 
 
+class NewtonOpts(C.Structure):
+    _fields_ = [("scheme", C.c_int), ("max_iter_inner", C.c_int), ("is_transient", C.c_int)]
+
+
+class NewtonStats(C.Structure):
+    _fields_ = [("n_inner", C.c_int), ("err0", C.c_double), ("err", C.c_double)]
+
+
 class MlpTrainOpts(C.Structure):
     _fields_ = [("epochs", C.c_int), ("batch", C.c_int), ("lr", C.c_double), ("seed", C.c_ulonglong)]
 
@@ -114,6 +122,8 @@ EXPORTS = {
     "fv3d_solve_implicit": ([C.c_void_p, C.POINTER(ImplicitOpts), C.POINTER(ImplicitStats)], C.c_int),
     "fv3d_implicit_history": ([C.c_void_p, _f8p, C.c_int, C.POINTER(C.c_int)], C.c_int),
     "fv3d_get_blocks": ([C.c_void_p, _f8p], C.c_int),
+    "fv3d_step_newton": ([C.c_void_p, C.POINTER(NewtonOpts), C.c_int, C.c_double, C.c_double,
+                          C.POINTER(NewtonStats)], C.c_int),
     "fv3d_mlp_num_params": ([], C.c_int),
     "fv3d_mlp_init": ([C.c_void_p, C.c_ulonglong], C.c_int),
     "fv3d_mlp_get_params": ([C.c_void_p, _f4p], C.c_int),
@@ -282,6 +292,17 @@ class Solver:
         out = np.empty((self.nc, 5, 5))
         self._check(self.lib.fv3d_get_blocks(self.h, _p(out, _f8p)))
         return out  # out[i, col, row]
+
+    def step_newton(self, iter_: int, t: float, dt: float, scheme: str = "euler", max_iter_inner: int = 100,
+                    is_transient: bool = True, check: bool = True):
+        """timestep_newton (implicit.c:224-351): one implicit BE / BDF2 step with
+        the lumped Jacobian; returns the stats (n_inner, err0, err)."""
+        o = NewtonOpts({"euler": 0, "bdf2": 1}[scheme], max_iter_inner, int(is_transient))
+        st = NewtonStats()
+        rc = self.lib.fv3d_step_newton(self.h, C.byref(o), iter_, t, dt, C.byref(st))
+        if check:
+            self._check(rc)
+        return {"n_inner": st.n_inner, "err0": st.err0, "err": st.err, "status": rc}
 
     # ---- learned preconditioner ----
     def mlp_init(self, seed: int = 1):

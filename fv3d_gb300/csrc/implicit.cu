@@ -429,6 +429,81 @@ __global__ void k_min_rho_p(int nc, const double* __restrict__ U, double km1, un
   if ((threadIdx.x & 31) == 0) atomicMin(out, b);
 }
 
+// ---- the reference's implicit time step ------------------------------------
+// f_Y = -(Y - Y_old0) / dt + b dY/dt - sum_s a_s / dt Y_old_s  (the newton
+// right-hand side of implicit.c, in its operation order)
+__global__ void k_newton_rhs(size_t n, const double* __restrict__ Y, const double* __restrict__ old0,
+                             const double* __restrict__ old1, const double* __restrict__ dYdt, double dt, double b,
+                             double a0, double a1, int stages, double* __restrict__ fY) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    double f = -(Y[i] - old0[i]) / dt + b * dYdt[i];
+    f -= a0 / dt * old0[i];
+    if (stages > 1) f -= a1 / dt * old1[i];
+    fY[i] = f;
+  }
+}
+
+// column v of the lumped blocks (implicit.c:98-116): (-R(Y + e/2) + R(Y - e/2))
+// * b / (eps + 1e-16), plus 1/dt on the diagonal; blocks column-major
+__global__ void k_newton_column(int nc, int v, const double* __restrict__ Rp, const double* __restrict__ Rm,
+                                double f, double idt, double* __restrict__ D) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    double x = -Rp[(size_t)j * nc + c];
+    x += Rm[(size_t)j * nc + c];
+    x *= f;
+    if (j == v) x += idt;
+    D[(size_t)c * 25 + v * 5 + j] = x;
+  }
+}
+
+// x_c = D_c^{-1} b_c per cell (5x5, column-major, Gaussian elimination with
+// partial pivoting in FP64); a singular block gives NaN (reported by the host)
+__global__ void k_block_solve(int nc, const double* __restrict__ D, const double* __restrict__ b,
+                              double* __restrict__ x) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  double M[5][6];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+#pragma unroll
+    for (int j = 0; j < 5; ++j) M[i][j] = D[(size_t)c * 25 + j * 5 + i];
+    M[i][5] = b[(size_t)i * nc + c];
+  }
+  bool ok = true;
+#pragma unroll
+  for (int col = 0; col < 5; ++col) {
+    int piv = col;
+#pragma unroll
+    for (int i = col + 1; i < 5; ++i)
+      if (fabs(M[i][col]) > fabs(M[piv][col])) piv = i;
+    if (!(fabs(M[piv][col]) > 0.0)) ok = false;
+#pragma unroll
+    for (int i = 0; i < 5; ++i)
+      if (i == piv && piv != col)
+#pragma unroll
+        for (int j = 0; j < 6; ++j) { const double tmp = M[col][j]; M[col][j] = M[i][j]; M[i][j] = tmp; }
+#pragma unroll
+    for (int i = col + 1; i < 5; ++i) {
+      const double l = M[i][col] / M[col][col];
+#pragma unroll
+      for (int j = col; j < 6; ++j) M[i][j] -= l * M[col][j];
+    }
+  }
+  double y[5];
+#pragma unroll
+  for (int i = 4; i >= 0; --i) {
+    double s = M[i][5];
+#pragma unroll
+    for (int j = i + 1; j < 5; ++j) s -= M[i][j] * y[j];
+    y[i] = s / M[i][i];
+  }
+#pragma unroll
+  for (int i = 0; i < 5; ++i) x[(size_t)i * nc + c] = ok ? y[i] : NAN;
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -782,6 +857,89 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
   return FV3D_OK;
 }
 
+// timestep_newton (implicit.c:224-351): U is the state Y; R(U) the FP64
+// time derivative; ten perturbed residuals build the lumped blocks each
+// Newton iteration; the block-diagonal system is solved cell by cell
+fv3d_status Implicit::step_newton(Ctx& ctx, const fv3d_newton_opts& o, int iter, double t, double dt,
+                                  fv3d_newton_stats* stats) {
+  (void)t;  // the implemented boundary conditions do not depend on time
+  fv3d_status st = ensure_fp64_path(ctx);
+  if (st == FV3D_OK) st = setup(ctx, 1);
+  if (st != FV3D_OK) return st;
+  cudaError_t e = cudaSuccess;
+  for (DevBuf<double>* b : {&old0, &old1, &dYdt, &fY})
+    if (e == cudaSuccess && b->n < n) e = b->alloc(n);
+  if ((st = ctx.cuda(e, "implicit step allocation")) != FV3D_OK) return st;
+  const int grid = std::min(4096, blocks(n));
+  double* U = ctx.d_U.p;
+  if (!newton_ready || iter == 0) {
+    n_bdf = (o.scheme == FV3D_NEWTON_EULER) ? 1 : 2;
+    ICK(cudaMemsetAsync(old0.p, 0, sizeof(double) * n, ctx.stream));
+    ICK(cudaMemsetAsync(old1.p, 0, sizeof(double) * n, ctx.stream));
+    if ((st = residual64(ctx, U, dYdt.p)) != FV3D_OK) return st;  // time derivative at t
+    newton_ready = true;
+  }
+  const bool start = iter < n_bdf;
+  const int stages = start ? 1 : n_bdf;
+  const double a0 = (start || o.scheme == FV3D_NEWTON_EULER) ? 0.0 : -1. / 3.;
+  const double a1 = (start || o.scheme == FV3D_NEWTON_EULER) ? 0.0 : 1 / 3.;
+  const double bb = (start || o.scheme == FV3D_NEWTON_EULER) ? 1.0 : 2. / 3.;
+  if (stages > 1) ICK(cudaMemcpyAsync(old1.p, old0.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx.stream));
+  ICK(cudaMemcpyAsync(old0.p, U, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx.stream));
+  k_newton_rhs<<<grid, 256, 0, ctx.stream>>>(n, U, old0.p, old1.p, dYdt.p, dt, bb, a0, a1, stages, fY.p);
+  ICK(cudaGetLastError());
+  double err0 = 0.0, err = 0.0;
+  if ((st = norm(ctx, fY.p, &err0)) != FV3D_OK) return st;
+  err = err0;
+  std::vector<double> slice(ctx.nc);
+  int it;
+  for (it = 1; it <= o.max_iter_inner; ++it) {
+    // lumped Jacobian (implicit.c:65-117); eps from the variable's norm in
+    // reference cell order
+    for (int v = 0; v < 5; ++v) {
+      ICK(cudaMemcpyAsync(slice.data(), U + (size_t)v * ctx.nc, sizeof(double) * ctx.nc, cudaMemcpyDeviceToHost,
+                          ctx.stream));
+      ICK(cudaStreamSynchronize(ctx.stream));
+      double s2 = 0.0;
+      for (int i = 0; i < ctx.nc; ++i) s2 += slice[ctx.iperm[i]] * slice[ctx.iperm[i]];
+      const double eps = sqrt(s2) * 1e-4;
+      k_perturb_all<<<grid, 256, 0, ctx.stream>>>(ctx.nc, U, v, 0.5 * eps, Wst.p);
+      if ((st = residual64(ctx, Wst.p, Rp.p)) != FV3D_OK) return st;
+      k_perturb_all<<<grid, 256, 0, ctx.stream>>>(ctx.nc, U, v, -0.5 * eps, Wst.p);
+      if ((st = residual64(ctx, Wst.p, w.p)) != FV3D_OK) return st;
+      k_newton_column<<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, v, Rp.p, w.p, bb / (eps + 1e-16), 1.0 / dt,
+                                                              D.p);
+    }
+    ICK(cudaGetLastError());
+    if (err >= err0) {
+      k_block_solve<<<blocks(ctx.nc, 128), 128, 0, ctx.stream>>>(ctx.nc, D.p, fY.p, x.p);
+      k_lincomb<<<grid, 256, 0, ctx.stream>>>(n, 1.0, U, 1.0, x.p, Wst.p);
+      ICK(cudaMemcpyAsync(U, Wst.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx.stream));
+      ICK(cudaGetLastError());
+      if ((st = residual64(ctx, U, dYdt.p)) != FV3D_OK) return st;
+      k_newton_rhs<<<grid, 256, 0, ctx.stream>>>(n, U, old0.p, old1.p, dYdt.p, dt, bb, a0, a1, stages, fY.p);
+      ICK(cudaGetLastError());
+      if ((st = norm(ctx, fY.p, &err)) != FV3D_OK) return st;
+      if (!std::isfinite(err)) return ctx.fail(FV3D_ERR_NONFINITE, "implicit step: non-finite residual");
+    } else {
+      if ((st = residual64(ctx, U, dYdt.p)) != FV3D_OK) return st;
+    }
+    if (err < err0) break;
+    if (!o.is_transient) break;
+  }
+  ICK(cudaMemcpyAsync(ctx.d_dphi.p, dYdt.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx.stream));
+  ICK(cudaStreamSynchronize(ctx.stream));
+  ctx.residual_valid = true;
+  if (stats) {
+    stats->n_inner = it;
+    stats->err0 = err0;
+    stats->err = err;
+  }
+  if (it >= o.max_iter_inner)
+    return ctx.fail(FV3D_ERR_NOT_CONVERGED, "implicit step: no convergence in %d iterations", o.max_iter_inner);
+  return FV3D_OK;
+}
+
 fv3d_status Implicit::ICK_copy(Ctx& ctx, double* dst, const double* src) {
   ICK(cudaMemcpyAsync(dst, src, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx.stream));
   return FV3D_OK;
@@ -846,4 +1004,20 @@ extern "C" fv3d_status fv3d_get_blocks(fv3d_ctx* handle, double* blocks_out) {
   for (int c = 0; c < ctx->nc; ++c)
     memcpy(blocks_out + 25 * (size_t)ctx->perm[c], &tmp[25 * (size_t)c], sizeof(double) * 25);
   return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_step_newton(fv3d_ctx* handle, const fv3d_newton_opts* opts, int iter, double t,
+                                        double dt, fv3d_newton_stats* stats) {
+  if (handle == nullptr || opts == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (!ctx->mesh_ready || !ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "mesh and state required");
+  if ((opts->scheme != FV3D_NEWTON_EULER && opts->scheme != FV3D_NEWTON_BDF2) || opts->max_iter_inner < 1 ||
+      !(dt > 0.0) || iter < 0)
+    return ctx->fail(FV3D_ERR_INVALID_ARG, "bad implicit step arguments");
+  for (int b = 0; b < ctx->nb; ++b)
+    if (!(ctx->region_set & (1u << ctx->h_fregion[b])))
+      return ctx->fail(FV3D_ERR_STATE, "boundary region %d has no condition", ctx->h_fregion[b]);
+  if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "cudaSetDevice");
+  if (!ctx->implicit) ctx->implicit = new Implicit();
+  return ctx->implicit->step_newton(*ctx, *opts, iter, t, dt, stats);
 }

@@ -63,6 +63,13 @@ struct Implicit {
   fv3d_status dots_dev(Ctx& ctx, const T* w, const T* V, int k, double* dst, bool take_sqrt, double c);
   fv3d_status norm(Ctx& ctx, const double* v, double* out);
   fv3d_status ICK_copy(Ctx& ctx, double* dst, const double* src);
+
+  // the reference's implicit time step (timestep_newton)
+  DevBuf<double> old0, old1, dYdt, fY;
+  int n_bdf = 0;
+  bool newton_ready = false;
+  fv3d_status step_newton(Ctx& ctx, const fv3d_newton_opts& o, int iter, double t, double dt,
+                          fv3d_newton_stats* stats);
 };
 
 }  // namespace fv3d

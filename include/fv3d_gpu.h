@@ -215,6 +215,29 @@ fv3d_status fv3d_implicit_history(const fv3d_ctx *ctx, double *res, int max, int
  * reference cell order (lumped blocks: compare with calc_jacobian_numerical) */
 fv3d_status fv3d_get_blocks(fv3d_ctx *ctx, double *blocks);
 
+/* ---- the reference's implicit time step -------------------------------------- */
+/* timestep_newton (implicit.c:224-351) with the lumped Jacobian of
+ * calc_jacobian_numerical (implicit.c:61-119: every cell perturbed at once by
+ * +-eps/2, eps = 1e-4 ||Y_v||_2, ten FP64 residuals per Newton iteration).
+ * The reference solves the block-diagonal system J dY = f_Y with basec's
+ * GMRES / BiCGStab to tolerance_lsoe; here each cell's 5x5 block is solved
+ * directly (Gaussian elimination with partial pivoting, FP64), which is the
+ * converged Krylov answer.  iter is the time-step index (0 starts BDF2 with
+ * backward Euler and evaluates the time derivative at t, as timedisc.c does). */
+typedef enum { FV3D_NEWTON_EULER = 0, FV3D_NEWTON_BDF2 = 1 } fv3d_newton_scheme;
+typedef struct {
+    int scheme;          /* a fv3d_newton_scheme value; coefficients of implicit.c:37-38 */
+    int max_iter_inner;  /* Newton iterations per step (reference default 100) */
+    int is_transient;    /* 0: stop after the first Newton iteration */
+} fv3d_newton_opts;
+typedef struct {
+    int n_inner;         /* Newton iterations taken (the reference's n_inner) */
+    double err0, err;    /* ||f_Y|| before and after */
+} fv3d_newton_stats;
+/* FV3D_ERR_NOT_CONVERGED when it reaches max_iter_inner, as the reference */
+fv3d_status fv3d_step_newton(fv3d_ctx *ctx, const fv3d_newton_opts *opts, int iter, double t,
+                             double dt, fv3d_newton_stats *stats);
+
 /* ---- learned preconditioner (per-cell MLP 36-64-64-64-5, GELU) -------------------- */
 /* BF16 weights / FP32 accumulation on tensor cores, trained on (residual,
  * Newton-correction) pairs that the plain implicit solver harvests; used only

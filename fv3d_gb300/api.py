@@ -84,6 +84,21 @@ class NewtonStats(C.Structure):
     _fields_ = [("n_inner", C.c_int), ("err0", C.c_double), ("err", C.c_double)]
 
 
+ITERATION_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double), C.c_int)
+
+
+class TimedOpts(C.Structure):
+    _fields_ = [("implicit", C.c_int), ("scheme", C.c_int), ("max_iter", C.c_int), ("is_transient", C.c_int),
+                ("abort_residual", C.c_double), ("t_start", C.c_double), ("t_end", C.c_double),
+                ("cfl", C.c_double), ("max_iter_inner", C.c_int), ("on_iteration", ITERATION_FN),
+                ("user", C.c_void_p)]
+
+
+class TimedStats(C.Structure):
+    _fields_ = [("iter", C.c_int), ("t", C.c_double), ("dt", C.c_double), ("res", C.c_double * 5),
+                ("stop_reason", C.c_int)]
+
+
 class MlpTrainOpts(C.Structure):
     _fields_ = [("epochs", C.c_int), ("batch", C.c_int), ("lr", C.c_double), ("seed", C.c_ulonglong)]
 
@@ -124,6 +139,7 @@ EXPORTS = {
     "fv3d_get_blocks": ([C.c_void_p, _f8p], C.c_int),
     "fv3d_step_newton": ([C.c_void_p, C.POINTER(NewtonOpts), C.c_int, C.c_double, C.c_double,
                           C.POINTER(NewtonStats)], C.c_int),
+    "fv3d_timedisc": ([C.c_void_p, C.POINTER(TimedOpts), C.POINTER(TimedStats)], C.c_int),
     "fv3d_mlp_num_params": ([], C.c_int),
     "fv3d_mlp_init": ([C.c_void_p, C.c_ulonglong], C.c_int),
     "fv3d_mlp_get_params": ([C.c_void_p, _f4p], C.c_int),
@@ -303,6 +319,26 @@ class Solver:
         if check:
             self._check(rc)
         return {"n_inner": st.n_inner, "err0": st.err0, "err": st.err, "status": rc}
+
+    def timedisc(self, scheme="rk33", implicit=False, max_iter=1000, is_transient=True, abort_residual=1e-10,
+                 t_start=0.0, t_end=0.2, cfl=0.5, max_iter_inner=100, check=True):
+        """timedisc (timedisc.c:134-222): returns the final stats and the
+        per-iteration rows (iter, t, dt, res[5], n_inner) print_residual prints."""
+        rows = []
+
+        def on_iter(_user, it, t, dt, res, n_inner):
+            rows.append((it, t, dt, [res[j] for j in range(5)], n_inner))
+
+        cb = ITERATION_FN(on_iter)
+        sch = {"euler": 0, "bdf2": 1}[scheme] if implicit else SCHEMES[scheme]
+        o = TimedOpts(int(implicit), sch, max_iter, int(is_transient), abort_residual, t_start, t_end, cfl,
+                      max_iter_inner, cb, None)
+        st = TimedStats()
+        rc = self.lib.fv3d_timedisc(self.h, C.byref(o), C.byref(st))
+        if check:
+            self._check(rc)
+        return {"iter": st.iter, "t": st.t, "dt": st.dt, "res": list(st.res), "stop_reason": st.stop_reason,
+                "status": rc}, rows
 
     # ---- learned preconditioner ----
     def mlp_init(self, seed: int = 1):

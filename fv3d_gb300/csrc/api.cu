@@ -6,6 +6,8 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cfloat>
+#include <cstddef>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -534,22 +536,51 @@ static const double RK_G[3][5] = {
      2277821191437.0 / 14882151754819.0}};
 static const int RK_S[3] = {1, 3, 5};
 
-static fv3d_status enqueue_step(Ctx* ctx, int scheme, double cfl) {
+// store_r: the last stage also stores its time derivative in dphi (what
+// calc_global_residual reads after a reference step)
+static fv3d_status enqueue_step(Ctx* ctx, int scheme, double cfl, bool store_r) {
   const bool dt_dev = cfl > 0.0;
   if (scheme == FV3D_SSP_RK3) {
     const double c0[3] = {0.0, 0.75, 1.0 / 3.0}, c1[3] = {1.0, 0.25, 2.0 / 3.0};
     for (int s = 0; s < 3; ++s) {
-      StageCoef co{0, 0, c0[s], c1[s], s == 0, s == 2};
+      StageCoef co{0, 0, c0[s], c1[s], s == 0, s == 2, store_r && s == 2};
       CK(ctx->launch_stage_kernels(2, dt_dev && s == 2, co, 7));
     }
   } else {
     for (int s = 0; s < RK_S[scheme]; ++s) {
-      StageCoef co{RK_A[scheme][s], RK_G[scheme][s], 0, 0, s == 0, s == RK_S[scheme] - 1};
-      CK(ctx->launch_stage_kernels(1, dt_dev && s == RK_S[scheme] - 1, co, 7));
+      const bool last = s == RK_S[scheme] - 1;
+      StageCoef co{RK_A[scheme][s], RK_G[scheme][s], 0, 0, s == 0, last, store_r && last};
+      CK(ctx->launch_stage_kernels(1, dt_dev && last, co, 7));
     }
   }
   k_finish_step<<<1, 1, 0, ctx->stream>>>(ctx->d_sc.p, cfl);
   CK(cudaGetLastError());
+  return FV3D_OK;
+}
+
+// the captured graph of one explicit step, built on first use
+static fv3d_status step_graph(Ctx* ctx, int scheme, double cfl, bool store_r, cudaGraphExec_t* out) {
+  const std::tuple<int, double, int> key(scheme, cfl, store_r ? 1 : 0);
+  auto it = ctx->graphs.find(key);
+  if (it != ctx->graphs.end()) {
+    *out = it->second;
+    return FV3D_OK;
+  }
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  fv3d_status est = enqueue_step(ctx, scheme, cfl, store_r);
+  cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+  if (est != FV3D_OK) {
+    if (g) cudaGraphDestroy(g);
+    return est;
+  }
+  CK(ce);
+  ce = cudaGraphInstantiate(&exec, g, 0);
+  cudaGraphDestroy(g);
+  CK(ce);
+  ctx->graphs[key] = exec;
+  *out = exec;
   return FV3D_OK;
 }
 
@@ -573,26 +604,8 @@ extern "C" fv3d_status fv3d_step_explicit(fv3d_ctx* handle, int scheme, int n_st
   k_set_dt<<<1, 1, 0, ctx->stream>>>(ctx->d_sc.p, ctx->d_bits.p, cfl, dt_fixed);
   CK(cudaGetLastError());
   // one graph per (scheme, cfl) replayed n_steps times
-  const std::pair<int, double> key(scheme, cfl);
-  auto it = ctx->graphs.find(key);
   cudaGraphExec_t exec = nullptr;
-  if (it == ctx->graphs.end()) {
-    cudaGraph_t g = nullptr;
-    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    fv3d_status est = enqueue_step(ctx, scheme, cfl);
-    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
-    if (est != FV3D_OK) {
-      if (g) cudaGraphDestroy(g);
-      return est;
-    }
-    CK(ce);
-    ce = cudaGraphInstantiate(&exec, g, 0);
-    cudaGraphDestroy(g);
-    CK(ce);
-    ctx->graphs[key] = exec;
-  } else {
-    exec = it->second;
-  }
+  if ((st = step_graph(ctx, scheme, cfl, false, &exec)) != FV3D_OK) return st;
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   for (int i = 0; i < n_steps; ++i) CK(cudaGraphLaunch(exec, ctx->stream));
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
@@ -716,5 +729,114 @@ extern "C" fv3d_status fv3d_profile_stage(fv3d_ctx* handle, int n_reps, double c
   for (int i = 0; i < 4; ++i) cudaEventDestroy(ev[i]);
   for (int k = 0; k < 3; ++k) ms[k] = acc[k] / n_reps;
   if (!ctx->fp64()) { ms[1] = ms[2]; ms[2] = 0.0; }
+  return FV3D_OK;
+}
+
+// ---------------------------------------------------------------------------
+// timedisc (timedisc.c:134-222): the step loop with its stop criteria
+// ---------------------------------------------------------------------------
+extern "C" fv3d_status fv3d_timedisc(fv3d_ctx* handle, const fv3d_timedisc_opts* o, fv3d_timedisc_stats* stats) {
+  if (handle == nullptr || o == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  REQUIRE(o->implicit == 0 || o->implicit == 1, FV3D_ERR_INVALID_ARG, "bad time discretisation %d", o->implicit);
+  REQUIRE(o->implicit ? (o->scheme == FV3D_NEWTON_EULER || o->scheme == FV3D_NEWTON_BDF2)
+                      : (o->scheme >= 0 && o->scheme <= 3),
+          FV3D_ERR_INVALID_ARG, "bad scheme %d", o->scheme);
+  REQUIRE(o->max_iter >= 1, FV3D_ERR_INVALID_ARG, "max_iter must be >= 1");
+  fv3d_status st = check_ready(ctx);
+  if (st != FV3D_OK) return st;
+  if (!ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "no state set");
+  CK(cudaSetDevice(ctx->cfg.device));
+  // steady runs have no end time (init_timedisc sets t_end = BC_DMAX)
+  const double t_end = o->is_transient ? o->t_end : DBL_MAX;
+  double t = o->t_start, dt = 0.0;
+  double res[5] = {0, 0, 0, 0, 0};
+  int iter = 0, reason = 0, n_inner = 0;
+  bool finalize = false;
+  const bool dev_dt = !o->implicit && o->cfl > 0.0;
+  cudaGraphExec_t exec = nullptr;
+  if (!o->implicit) {
+    if ((st = step_graph(ctx, o->scheme, o->cfl, true, &exec)) != FV3D_OK) return st;
+    DevScalars h0{};
+    h0.t = t;
+    CK(cudaMemcpyAsync(ctx->d_sc.p, &h0, sizeof(h0), cudaMemcpyHostToDevice, ctx->stream));
+    if (dev_dt) {  // first dt from the initial state; later ones from each step's last stage
+      if ((st = reduce_timestep(ctx, false)) != FV3D_OK) return st;
+      k_set_dt<<<1, 1, 0, ctx->stream>>>(ctx->d_sc.p, ctx->d_bits.p, o->cfl, 0.0);
+      CK(cudaGetLastError());
+    }
+  }
+  const int nb = nblk(ctx->nc);
+  DevScalars hs{};
+  while (true) {
+    // time step: the device's (fused CFL) or calc_ns_timestep's / the
+    // convective formula's from the current state
+    if (dev_dt) {
+      CK(cudaMemcpyAsync(&hs, ctx->d_sc.p, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+      if (hs.status & 1) return ctx->fail(FV3D_ERR_NONFINITE, "non-finite state or time step at iteration %d", iter);
+      dt = hs.dt;
+    } else {
+      if ((st = fv3d_timestep(handle, o->cfl, &dt)) != FV3D_OK) return st;
+    }
+    if (!(dt > 0.0) || std::isinf(dt))
+      return ctx->fail(FV3D_ERR_NONFINITE, "time step %g at iteration %d", dt, iter);
+    bool dt_changed = !dev_dt;
+    if (t + dt > t_end) {
+      dt = t_end - t;
+      finalize = true;
+      dt_changed = true;
+      reason = 0;
+    }
+    if (!o->implicit) {
+      if (dt_changed)
+        CK(cudaMemcpyAsync(reinterpret_cast<char*>(ctx->d_sc.p) + offsetof(DevScalars, dt), &dt, sizeof(double),
+                           cudaMemcpyHostToDevice, ctx->stream));
+      CK(cudaGraphLaunch(exec, ctx->stream));
+      ctx->residual_valid = true;  // the last stage stored its time derivative
+    } else {
+      if (!ctx->implicit) ctx->implicit = new Implicit();
+      fv3d_newton_opts no{o->scheme, o->max_iter_inner, o->is_transient};
+      fv3d_newton_stats ns{};
+      if ((st = ctx->implicit->step_newton(*ctx, no, iter, t, dt, &ns)) != FV3D_OK) return st;
+      n_inner = ns.n_inner;
+    }
+    // calc_global_residual(dt) of the step's time derivative
+    k_residual_partial<<<nb, 256, 0, ctx->stream>>>(ctx->nc, ctx->d_dphi.p, ctx->d_vol.p, ctx->d_part.p);
+    k_residual_final<<<1, 256, 0, ctx->stream>>>(nb, ctx->d_part.p, dt / ctx->vol_total, ctx->d_part.p + 5 * (size_t)nb);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(res, ctx->d_part.p + 5 * (size_t)nb, sizeof(res), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (int j = 0; j < 5; ++j)
+      if (!std::isfinite(res[j])) return ctx->fail(FV3D_ERR_NONFINITE, "non-finite residual at iteration %d", iter);
+    t = t + dt;
+    iter = iter + 1;
+    double rmax = res[0];
+    for (int j = 1; j < 5; ++j) rmax = std::max(rmax, res[j]);
+    if (!o->is_transient && rmax < o->abort_residual) {
+      finalize = true;
+      reason = 1;
+    }
+    if (iter >= o->max_iter && !finalize) {
+      finalize = true;
+      reason = 2;
+    }
+    if (o->on_iteration) o->on_iteration(o->user, iter, t, dt, res, n_inner);
+    if (finalize) break;
+  }
+  if (!o->implicit) {
+    CK(cudaMemcpyAsync(&hs, ctx->d_sc.p, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (hs.status & kStatusStageTimeout)
+      return ctx->fail(FV3D_ERR_TIMEOUT, "gradient pass: a tile's staged copies did not arrive within 0.5 s");
+    if (hs.status & 1) return ctx->fail(FV3D_ERR_NONFINITE, "non-finite state at iteration %d", iter);
+  }
+  if (stats) {
+    stats->iter = iter;
+    stats->t = t;
+    stats->dt = dt;
+    for (int j = 0; j < 5; ++j) stats->res[j] = res[j];
+    stats->stop_reason = reason;
+  }
   return FV3D_OK;
 }

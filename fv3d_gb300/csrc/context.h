@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <map>
+#include <tuple>
 #include <string>
 #include <vector>
 
@@ -73,7 +74,7 @@ struct Ctx {
   DevBuf<DevScalars> d_sc;
   DevBuf<unsigned long long> d_bits;
 
-  std::map<std::pair<int, double>, cudaGraphExec_t> graphs;
+  std::map<std::tuple<int, double, int>, cudaGraphExec_t> graphs;  // (scheme, cfl, store_r)
   Implicit* implicit = nullptr;  // Newton-Krylov work space, created on first use
   Mlp* mlp = nullptr;            // learned preconditioner, created on first use
 

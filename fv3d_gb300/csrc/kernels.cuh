@@ -320,6 +320,8 @@ struct StageCoef {
   double c0, c1;      // SSP combination
   int first;          // first stage of the step
   int last;           // last stage of the step
+  int store_r;        // also store this stage's time derivative in dphi (the
+                      // reference's dphi after a step: that of the last stage)
 };
 
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
@@ -360,10 +362,11 @@ __global__ void __launch_bounds__(256) k_gather_update(const __grid_constant__ K
 #pragma unroll
       for (int j = 0; j < 5; ++j) r[j] = (double)(-s[j].value() * rv);
     }
-    if (MODE == 0) {
+    if (MODE == 0 || co.store_r) {
 #pragma unroll
       for (int j = 0; j < 5; ++j) a.dphi[(size_t)j * a.nc + c] = r[j];
-    } else {
+    }
+    if (MODE != 0) {
       const double dt = a.sc->dt;
       double u[5], uold[5];
 #pragma unroll

@@ -499,10 +499,11 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
     float rr[5];
 #pragma unroll
     for (int j = 0; j < 5; ++j) rr[j] = -s[j].value() * rv;
-    if (MODE == 0) {
+    if (MODE == 0 || co.store_r) {
 #pragma unroll
       for (int j = 0; j < 5; ++j) a.dphi[(size_t)j * a.nc + c] = (double)rr[j];
-    } else {
+    }
+    if (MODE != 0) {
       const double dt = a.sc->dt;
       float du[5];
       if (MODE == 1) {

@@ -238,6 +238,38 @@ typedef struct {
 fv3d_status fv3d_step_newton(fv3d_ctx *ctx, const fv3d_newton_opts *opts, int iter, double t,
                              double dt, fv3d_newton_stats *stats);
 
+/* ---- time loop ----------------------------------------------------------------- */
+/* timedisc (timedisc.c:134-222) with init_timedisc's options (timedisc.c:45-66):
+ * each iteration takes dt (cfl > 0: the convective CFL step, for explicit
+ * schemes computed on the device inside the previous step as the reference
+ * computes it on its stage-input primitives; cfl <= 0: calc_ns_timestep as
+ * written), clips it to t_end, takes one explicit step (one CUDA graph) or
+ * one fv3d_step_newton step, evaluates calc_global_residual(dt) of the step's
+ * time derivative, and stops at t_end (transient), when the largest residual
+ * falls below abort_residual (steady) or after max_iter iterations.
+ * on_iteration (may be NULL) receives what print_residual prints. */
+typedef void (*fv3d_iteration_fn)(void *user, int iter, double t, double dt, const double res[5],
+                                  int n_inner);
+typedef struct {
+    int implicit;           /* 0: explicit (timestep_lserkw2 / SSP-RK3), 1: implicit (timestep_newton) */
+    int scheme;             /* explicit: FV3D_RK_*, FV3D_SSP_RK3; implicit: a fv3d_newton_scheme value */
+    int max_iter;
+    int is_transient;
+    double abort_residual;
+    double t_start, t_end;
+    double cfl;             /* see above */
+    int max_iter_inner;     /* implicit */
+    fv3d_iteration_fn on_iteration;
+    void *user;
+} fv3d_timedisc_opts;
+typedef struct {
+    int iter;               /* iterations taken */
+    double t, dt;           /* final time, last step */
+    double res[5];          /* last calc_global_residual */
+    int stop_reason;        /* 0: t_end, 1: abort_residual, 2: max_iter */
+} fv3d_timedisc_stats;
+fv3d_status fv3d_timedisc(fv3d_ctx *ctx, const fv3d_timedisc_opts *opts, fv3d_timedisc_stats *stats);
+
 /* ---- learned preconditioner (per-cell MLP 36-64-64-64-5, GELU) -------------------- */
 /* BF16 weights / FP32 accumulation on tensor cores, trained on (residual,
  * Newton-correction) pairs that the plain implicit solver harvests; used only

@@ -8,6 +8,7 @@
 #include <cstdio>
 #include <cfloat>
 #include <cstddef>
+#include <cstdint>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -52,6 +53,84 @@ __global__ void k_import(int nc, const int* __restrict__ perm, const double* __r
 }
 
 // SoA [m][n] (renumbered) -> reference AoS [n][m]; with prims: [n][10]
+// the same import reading the caller's pinned host rows directly: each CTA
+// copies its 128 rows (640 doubles, contiguous) with 16-byte loads over the
+// host link into shared memory, then scatters them into the renumbered device
+// arrays (the host buffer must be 16-byte aligned; checked by the caller)
+constexpr int kIoRows = 128;
+__global__ void __launch_bounds__(kIoRows) k_import_host(int nc, const int* __restrict__ iperm,
+                                                         const double* __restrict__ in, double* __restrict__ U,
+                                                         float* __restrict__ Uf, float* __restrict__ UfN,
+                                                         double km1, double R) {
+  __shared__ __align__(16) double sm[kIoRows * 5];
+  const size_t i0 = (size_t)blockIdx.x * kIoRows;
+  const int cnt = (int)min((size_t)kIoRows, (size_t)nc - i0);
+  const int nd = cnt * 5;
+  const double2* src = reinterpret_cast<const double2*>(in + 5 * i0);
+  for (int k = threadIdx.x; k < nd / 2; k += kIoRows) reinterpret_cast<double2*>(sm)[k] = src[k];
+  if ((nd & 1) && threadIdx.x == 0) sm[nd - 1] = in[5 * i0 + nd - 1];
+  __syncthreads();
+  if ((int)threadIdx.x >= cnt) return;
+  const int c = iperm[i0 + threadIdx.x];
+  double u[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) { u[j] = sm[5 * threadIdx.x + j]; U[(size_t)j * nc + c] = u[j]; }
+  if (Uf != nullptr) {
+    float rho = (float)u[0], mx = (float)u[1], my = (float)u[2], mz = (float)u[3];
+    float ke = 0.5f * (mx * (mx / rho) + my * (my / rho) + mz * (mz / rho));
+    float p = fmaxf(1.00E-10f, (float)(km1 * (u[4] - (double)ke)));
+    float T = p / (rho * (float)R);
+    float4* d = reinterpret_cast<float4*>(Uf) + 2 * (size_t)c;
+    d[0] = make_float4(rho, mx, my, mz);
+    d[1] = make_float4((float)u[4], p, T, 0.f);
+    float4* b = reinterpret_cast<float4*>(UfN) + 2 * (size_t)c;
+    b[0] = d[0];
+    b[1] = d[1];
+  }
+}
+
+// export of the 5 conserved variables straight into the caller's pinned
+// host rows: each CTA gathers its 128 rows into shared memory and writes
+// them with 16-byte stores over the host link (16-byte aligned buffer)
+__global__ void __launch_bounds__(kIoRows) k_export_host(int nc, const int* __restrict__ iperm,
+                                                         const double* __restrict__ S, double* __restrict__ out) {
+  __shared__ __align__(16) double sm[kIoRows * 5];
+  const size_t i0 = (size_t)blockIdx.x * kIoRows;
+  const int cnt = (int)min((size_t)kIoRows, (size_t)nc - i0);
+  if ((int)threadIdx.x < cnt) {
+    const int c = iperm[i0 + threadIdx.x];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) sm[5 * threadIdx.x + j] = S[(size_t)j * nc + c];
+  }
+  __syncthreads();
+  const int nd = cnt * 5;
+  double2* dst = reinterpret_cast<double2*>(out + 5 * i0);
+  for (int k = threadIdx.x; k < nd / 2; k += kIoRows) dst[k] = reinterpret_cast<const double2*>(sm)[k];
+  if ((nd & 1) && threadIdx.x == 0) out[5 * i0 + nd - 1] = sm[nd - 1];
+}
+
+// the convective time-step bound min V / sum_d (|u_d| + c) dx_d of the FP32
+// state records (mixed path: the precision of its fused per-step bound)
+__global__ void k_timestep_f32(int nc, const float* __restrict__ Uf, const double* __restrict__ vol,
+                               const double* __restrict__ dx, float kappa, unsigned long long* conv_bits) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long bc = 0x7ff0000000000000ull;
+  if (c < nc) {
+    const float4* r = reinterpret_cast<const float4*>(Uf) + 2 * (size_t)c;
+    const float4 a = r[0], b = r[1];
+    const float ir = 1.f / a.x;
+    const float u = a.y * ir, v = a.z * ir, w = a.w * ir;
+    const float cs = sqrtf(kappa * b.y * ir);
+    const double* d = dx + 3 * (size_t)c;
+    const float ds = (fabsf(u) + cs) * (float)d[0] + (fabsf(v) + cs) * (float)d[1] + (fabsf(w) + cs) * (float)d[2];
+    const double lc = (double)((float)vol[c] / ds);
+    if (lc > 0.0) bc = (unsigned long long)__double_as_longlong(lc);
+    if (!(lc == lc)) bc = 0x7ff8000000000000ull;
+  }
+  bc = warp_min_u64(bc);
+  if ((threadIdx.x & 31) == 0) atomicMin(conv_bits, bc);
+}
+
 __global__ void k_export(int nc, int m, const int* __restrict__ perm, const double* __restrict__ S,
                          double* __restrict__ out, int with_prims, double km1, double R) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -423,16 +502,36 @@ static fv3d_status check_ready(Ctx* ctx) {
   return FV3D_OK;
 }
 
+// the device address of a caller buffer in page-locked host memory
+// (cudaHostAlloc / cudaHostRegister), or null for pageable memory
+static const double* pinned_device_view(const double* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();  // clear: an unknown pointer is pageable memory
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || at.devicePointer == nullptr) return nullptr;
+  if (reinterpret_cast<uintptr_t>(at.devicePointer) % 16 != 0) return nullptr;  // the kernels use 16-byte accesses
+  return static_cast<const double*>(at.devicePointer);
+}
+
 extern "C" fv3d_status fv3d_set_state(fv3d_ctx* handle, const double* u) {
   if (handle == nullptr || u == nullptr) return FV3D_ERR_INVALID_ARG;
   Ctx* ctx = reinterpret_cast<Ctx*>(handle);
   if (!ctx->mesh_ready) return ctx->fail(FV3D_ERR_STATE, "no mesh loaded");
   CK(cudaSetDevice(ctx->cfg.device));
-  CK(cudaMemcpyAsync(ctx->d_stage.p, u, sizeof(double) * 5 * (size_t)ctx->nc, cudaMemcpyHostToDevice,
-                     ctx->stream));
-  k_import<<<nblk(ctx->nc), 256, 0, ctx->stream>>>(ctx->nc, ctx->d_perm.p, ctx->d_stage.p, ctx->d_U.p,
-                                                  ctx->d_Uf.p, ctx->d_UfN.p, ctx->phys.km1,
-                                                  ctx->cfg.R_mix);
+  const double* hdev = pinned_device_view(u);
+  if (hdev != nullptr) {
+    // pinned caller memory: one kernel reads it over the host link
+    k_import_host<<<(ctx->nc + kIoRows - 1) / kIoRows, kIoRows, 0, ctx->stream>>>(
+        ctx->nc, ctx->d_iperm.p, hdev, ctx->d_U.p, ctx->d_Uf.p, ctx->d_UfN.p, ctx->phys.km1, ctx->cfg.R_mix);
+  } else {
+    CK(cudaMemcpyAsync(ctx->d_stage.p, u, sizeof(double) * 5 * (size_t)ctx->nc, cudaMemcpyHostToDevice,
+                       ctx->stream));
+    k_import<<<nblk(ctx->nc), 256, 0, ctx->stream>>>(ctx->nc, ctx->d_perm.p, ctx->d_stage.p, ctx->d_U.p,
+                                                    ctx->d_Uf.p, ctx->d_UfN.p, ctx->phys.km1,
+                                                    ctx->cfg.R_mix);
+  }
   CK(cudaGetLastError());
   ctx->state_ready = true;
   return FV3D_OK;
@@ -440,6 +539,15 @@ extern "C" fv3d_status fv3d_set_state(fv3d_ctx* handle, const double* u) {
 
 static fv3d_status export_soa(Ctx* ctx, const double* src, int m, int with_prims, double* out) {
   const int w = with_prims ? 10 : m;
+  double* hdev = (with_prims || m != 5) ? nullptr : const_cast<double*>(pinned_device_view(out));
+  if (hdev != nullptr) {
+    // pinned caller memory: one kernel writes it over the host link
+    k_export_host<<<(ctx->nc + kIoRows - 1) / kIoRows, kIoRows, 0, ctx->stream>>>(ctx->nc, ctx->d_iperm.p, src,
+                                                                                  hdev);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+    return FV3D_OK;
+  }
   k_export<<<nblk(ctx->nc), 256, 0, ctx->stream>>>(ctx->nc, m, ctx->d_perm.p, src, ctx->d_stage.p,
                                                   with_prims, ctx->phys.km1, ctx->cfg.R_mix);
   CK(cudaGetLastError());
@@ -494,6 +602,18 @@ static fv3d_status reduce_timestep(Ctx* ctx, bool with_visc) {
   (void)with_visc;
   return FV3D_OK;
 }
+
+// the initial convective bound of an explicit run: FP32 records on the mixed
+// path (as its fused per-step bound), FP64 state otherwise
+static fv3d_status reduce_step_bound(Ctx* ctx) {
+  if (ctx->fp64()) return reduce_timestep(ctx, false);
+  CK(cudaMemsetAsync(ctx->d_bits.p, 0xff, 2 * sizeof(unsigned long long), ctx->stream));
+  k_timestep_f32<<<nblk(ctx->nc), 256, 0, ctx->stream>>>(ctx->nc, ctx->d_Uf.p, ctx->d_vol.p, ctx->d_dx.p,
+                                                        (float)ctx->cfg.kappa, ctx->d_bits.p);
+  CK(cudaGetLastError());
+  return FV3D_OK;
+}
+
 
 extern "C" fv3d_status fv3d_timestep(fv3d_ctx* handle, double cfl, double* dt) {
   if (handle == nullptr || dt == nullptr) return FV3D_ERR_INVALID_ARG;
@@ -598,7 +718,7 @@ extern "C" fv3d_status fv3d_step_explicit(fv3d_ctx* handle, int scheme, int n_st
   // initial dt from the current state (timedisc.c:163-165 at the first step)
   CK(cudaMemsetAsync(ctx->d_sc.p, 0, sizeof(DevScalars), ctx->stream));
   if (cfl > 0.0) {
-    st = reduce_timestep(ctx, false);
+    st = reduce_step_bound(ctx);
     if (st != FV3D_OK) return st;
   }
   k_set_dt<<<1, 1, 0, ctx->stream>>>(ctx->d_sc.p, ctx->d_bits.p, cfl, dt_fixed);
@@ -761,7 +881,7 @@ extern "C" fv3d_status fv3d_timedisc(fv3d_ctx* handle, const fv3d_timedisc_opts*
     h0.t = t;
     CK(cudaMemcpyAsync(ctx->d_sc.p, &h0, sizeof(h0), cudaMemcpyHostToDevice, ctx->stream));
     if (dev_dt) {  // first dt from the initial state; later ones from each step's last stage
-      if ((st = reduce_timestep(ctx, false)) != FV3D_OK) return st;
+      if ((st = reduce_step_bound(ctx)) != FV3D_OK) return st;
       k_set_dt<<<1, 1, 0, ctx->stream>>>(ctx->d_sc.p, ctx->d_bits.p, o->cfl, 0.0);
       CK(cudaGetLastError());
     }

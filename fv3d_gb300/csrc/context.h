@@ -60,7 +60,7 @@ struct Ctx {
   std::vector<double> h_lam, h_lsq, h_vol, h_dx;
 
   // device mesh
-  DevBuf<int> d_perm, d_fc0, d_fc1, d_fregion, d_cface, d_cnbr;
+  DevBuf<int> d_iperm, d_perm, d_fc0, d_fc1, d_fregion, d_cface, d_cnbr;
   DevBuf<char> d_geo, d_lam, d_lsq, d_rvol;  // FP64-path geometry (double)
   DevBuf<double> d_vol, d_dx;
   // device solution data
@@ -84,7 +84,7 @@ struct Ctx {
   fv3d_status cuda(cudaError_t e, const char* what);
   void release_graphs();
   void free_device() {
-    d_cnbr.release(); d_perm.release(); d_fc0.release(); d_fc1.release(); d_fregion.release(); d_cface.release();
+    d_cnbr.release(); d_perm.release(); d_iperm.release(); d_fc0.release(); d_fc1.release(); d_fregion.release(); d_cface.release();
     d_geo.release(); d_lam.release(); d_lsq.release(); d_rvol.release(); d_vol.release(); d_dx.release();
     d_U.release(); d_K.release(); d_U0.release(); d_dphi.release(); d_stage.release(); d_part.release();
     d_Uf.release(); d_rec.release(); d_FA.release(); d_sc.release(); d_bits.release();

@@ -548,6 +548,17 @@ fv3d_status Implicit::setup(Ctx& ctx, int m) {
   return FV3D_OK;
 }
 
+// the FP32 base and stage records of the state U, when the mixed arrays exist
+// (the Jacobian-vector products overwrite the stage records)
+static fv3d_status refresh_records(Ctx& ctx) {
+  if (ctx.d_Uf.p == nullptr) return FV3D_OK;
+  k_make_record<<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, ctx.d_U.p, ctx.d_Uf.p, ctx.phys.f32[1],
+                                                        ctx.phys.f32[4]);
+  ICK(cudaMemcpyAsync(ctx.d_UfN.p, ctx.d_Uf.p, sizeof(float) * 8 * (size_t)ctx.nc, cudaMemcpyDeviceToDevice,
+                      ctx.stream));
+  return FV3D_OK;
+}
+
 // R(state) in FP64 into `out`
 static fv3d_status residual64(Ctx& ctx, const double* state, double* out) {
   KArgs<double> a = ctx.args<double>();
@@ -836,6 +847,7 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
       if (attempt == 5) return ctx.fail(FV3D_ERR_NOT_CONVERGED, "Newton update not admissible at step %d", newton);
     }
   }
+  if ((st = refresh_records(ctx)) != FV3D_OK) return st;
   ICK(cudaStreamSynchronize(ctx.stream));
   const double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   if (stats != nullptr) {
@@ -928,6 +940,7 @@ fv3d_status Implicit::step_newton(Ctx& ctx, const fv3d_newton_opts& o, int iter,
     if (!o.is_transient) break;
   }
   ICK(cudaMemcpyAsync(ctx.d_dphi.p, dYdt.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx.stream));
+  if ((st = refresh_records(ctx)) != FV3D_OK) return st;
   ICK(cudaStreamSynchronize(ctx.stream));
   ctx.residual_valid = true;
   if (stats) {

@@ -305,6 +305,7 @@ fv3d_status upload_mesh(Ctx& ctx) {
   const int nc = ctx.nc, nf = ctx.nf;
   ctx.ncp = (nc + kTile - 1) / kTile * kTile;
   UP(ctx.d_perm, ctx.perm.data(), (size_t)nc);
+  UP(ctx.d_iperm, ctx.iperm.data(), (size_t)nc);
   UP(ctx.d_fc0, ctx.h_fc0.data(), (size_t)nf);
   UP(ctx.d_fc1, ctx.h_fc1.data(), (size_t)nf);
   if (ctx.nb > 0) UP(ctx.d_fregion, ctx.h_fregion.data(), (size_t)ctx.nb);

@@ -458,7 +458,9 @@ __device__ __forceinline__ void mx_make_state(float rho, float mx, float my, flo
 
 // MODE 0: residual only; 1: low-storage RK stage; 2: SSP-RK3 stage.
 // co.first / co.last mark the step's first and last stage.
-template <int MCF, int MODE, bool DT, bool VISC>
+// STORE: also store the stage's time derivative in dphi (co.store_r; a
+// template flag: a run-time test of it costs the hot instantiations 2 %)
+template <int MCF, int MODE, bool DT, bool VISC, bool STORE = false>
 __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(const __grid_constant__ MxArgs a,
                                                         StageCoef co) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -499,7 +501,7 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
     float rr[5];
 #pragma unroll
     for (int j = 0; j < 5; ++j) rr[j] = -s[j].value() * rv;
-    if (MODE == 0 || co.store_r) {
+    if (MODE == 0 || STORE) {
 #pragma unroll
       for (int j = 0; j < 5; ++j) a.dphi[(size_t)j * a.nc + c] = (double)rr[j];
     }

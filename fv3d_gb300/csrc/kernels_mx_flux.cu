@@ -7,7 +7,11 @@ namespace fv3d {
 template <int MCF>
 static void flux_mcf(const MxArgs& a, const Disc& d, int mode, bool dt, const StageCoef& co,
                      cudaStream_t s, int B) {
-#define MX_FU(M, D, V) k_mx_flux_update<MCF, M, D, V><<<B, 256, 0, s>>>(a, co)
+#define MX_FU(M, D, V)                                                   \
+  do {                                                                  \
+    if (M != 0 && co.store_r) k_mx_flux_update<MCF, M, D, V, true><<<B, 256, 0, s>>>(a, co); \
+    else k_mx_flux_update<MCF, M, D, V><<<B, 256, 0, s>>>(a, co);        \
+  } while (0)
   if (mode == 0) { if (d.viscous) MX_FU(0, false, true); else MX_FU(0, false, false); }
   else if (mode == 1) {
     if (dt) { if (d.viscous) MX_FU(1, true, true); else MX_FU(1, true, false); }

@@ -254,6 +254,22 @@ def run_channel(args):
     print(json.dumps(line))
 
 
+def max_over_ranks(ms, dist):
+    """The slowest rank's timed-region length (the job's time)."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_value(cells, stages, ms, world):
+    """Mcell-updates/s per RK stage of all ranks together (each rank a
+    replica of the same workload)."""
+    return cells * stages / (ms * 1e-3) / 1e6 * world
+
+
 def main():
     args = parse()
     if args.case == "channel":
@@ -282,14 +298,11 @@ def main():
         dist.barrier()
     with ClockSampler(local) as clk:
         st = s.step_explicit(scheme, args.steps, cfl=0.5)   # CUDA events around the graph replays
-    ms = st["elapsed_ms"]
     if dist:
-        import torch
-        t = torch.tensor([ms], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        dist.barrier()
+    ms = max_over_ranks(st["elapsed_ms"], dist)
     n_stages = args.steps * nst
-    value = case.mesh.n_cells * n_stages / (ms * 1e-3) / 1e6 * world
+    value = whole_job_value(case.mesh.n_cells, n_stages, ms, world)
     # per-kernel durations (CUDA events around each launch on the context stream)
     kms = s.profile_stage(20, 0.5)
     model = byte_model(case, args.precision)

@@ -51,11 +51,7 @@ namespace fv3d {
 #ifndef FV3D_TMA_MINBLOCKS
 #define FV3D_TMA_MINBLOCKS 4
 #endif
-// the staged gradient pass as a persistent kernel with two tile buffers
-// (k_mx_sides_tma2): the next tile's copies fly while a tile is computed
-#ifndef FV3D_SIDES_PERSIST
-#define FV3D_SIDES_PERSIST 1
-#endif
+
 #ifndef FV3D_FLUX_MINBLOCKS
 #define FV3D_FLUX_MINBLOCKS 1
 #endif

@@ -9,16 +9,38 @@ namespace fv3d {
 #if FV3D_SIDES_TMA
 static int g_sm_count = 0;  // multiprocessors of the device, read in setup_mx_sides
 
+// the persistent two-buffer form while both buffers fit in this many bytes
+// (4 CTAs per SM); larger tiles (6 or 8 face slots with least squares, 8
+// with Green-Gauss) run one tile per CTA with one buffer, so that 4 CTAs
+// still fit on an SM
+#ifndef FV3D_PERSIST_MAX_SMEM
+#define FV3D_PERSIST_MAX_SMEM (64 * 1024)
+#endif
+template <int MCF, int G>
+constexpr bool sides_persistent() {
+  return 2 * sides_buf_stride<MCF, G>() <= FV3D_PERSIST_MAX_SMEM;
+}
+
 // second-order passes: the tile-staged kernel
 template <int MCF, int G, bool L, bool M, bool V>
 static void launch_staged(const MxArgs& a, cudaStream_t s) {
-#if FV3D_SIDES_PERSIST
-  const int ntiles = a.ncp / kTile;
-  const int grid = std::min(ntiles, std::max(1, g_sm_count) * 4);
-  k_mx_sides_tma2<MCF, G, L, M, V><<<grid, kTile, 2 * sides_buf_stride<MCF, G>(), s>>>(a);
-#else
-  k_mx_sides_tma<MCF, G, L, M, V><<<a.ncp / kTile, kTile, SidesTile<MCF, G>::total, s>>>(a);
-#endif
+  if constexpr (sides_persistent<MCF, G>()) {
+    const int ntiles = a.ncp / kTile;
+    const int grid = std::min(ntiles, std::max(1, g_sm_count) * 4);
+    k_mx_sides_tma2<MCF, G, L, M, V><<<grid, kTile, 2 * sides_buf_stride<MCF, G>(), s>>>(a);
+  } else {
+    k_mx_sides_tma<MCF, G, L, M, V><<<a.ncp / kTile, kTile, SidesTile<MCF, G>::total, s>>>(a);
+  }
+}
+
+template <int MCF, int G, bool L, bool M, bool V>
+static cudaError_t staged_attr() {
+  if constexpr (sides_persistent<MCF, G>())
+    return cudaFuncSetAttribute(k_mx_sides_tma2<MCF, G, L, M, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                2 * sides_buf_stride<MCF, G>());
+  else
+    return cudaFuncSetAttribute(k_mx_sides_tma<MCF, G, L, M, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                SidesTile<MCF, G>::total);
 }
 #define MX_SIDES(G, L, M, V)                                              \
   do {                                                                   \
@@ -54,17 +76,8 @@ cudaError_t setup_mx_sides() {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_sm_count, cudaDevAttrMultiProcessorCount, dev);
-#if FV3D_SIDES_PERSIST
-#define MX_ATTR(MCF, G, L, M, V)                                                                    \
-  if (e == cudaSuccess)                                                                            \
-    e = cudaFuncSetAttribute(k_mx_sides_tma2<MCF, G, L, M, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             2 * sides_buf_stride<MCF, G>());
-#else
-#define MX_ATTR(MCF, G, L, M, V)                                                                    \
-  if (e == cudaSuccess)                                                                            \
-    e = cudaFuncSetAttribute(k_mx_sides_tma<MCF, G, L, M, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                             SidesTile<MCF, G>::total);
-#endif
+#define MX_ATTR(MCF, G, L, M, V) \
+  if (e == cudaSuccess) e = staged_attr<MCF, G, L, M, V>();
 #define MX_ATTR_ALL(MCF, G)                                                                          \
   MX_ATTR(MCF, G, false, false, false) MX_ATTR(MCF, G, false, false, true)                           \
   MX_ATTR(MCF, G, true, false, false) MX_ATTR(MCF, G, true, false, true)                             \

@@ -66,6 +66,14 @@ struct MlpAct {
   float y[MLP_TILE * 8];
 };
 
+// inference: no pre-activations kept
+struct MlpActInf {
+  bf16 x[MLP_TILE * LD_X];
+  bf16 a1[MLP_TILE * LD_H], a2[MLP_TILE * LD_H], a3[MLP_TILE * LD_H];
+  float y[MLP_TILE * 8];
+  float vn[MLP_TILE];
+};
+
 struct MlpTrainSmem {
   MlpW w;
   MlpBwdW wt;
@@ -130,15 +138,20 @@ __device__ __forceinline__ void warp_gemm(const bf16* A, int lda, const bf16* B,
   }
 }
 
-// forward of the warp's 16 rows; keeps pre-activations when h != nullptr
-__device__ void mlp_forward_warp(const MlpW& w, MlpAct& s, int r0, bool keep) {
+// forward of the warp's 16 rows; keeps the pre-activations (training) when
+// the activation struct has them
+__device__ __forceinline__ float* pre_act(MlpAct& s, int l) { return l == 1 ? s.h1 : (l == 2 ? s.h2 : s.h3); }
+__device__ __forceinline__ float* pre_act(MlpActInf&, int) { return nullptr; }
+
+template <class Act>
+__device__ void mlp_forward_warp(const MlpW& w, Act& s, int r0, bool keep) {
   const bf16* x = s.x + r0 * LD_X;
   bf16* a1 = s.a1 + r0 * LD_H;
   bf16* a2 = s.a2 + r0 * LD_H;
   bf16* a3 = s.a3 + r0 * LD_H;
-  float* h1 = s.h1 + r0 * LDF;
-  float* h2 = s.h2 + r0 * LDF;
-  float* h3 = s.h3 + r0 * LDF;
+  float* h1 = keep ? pre_act(s, 1) + r0 * LDF : nullptr;
+  float* h2 = keep ? pre_act(s, 2) + r0 * LDF : nullptr;
+  float* h3 = keep ? pre_act(s, 3) + r0 * LDF : nullptr;
   warp_gemm(x, LD_X, w.W0, LD_X, MLP_INP, MLP_H, [&](int r, int c, float v) {
     v += w.b0[c];
     if (keep) h1[r * LDF + c] = v;
@@ -299,24 +312,29 @@ __global__ void k_adam(float* __restrict__ P, const float* __restrict__ g, float
 }
 
 // forward over host-provided samples (tests): X [n][36] -> Y [n][5]
+// inference kernels: persistent CTAs (weights converted into shared memory
+// once per CTA), one 64-sample tile per iteration, 4 warps x 16 rows
 __global__ void __launch_bounds__(128) k_mlp_forward(const float* __restrict__ P, const float* __restrict__ X,
                                                      int n, float* __restrict__ Y) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MlpW& W = *reinterpret_cast<MlpW*>(smem_raw);
-  MlpAct& A = *reinterpret_cast<MlpAct*>(smem_raw + sizeof(MlpW));
-  const int base = blockIdx.x * MLP_TILE;
+  MlpActInf& A = *reinterpret_cast<MlpActInf*>(smem_raw + sizeof(MlpW));
   load_weights(P, W, nullptr);
-  for (int i = threadIdx.x; i < MLP_TILE * LD_X; i += blockDim.x) {
-    const int r = i / LD_X, k = i % LD_X;
-    A.x[i] = __float2bfloat16((base + r < n && k < MLP_IN) ? X[(size_t)(base + r) * MLP_IN + k] : 0.f);
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5;
-  mlp_forward_warp(W, A, warp * 16, false);
-  __syncthreads();
-  for (int i = threadIdx.x; i < MLP_TILE * MLP_OUT; i += blockDim.x) {
-    const int r = i / MLP_OUT, o = i % MLP_OUT;
-    if (base + r < n) Y[(size_t)(base + r) * MLP_OUT + o] = A.y[r * 8 + o];
+  const int ntiles = (n + MLP_TILE - 1) / MLP_TILE;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int base = tile * MLP_TILE;
+    __syncthreads();  // weights loaded / previous tile's outputs read
+    for (int i = threadIdx.x; i < MLP_TILE * LD_X; i += blockDim.x) {
+      const int r = i / LD_X, k = i % LD_X;
+      A.x[i] = __float2bfloat16((base + r < n && k < MLP_IN) ? X[(size_t)(base + r) * MLP_IN + k] : 0.f);
+    }
+    __syncthreads();
+    mlp_forward_warp(W, A, (threadIdx.x >> 5) * 16, false);
+    __syncthreads();
+    for (int i = threadIdx.x; i < MLP_TILE * MLP_OUT; i += blockDim.x) {
+      const int r = i / MLP_OUT, o = i % MLP_OUT;
+      if (base + r < n) Y[(size_t)(base + r) * MLP_OUT + o] = A.y[r * 8 + o];
+    }
   }
 }
 
@@ -329,36 +347,39 @@ __global__ void __launch_bounds__(128) k_mlp_apply(const float* __restrict__ P, 
                                                    T* __restrict__ z) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   MlpW& W = *reinterpret_cast<MlpW*>(smem_raw);
-  MlpAct& A = *reinterpret_cast<MlpAct*>(smem_raw + sizeof(MlpW));
-  __shared__ float vn[MLP_TILE];
-  const int base = blockIdx.x * MLP_TILE;
+  MlpActInf& A = *reinterpret_cast<MlpActInf*>(smem_raw + sizeof(MlpW));
   load_weights(P, W, nullptr);
-  if (threadIdx.x < MLP_TILE) {
-    const int c = base + threadIdx.x;
-    float s = 0.f;
-    if (c < nc)
-      for (int j = 0; j < 5; ++j) {
-        const float x = (float)v[(size_t)j * nc + c];
-        s += x * x;
-      }
-    vn[threadIdx.x] = sqrtf(s);
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < MLP_TILE * LD_X; i += blockDim.x) {
-    const int r = i / LD_X, k = i % LD_X, c = base + r;
-    float x = 0.f;
-    if (c < nc) {
-      if (k < 31) x = feat[(size_t)c * MLP_FEAT + k];
-      else if (k < MLP_IN && vn[r] > 0.f) x = (float)v[(size_t)(k - 31) * nc + c] / vn[r];
+  const int ntiles = (nc + MLP_TILE - 1) / MLP_TILE;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int base = tile * MLP_TILE;
+    __syncthreads();  // weights loaded / previous tile's outputs read
+    if (threadIdx.x < MLP_TILE) {
+      const int c = base + threadIdx.x;
+      float s = 0.f;
+      if (c < nc)
+        for (int j = 0; j < 5; ++j) {
+          const float x = (float)v[(size_t)j * nc + c];
+          s += x * x;
+        }
+      A.vn[threadIdx.x] = sqrtf(s);
     }
-    A.x[i] = __float2bfloat16(x);
-  }
-  __syncthreads();
-  mlp_forward_warp(W, A, (threadIdx.x >> 5) * 16, false);
-  __syncthreads();
-  for (int i = threadIdx.x; i < MLP_TILE * MLP_OUT; i += blockDim.x) {
-    const int r = i / MLP_OUT, o = i % MLP_OUT, c = base + r;
-    if (c < nc) z[(size_t)o * nc + c] = (T)(A.y[r * 8 + o] * vn[r] * feat[(size_t)c * MLP_FEAT + 31]);
+    __syncthreads();
+    for (int i = threadIdx.x; i < MLP_TILE * LD_X; i += blockDim.x) {
+      const int r = i / LD_X, k = i % LD_X, c = base + r;
+      float x = 0.f;
+      if (c < nc) {
+        if (k < 31) x = feat[(size_t)c * MLP_FEAT + k];
+        else if (k < MLP_IN && A.vn[r] > 0.f) x = (float)v[(size_t)(k - 31) * nc + c] / A.vn[r];
+      }
+      A.x[i] = __float2bfloat16(x);
+    }
+    __syncthreads();
+    mlp_forward_warp(W, A, (threadIdx.x >> 5) * 16, false);
+    __syncthreads();
+    for (int i = threadIdx.x; i < MLP_TILE * MLP_OUT; i += blockDim.x) {
+      const int r = i / MLP_OUT, o = i % MLP_OUT, c = base + r;
+      if (c < nc) z[(size_t)o * nc + c] = (T)(A.y[r * 8 + o] * A.vn[r] * feat[(size_t)c * MLP_FEAT + 31]);
+    }
   }
 }
 
@@ -425,7 +446,17 @@ __global__ void __launch_bounds__(256) k_mlp_weight_norm(int count, float* __res
 }
 
 size_t train_smem() { return sizeof(MlpTrainSmem); }
-size_t fwd_smem() { return sizeof(MlpW) + sizeof(MlpAct); }
+size_t fwd_smem() { return sizeof(MlpW) + sizeof(MlpActInf); }
+// persistent inference grids: resident CTAs of the device
+int inference_grid(int ntiles) {
+  static int sms = 0;
+  if (sms == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      sms = 1;
+  }
+  return std::max(1, std::min(ntiles, sms * 3));
+}
 
 }  // namespace
 
@@ -478,7 +509,7 @@ fv3d_status Mlp::forward_host(Ctx& ctx, const float* X, int n, float* Y) {
   MCK(dX.alloc((size_t)n * MLP_IN));
   MCK(dY.alloc((size_t)n * MLP_OUT));
   MCK(cudaMemcpy(dX.p, X, sizeof(float) * n * MLP_IN, cudaMemcpyHostToDevice));
-  k_mlp_forward<<<(n + MLP_TILE - 1) / MLP_TILE, 128, fwd_smem(), ctx.stream>>>(P.p, dX.p, n, dY.p);
+  k_mlp_forward<<<inference_grid((n + MLP_TILE - 1) / MLP_TILE), 128, fwd_smem(), ctx.stream>>>(P.p, dX.p, n, dY.p);
   MCK(cudaGetLastError());
   MCK(cudaStreamSynchronize(ctx.stream));
   MCK(cudaMemcpy(Y, dY.p, sizeof(float) * n * MLP_OUT, cudaMemcpyDeviceToHost));
@@ -575,14 +606,14 @@ fv3d_status Mlp::build_features(Ctx& ctx, const Implicit& im) {
 }
 
 fv3d_status Mlp::apply(Ctx& ctx, const double* vin, double* zout) {
-  k_mlp_apply<double><<<(ctx.nc + MLP_TILE - 1) / MLP_TILE, 128, fwd_smem(), ctx.stream>>>(P.p, ctx.nc, feat.p, vin,
+  k_mlp_apply<double><<<inference_grid((ctx.nc + MLP_TILE - 1) / MLP_TILE), 128, fwd_smem(), ctx.stream>>>(P.p, ctx.nc, feat.p, vin,
                                                                                           zout);
   MCK(cudaGetLastError());
   return FV3D_OK;
 }
 
 fv3d_status Mlp::apply(Ctx& ctx, const float* vin, float* zout) {
-  k_mlp_apply<float><<<(ctx.nc + MLP_TILE - 1) / MLP_TILE, 128, fwd_smem(), ctx.stream>>>(P.p, ctx.nc, feat.p, vin,
+  k_mlp_apply<float><<<inference_grid((ctx.nc + MLP_TILE - 1) / MLP_TILE), 128, fwd_smem(), ctx.stream>>>(P.p, ctx.nc, feat.p, vin,
                                                                                          zout);
   MCK(cudaGetLastError());
   return FV3D_OK;

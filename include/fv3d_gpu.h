@@ -247,7 +247,9 @@ fv3d_status fv3d_step_newton(fv3d_ctx *ctx, const fv3d_newton_opts *opts, int it
  * one fv3d_step_newton step, evaluates calc_global_residual(dt) of the step's
  * time derivative, and stops at t_end (transient), when the largest residual
  * falls below abort_residual (steady) or after max_iter iterations.
- * on_iteration (may be NULL) receives what print_residual prints. */
+ * on_iteration (may be NULL) receives what print_residual prints.  A zero
+ * time step (calc_ns_timestep's inviscid branch, navier_stokes.c:188-192) is
+ * FV3D_ERR_NONFINITE here; the reference loops on without advancing. */
 typedef void (*fv3d_iteration_fn)(void *user, int iter, double t, double dt, const double res[5],
                                   int n_inner);
 typedef struct {

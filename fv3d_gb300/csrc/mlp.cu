@@ -66,14 +66,6 @@ struct MlpAct {
   float y[MLP_TILE * 8];
 };
 
-// inference: no pre-activations kept
-struct MlpActInf {
-  bf16 x[MLP_TILE * LD_X];
-  bf16 a1[MLP_TILE * LD_H], a2[MLP_TILE * LD_H], a3[MLP_TILE * LD_H];
-  float y[MLP_TILE * 8];
-  float vn[MLP_TILE];
-};
-
 struct MlpTrainSmem {
   MlpW w;
   MlpBwdW wt;
@@ -141,7 +133,6 @@ __device__ __forceinline__ void warp_gemm(const bf16* A, int lda, const bf16* B,
 // forward of the warp's 16 rows; keeps the pre-activations (training) when
 // the activation struct has them
 __device__ __forceinline__ float* pre_act(MlpAct& s, int l) { return l == 1 ? s.h1 : (l == 2 ? s.h2 : s.h3); }
-__device__ __forceinline__ float* pre_act(MlpActInf&, int) { return nullptr; }
 
 template <class Act>
 __device__ void mlp_forward_warp(const MlpW& w, Act& s, int r0, bool keep) {
@@ -312,73 +303,162 @@ __global__ void k_adam(float* __restrict__ P, const float* __restrict__ g, float
 }
 
 // forward over host-provided samples (tests): X [n][36] -> Y [n][5]
-// inference kernels: persistent CTAs (weights converted into shared memory
-// once per CTA), one 64-sample tile per iteration, 4 warps x 16 rows
-__global__ void __launch_bounds__(128) k_mlp_forward(const float* __restrict__ P, const float* __restrict__ X,
-                                                     int n, float* __restrict__ Y) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  MlpW& W = *reinterpret_cast<MlpW*>(smem_raw);
-  MlpActInf& A = *reinterpret_cast<MlpActInf*>(smem_raw + sizeof(MlpW));
-  load_weights(P, W, nullptr);
-  const int ntiles = (n + MLP_TILE - 1) / MLP_TILE;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int base = tile * MLP_TILE;
-    __syncthreads();  // weights loaded / previous tile's outputs read
-    for (int i = threadIdx.x; i < MLP_TILE * LD_X; i += blockDim.x) {
-      const int r = i / LD_X, k = i % LD_X;
-      A.x[i] = __float2bfloat16((base + r < n && k < MLP_IN) ? X[(size_t)(base + r) * MLP_IN + k] : 0.f);
+// ---------------------------------------------------------------------------
+// register-resident forward for inference: one warp runs 16 rows through all
+// four layers.  The m16n8k16 accumulator fragment of n-tiles 2q and 2q+1
+// (rows g, g+8; columns 2t, 2t+1 of each) is exactly the A fragment of the
+// next layer's k-chunk q, so activations never leave registers; only the
+// weights (B fragments) come from shared memory.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+// one hidden layer: h = gelu(A W^T + b), K = 16 * KC input columns, 64 outputs
+template <int KC>
+__device__ __forceinline__ void fused_layer(const uint32_t (&a)[KC][4], const bf16* W, int ldw, const float* b,
+                                            uint32_t (&out)[4][4]) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  float h[8][4];
+#pragma unroll
+  for (int nt = 0; nt < 8; ++nt) {
+    float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int kt = 0; kt < KC; ++kt) {
+      const bf16* bp = W + (nt * 8 + g) * ldw + kt * 16 + 2 * t;
+      mma16816(c, a[kt][0], a[kt][1], a[kt][2], a[kt][3], ld2(bp), ld2(bp + 8));
     }
-    __syncthreads();
-    mlp_forward_warp(W, A, (threadIdx.x >> 5) * 16, false);
-    __syncthreads();
-    for (int i = threadIdx.x; i < MLP_TILE * MLP_OUT; i += blockDim.x) {
-      const int r = i / MLP_OUT, o = i % MLP_OUT;
-      if (base + r < n) Y[(size_t)(base + r) * MLP_OUT + o] = A.y[r * 8 + o];
+    const float b0 = b[nt * 8 + 2 * t], b1 = b[nt * 8 + 2 * t + 1];
+    h[nt][0] = gelu(c[0] + b0);
+    h[nt][1] = gelu(c[1] + b1);
+    h[nt][2] = gelu(c[2] + b0);
+    h[nt][3] = gelu(c[3] + b1);
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    out[q][0] = pack_bf16(h[2 * q][0], h[2 * q][1]);
+    out[q][1] = pack_bf16(h[2 * q][2], h[2 * q][3]);
+    out[q][2] = pack_bf16(h[2 * q + 1][0], h[2 * q + 1][1]);
+    out[q][3] = pack_bf16(h[2 * q + 1][2], h[2 * q + 1][3]);
+  }
+}
+
+// x (A fragments of the 48-wide input, 3 k-chunks) -> y: this thread's
+// outputs (row g: y[0], y[1] for outputs 2t, 2t+1; row g + 8: y[2], y[3])
+__device__ __forceinline__ void fused_forward(const MlpW& w, const uint32_t (&x)[3][4], float (&y)[4]) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  uint32_t a1[4][4], a2[4][4], a3[4][4];
+  fused_layer<3>(x, w.W0, LD_X, w.b0, a1);
+  fused_layer<4>(a1, w.W1, LD_H, w.b1, a2);
+  fused_layer<4>(a2, w.W2, LD_H, w.b2, a3);
+  float c[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int kt = 0; kt < 4; ++kt) {
+    const bf16* bp = w.W3 + g * LD_H + kt * 16 + 2 * t;
+    mma16816(c, a3[kt][0], a3[kt][1], a3[kt][2], a3[kt][3], ld2(bp), ld2(bp + 8));
+  }
+  const float b0 = w.b3[2 * t], b1 = w.b3[2 * t + 1];
+  y[0] = c[0] + b0;
+  y[1] = c[1] + b1;
+  y[2] = c[2] + b0;
+  y[3] = c[3] + b1;
+}
+
+// the input fragments of one row pair from a per-row value function x(row, k)
+template <class X>
+__device__ __forceinline__ void input_fragments(X xval, uint32_t (&x)[3][4]) {
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+  for (int kt = 0; kt < 3; ++kt) {
+    const int k0 = kt * 16 + 2 * t;
+    x[kt][0] = pack_bf16(xval(g, k0), xval(g, k0 + 1));
+    x[kt][1] = pack_bf16(xval(g + 8, k0), xval(g + 8, k0 + 1));
+    x[kt][2] = pack_bf16(xval(g, k0 + 8), xval(g, k0 + 9));
+    x[kt][3] = pack_bf16(xval(g + 8, k0 + 8), xval(g + 8, k0 + 9));
+  }
+}
+
+constexpr int kInfWarps = 8;  // warps per inference CTA
+
+// inference kernels: persistent CTAs of kInfWarps warps; the weights are
+// converted into shared memory once per CTA, then every warp takes 16-row
+// groups in turn through the register-resident forward
+__global__ void __launch_bounds__(32 * kInfWarps) k_mlp_forward(const float* __restrict__ P,
+                                                                const float* __restrict__ X, int n,
+                                                                float* __restrict__ Y) {
+  __shared__ __align__(16) MlpW W;
+  load_weights(P, W, nullptr);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int groups = (n + 15) / 16;
+  for (int grp = blockIdx.x * kInfWarps + (threadIdx.x >> 5); grp < groups; grp += gridDim.x * kInfWarps) {
+    const int r0 = grp * 16;
+    uint32_t x[3][4];
+    input_fragments(
+        [&](int r, int k) {
+          return (r0 + r < n && k < MLP_IN) ? X[(size_t)(r0 + r) * MLP_IN + k] : 0.f;
+        },
+        x);
+    float y[4];
+    fused_forward(W, x, y);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int row = r0 + g + 8 * h;
+      if (row >= n) continue;
+      if (2 * t < MLP_OUT) Y[(size_t)row * MLP_OUT + 2 * t] = y[2 * h];
+      if (2 * t + 1 < MLP_OUT) Y[(size_t)row * MLP_OUT + 2 * t + 1] = y[2 * h + 1];
     }
   }
 }
 
-// preconditioner application z = M(v): features of each cell from its
-// block / geometry record and its vector, MLP, rescale
-// (vectors in FP64 or, for the FP32 Krylov basis, FP32)
+// preconditioner application z = M(v) (vectors in FP64 or, for the FP32
+// Krylov basis, FP32): features of each cell from its block / geometry
+// record and its vector, MLP, rescale by |v| / ||D||_F
 template <class T>
-__global__ void __launch_bounds__(128) k_mlp_apply(const float* __restrict__ P, int nc,
-                                                   const float* __restrict__ feat, const T* __restrict__ v,
-                                                   T* __restrict__ z) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  MlpW& W = *reinterpret_cast<MlpW*>(smem_raw);
-  MlpActInf& A = *reinterpret_cast<MlpActInf*>(smem_raw + sizeof(MlpW));
+__global__ void __launch_bounds__(32 * kInfWarps) k_mlp_apply(const float* __restrict__ P, int nc,
+                                                              const float* __restrict__ feat,
+                                                              const T* __restrict__ v, T* __restrict__ z) {
+  __shared__ __align__(16) MlpW W;
   load_weights(P, W, nullptr);
-  const int ntiles = (nc + MLP_TILE - 1) / MLP_TILE;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int base = tile * MLP_TILE;
-    __syncthreads();  // weights loaded / previous tile's outputs read
-    if (threadIdx.x < MLP_TILE) {
-      const int c = base + threadIdx.x;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const int groups = (nc + 15) / 16;
+  for (int grp = blockIdx.x * kInfWarps + (threadIdx.x >> 5); grp < groups; grp += gridDim.x * kInfWarps) {
+    const int r0 = grp * 16;
+    // |v| of this thread's two rows
+    float vn[2], iv[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int c = r0 + g + 8 * h;
       float s = 0.f;
       if (c < nc)
+#pragma unroll
         for (int j = 0; j < 5; ++j) {
-          const float x = (float)v[(size_t)j * nc + c];
-          s += x * x;
+          const float e = (float)v[(size_t)j * nc + c];
+          s += e * e;
         }
-      A.vn[threadIdx.x] = sqrtf(s);
+      vn[h] = sqrtf(s);
+      iv[h] = (vn[h] > 0.f) ? 1.f / vn[h] : 0.f;
     }
-    __syncthreads();
-    for (int i = threadIdx.x; i < MLP_TILE * LD_X; i += blockDim.x) {
-      const int r = i / LD_X, k = i % LD_X, c = base + r;
-      float x = 0.f;
-      if (c < nc) {
-        if (k < 31) x = feat[(size_t)c * MLP_FEAT + k];
-        else if (k < MLP_IN && A.vn[r] > 0.f) x = (float)v[(size_t)(k - 31) * nc + c] / A.vn[r];
-      }
-      A.x[i] = __float2bfloat16(x);
-    }
-    __syncthreads();
-    mlp_forward_warp(W, A, (threadIdx.x >> 5) * 16, false);
-    __syncthreads();
-    for (int i = threadIdx.x; i < MLP_TILE * MLP_OUT; i += blockDim.x) {
-      const int r = i / MLP_OUT, o = i % MLP_OUT, c = base + r;
-      if (c < nc) z[(size_t)o * nc + c] = (T)(A.y[r * 8 + o] * A.vn[r] * feat[(size_t)c * MLP_FEAT + 31]);
+    uint32_t x[3][4];
+    input_fragments(
+        [&](int r, int k) {
+          const int c = r0 + r;
+          if (c >= nc || k >= MLP_IN) return 0.f;
+          if (k < 31) return feat[(size_t)c * MLP_FEAT + k];
+          return (float)v[(size_t)(k - 31) * nc + c] * iv[r >= 8 ? 1 : 0];
+        },
+        x);
+    float y[4];
+    fused_forward(W, x, y);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int c = r0 + g + 8 * h;
+      if (c >= nc) continue;
+      const float sc = vn[h] * feat[(size_t)c * MLP_FEAT + 31];
+      if (2 * t < MLP_OUT) z[(size_t)(2 * t) * nc + c] = (T)(y[2 * h] * sc);
+      if (2 * t + 1 < MLP_OUT) z[(size_t)(2 * t + 1) * nc + c] = (T)(y[2 * h + 1] * sc);
     }
   }
 }
@@ -446,7 +526,6 @@ __global__ void __launch_bounds__(256) k_mlp_weight_norm(int count, float* __res
 }
 
 size_t train_smem() { return sizeof(MlpTrainSmem); }
-size_t fwd_smem() { return sizeof(MlpW) + sizeof(MlpActInf); }
 // persistent inference grids: resident CTAs of the device
 int inference_grid(int ntiles) {
   static int sms = 0;
@@ -455,7 +534,7 @@ int inference_grid(int ntiles) {
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
       sms = 1;
   }
-  return std::max(1, std::min(ntiles, sms * 3));
+  return std::max(1, std::min(ntiles, sms * 3));  // 3 CTAs of 8 warps per SM (80 registers)
 }
 
 }  // namespace
@@ -490,9 +569,6 @@ fv3d_status Mlp::init(Ctx& ctx, unsigned long long seed) {
   adam_t = 0;
   ready = true;
   MCK(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
-  MCK(cudaFuncSetAttribute(k_mlp_forward, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem()));
-  MCK(cudaFuncSetAttribute(k_mlp_apply<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem()));
-  MCK(cudaFuncSetAttribute(k_mlp_apply<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fwd_smem()));
   return FV3D_OK;
 }
 
@@ -509,7 +585,8 @@ fv3d_status Mlp::forward_host(Ctx& ctx, const float* X, int n, float* Y) {
   MCK(dX.alloc((size_t)n * MLP_IN));
   MCK(dY.alloc((size_t)n * MLP_OUT));
   MCK(cudaMemcpy(dX.p, X, sizeof(float) * n * MLP_IN, cudaMemcpyHostToDevice));
-  k_mlp_forward<<<inference_grid((n + MLP_TILE - 1) / MLP_TILE), 128, fwd_smem(), ctx.stream>>>(P.p, dX.p, n, dY.p);
+  k_mlp_forward<<<inference_grid((n + 16 * kInfWarps - 1) / (16 * kInfWarps)), 32 * kInfWarps, 0, ctx.stream>>>(
+      P.p, dX.p, n, dY.p);
   MCK(cudaGetLastError());
   MCK(cudaStreamSynchronize(ctx.stream));
   MCK(cudaMemcpy(Y, dY.p, sizeof(float) * n * MLP_OUT, cudaMemcpyDeviceToHost));
@@ -606,14 +683,16 @@ fv3d_status Mlp::build_features(Ctx& ctx, const Implicit& im) {
 }
 
 fv3d_status Mlp::apply(Ctx& ctx, const double* vin, double* zout) {
-  k_mlp_apply<double><<<inference_grid((ctx.nc + MLP_TILE - 1) / MLP_TILE), 128, fwd_smem(), ctx.stream>>>(P.p, ctx.nc, feat.p, vin,
+  k_mlp_apply<double><<<inference_grid((ctx.nc + 16 * kInfWarps - 1) / (16 * kInfWarps)), 32 * kInfWarps, 0,
+                        ctx.stream>>>(P.p, ctx.nc, feat.p, vin,
                                                                                           zout);
   MCK(cudaGetLastError());
   return FV3D_OK;
 }
 
 fv3d_status Mlp::apply(Ctx& ctx, const float* vin, float* zout) {
-  k_mlp_apply<float><<<inference_grid((ctx.nc + MLP_TILE - 1) / MLP_TILE), 128, fwd_smem(), ctx.stream>>>(P.p, ctx.nc, feat.p, vin,
+  k_mlp_apply<float><<<inference_grid((ctx.nc + 16 * kInfWarps - 1) / (16 * kInfWarps)), 32 * kInfWarps, 0,
+                       ctx.stream>>>(P.p, ctx.nc, feat.p, vin,
                                                                                          zout);
   MCK(cudaGetLastError());
   return FV3D_OK;

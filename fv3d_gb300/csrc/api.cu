@@ -289,6 +289,7 @@ fv3d_status Ctx::cuda(cudaError_t e, const char* what) {
 void Ctx::release_graphs() {
   for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
   graphs.clear();
+  if (implicit) implicit->release_graphs();  // they capture the same buffers and constants
 }
 
 template <class R>

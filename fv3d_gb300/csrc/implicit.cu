@@ -35,7 +35,7 @@ namespace fv3d {
 
 namespace {
 
-constexpr int RED_BLOCKS = 608;   // fixed grid for deterministic reductions (4 per SM)
+constexpr int RED_BLOCKS = 304;   // fixed grid for deterministic reductions (2 per SM)
 // device coefficient slots: h1 [0, 32), h2 [32, 64), |w| and its derived
 // scalars [64, 68), |z|, 1/|z|, eps, 1/eps [68, 72), a host norm [96, 100);
 // FGMRES's y for the solution update at [0, k)
@@ -121,6 +121,134 @@ __global__ void __launch_bounds__(1024) k_dots_final(int nb, int k, const T* __r
       out[j] = t;
     }
   }
+}
+
+// ---- fused Gram-Schmidt passes -------------------------------------------
+// One pass over w and the k basis vectors per step of classical Gram-Schmidt
+// with re-orthogonalisation, each ending with a fixed-order reduction done
+// by the grid's last block (an atomic ticket; the block partials are summed
+// in block order, so the result does not depend on which block is last):
+//   PASS 1  h_j = w . V_j
+//   PASS 2  w <- w - sum_j h_j V_j, then h'_j = w . V_j of the new w
+//   PASS 3  w <- w - sum_j h'_j V_j, then |w| (and 1/|w|)
+//   PASS 0  |w| alone
+// Products and sums in T (FP32 basis: FP32 pipe), the final sums and the
+// coefficients in FP64.
+template <class T>
+__device__ void gs_finalize(const T* __restrict__ partial, int nb, int k, double* __restrict__ out, bool norm,
+                            double c, unsigned int* counter) {
+  __shared__ bool last;
+  // the threads that wrote this block's partials make them visible, then
+  // one thread takes the ticket
+  if (threadIdx.x < 32) __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  // one warp per column: each lane sums a fixed set of block partials
+  // (independent loads), then a fixed xor tree
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int j = warp; j < k; j += 8) {
+    T s0 = T(0), s1 = T(0);
+    int b = lane;
+    for (; b + 32 < nb; b += 64) {
+      s0 += __ldcg(partial + (size_t)b * 32 + j);
+      s1 += __ldcg(partial + (size_t)(b + 32) * 32 + j);
+    }
+    if (b < nb) s0 += __ldcg(partial + (size_t)b * 32 + j);
+    T v = s0 + s1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) {
+      const double t = (double)v;
+      if (norm) {
+        const double r = sqrt(t);
+        out[0] = r;
+        out[1] = (r > 0.0) ? 1.0 / r : 0.0;
+        out[2] = (r > 0.0) ? c / r : 0.0;
+        out[3] = (r > 0.0) ? r / c : 0.0;
+      } else {
+        out[j] = t;
+      }
+    }
+  }
+  if (threadIdx.x == 0) *counter = 0u;  // ready for the next pass
+}
+
+template <int KMAX, int PASS, class T>
+__global__ void __launch_bounds__(256) k_gs(size_t n, T* __restrict__ w, const T* __restrict__ V, int k,
+                                            const double* __restrict__ h_in, T* __restrict__ partial,
+                                            unsigned int* counter, double* __restrict__ out, double c,
+                                            const double* __restrict__ c_dev) {
+  if (c_dev != nullptr) c = *c_dev;  // the finite-difference scale, set per Newton step
+  __shared__ T hs[32];
+  __shared__ T sh[8][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (PASS >= 2 && threadIdx.x < 32) hs[threadIdx.x] = (threadIdx.x < (unsigned)k) ? (T)h_in[threadIdx.x] : T(0);
+  __syncthreads();
+  constexpr int NA = (PASS == 0 || PASS == 3) ? 1 : KMAX;
+  // elements per thread per iteration: several independent loads in flight
+  constexpr int U = (PASS <= 1) ? (KMAX <= 8 ? 8 : (KMAX <= 16 ? 4 : 2)) : (KMAX <= 8 ? 4 : (KMAX <= 16 ? 2 : 1));
+  T acc[NA];
+#pragma unroll
+  for (int j = 0; j < NA; ++j) acc[j] = T(0);
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  for (; i < n; i += U * stride) {
+    T wi[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) wi[u] = (i + u * stride < n) ? w[i + u * stride] : T(0);
+    if (PASS == 0) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) acc[0] = fmadd(wi[u], wi[u], acc[0]);
+    } else if (PASS == 1) {
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int j = 0; j < KMAX; ++j)
+          if (j < k && i + u * stride < n) acc[j] = fmadd(wi[u], V[(size_t)j * n + i + u * stride], acc[j]);
+    } else {
+      T v[U][KMAX];
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int j = 0; j < KMAX; ++j) v[u][j] = (j < k && i + u * stride < n) ? V[(size_t)j * n + i + u * stride] : T(0);
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        T sum = T(0);
+#pragma unroll
+        for (int j = 0; j < KMAX; ++j)
+          if (j < k) sum = fmadd(hs[j], v[u][j], sum);
+        const T wn = wi[u] - sum;
+        if (i + u * stride < n) w[i + u * stride] = wn;
+        if (PASS == 2) {
+#pragma unroll
+          for (int j = 0; j < KMAX; ++j)
+            if (j < k) acc[j] = fmadd(wn, v[u][j], acc[j]);
+        } else {
+          acc[0] = fmadd(wn, wn, acc[0]);
+        }
+      }
+    }
+  }
+  const int kk = (NA == 1) ? 1 : k;
+#pragma unroll
+  for (int j = 0; j < NA; ++j) {
+    if (j >= kk) break;
+    T v = acc[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) sh[warp][j] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32 && (int)threadIdx.x < kk) {
+    T s = T(0);
+#pragma unroll
+    for (int wv = 0; wv < 8; ++wv) s += sh[wv][threadIdx.x];
+    partial[(size_t)blockIdx.x * 32 + threadIdx.x] = s;
+  }
+  gs_finalize<T>(partial, gridDim.x, kk, out, PASS == 0 || PASS == 3, c, counter);
 }
 
 // out = x * (*s) when *s > 0 (s = 1/|x| from k_dots_final: the new Arnoldi vector)
@@ -518,6 +646,7 @@ __global__ void k_block_solve(int nc, const double* __restrict__ D, const double
 fv3d_status Implicit::setup(Ctx& ctx, int m) {
   const size_t n = 5 * (size_t)ctx.nc;
   if (this->n == n && this->m >= m) return FV3D_OK;
+  release_graphs();  // captured steps hold the old buffers
   this->n = n;
   this->m = m;
   auto al = [&](DevBuf<double>& b, size_t cnt) { return ctx.cuda(b.alloc(cnt), "implicit allocation"); };
@@ -531,7 +660,9 @@ fv3d_status Implicit::setup(Ctx& ctx, int m) {
                                         "implicit host buffer")) != FV3D_OK)
     return st;
   if ((st = ctx.cuda(Dinv.alloc(25 * (size_t)ctx.nc), "implicit allocation")) != FV3D_OK) return st;
-  if ((st = ctx.cuda(bits.alloc(1), "implicit allocation")) != FV3D_OK) return st;
+  if ((st = ctx.cuda(bits.alloc(2), "implicit allocation")) != FV3D_OK) return st;
+  // word 0: k_min_rho_p's minimum; word 1: the Gram-Schmidt passes' block ticket
+  ICK(cudaMemset(bits.p, 0, 2 * sizeof(unsigned long long)));
   // face centre distances for the two-point viscous term
   std::vector<double> fd(ctx.nf);
   for (int f = 0; f < ctx.nf; ++f) {
@@ -601,6 +732,23 @@ fv3d_status Implicit::dots_dev(Ctx& ctx, const T* wv, const T* Vb, int k, double
   return FV3D_OK;
 }
 
+// one fused Gram-Schmidt pass (k_gs) over a fixed grid of RED_BLOCKS blocks
+template <class T>
+fv3d_status Implicit::gs_pass(Ctx& ctx, int pass, T* wv, const T* Vb, int k, const double* h_in, double* dst,
+                              double c, const double* c_dev) {
+  const int nb = std::min(RED_BLOCKS, blocks(n));
+  T* pt = reinterpret_cast<T*>(part.p);
+  unsigned int* ctr = reinterpret_cast<unsigned int*>(bits.p + 1);  // zero between passes
+#define GS_LAUNCH(KM, P) k_gs<KM, P, T><<<nb, 256, 0, ctx.stream>>>(n, wv, Vb, k, h_in, pt, ctr, dst, c, c_dev)
+  if (pass == 0) GS_LAUNCH(1, 0);
+  else if (pass == 3) { if (k <= 8) GS_LAUNCH(8, 3); else if (k <= 16) GS_LAUNCH(16, 3); else GS_LAUNCH(32, 3); }
+  else if (pass == 1) { if (k <= 8) GS_LAUNCH(8, 1); else if (k <= 16) GS_LAUNCH(16, 1); else GS_LAUNCH(32, 1); }
+  else { if (k <= 8) GS_LAUNCH(8, 2); else if (k <= 16) GS_LAUNCH(16, 2); else GS_LAUNCH(32, 2); }
+#undef GS_LAUNCH
+  ICK(cudaGetLastError());
+  return FV3D_OK;
+}
+
 // |v| on the host (synchronises)
 fv3d_status Implicit::norm(Ctx& ctx, const double* v, double* out) {
   fv3d_status st = dots_dev<double>(ctx, v, v, 1, hdev.p + 96, true, 1.0);
@@ -627,8 +775,9 @@ fv3d_status Implicit::precondition(Ctx& ctx, const T* v, T* z) {
 // device, so a Jacobian-vector product needs no host synchronisation
 template <class T>
 fv3d_status Implicit::apply_A(Ctx& ctx, const T* z, T* out) {
-  const double rel = (opts.jv_precision == 1) ? 5e-4 : opts.fd_eps;
-  fv3d_status st = dots_dev<T>(ctx, z, z, 1, hdev.p + 68, true, rel * (1.0 + unorm));
+  // |z| and eps = c/|z| with c = rel (1 + |U|) from its device slot (set by
+  // set_fd_scale each Newton step), so captured iterations stay valid
+  fv3d_status st = gs_pass<T>(ctx, 0, const_cast<T*>(z), z, 1, nullptr, hdev.p + 68, 0.0, hdev.p + 100);
   if (st != FV3D_OK) return st;
   k_fd_state<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, ctx.d_U.p, z, hdev.p + 70, Wst.p);
   ICK(cudaGetLastError());
@@ -637,7 +786,6 @@ fv3d_status Implicit::apply_A(Ctx& ctx, const T* z, T* out) {
   if (st != FV3D_OK) return st;
   k_jv_combine<T><<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, z, Rp.p, Rb.p, idtl.p, hdev.p + 71, out);
   ICK(cudaGetLastError());
-  jv_count += 1;
   return FV3D_OK;
 }
 
@@ -674,6 +822,58 @@ fv3d_status Implicit::build_blocks(Ctx& ctx) {
 }
 
 // restarted FGMRES(m) for (I/dt - J) x = R, x0 = 0; returns iterations
+// one Arnoldi step k: z_k = M v_k, w = A z_k, classical Gram-Schmidt twice,
+// |w| and v_{k+1} = w / |w| on the device, the Hessenberg column copied to
+// the pinned host buffer.  Replayed from a CUDA graph per (k, preconditioner
+// kind) once captured: every scalar it needs lives in device memory.
+template <class T>
+fv3d_status Implicit::enqueue_arnoldi(Ctx& ctx, T* Vt, T* Zt, T* wt, int k) {
+  T* vk = Vt + (size_t)k * n;
+  T* zk = Zt + (size_t)k * n;
+  fv3d_status st = precondition<T>(ctx, vk, zk);
+  if (st != FV3D_OK) return st;
+  if ((st = apply_A<T>(ctx, zk, wt)) != FV3D_OK) return st;
+  if ((st = gs_pass<T>(ctx, 1, wt, Vt, k + 1, nullptr, hdev.p, 0.0, nullptr)) != FV3D_OK) return st;
+  if ((st = gs_pass<T>(ctx, 2, wt, Vt, k + 1, hdev.p, hdev.p + 32, 0.0, nullptr)) != FV3D_OK) return st;
+  if ((st = gs_pass<T>(ctx, 3, wt, Vt, k + 1, hdev.p + 32, hdev.p + 64, 1.0, nullptr)) != FV3D_OK) return st;
+  k_scale_dev<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, wt, hdev.p + 65, Vt + (size_t)(k + 1) * n);
+  ICK(cudaGetLastError());
+  ICK(cudaMemcpyAsync(hpin, hdev.p, sizeof(double) * kHostCoefs, cudaMemcpyDeviceToHost, ctx.stream));
+  return FV3D_OK;
+}
+
+template <class T>
+fv3d_status Implicit::arnoldi_step(Ctx& ctx, T* Vt, T* Zt, T* wt, int k) {
+  const int pc = (opts.preconditioner == FV3D_PC_LEARNED && use_block_jacobi) ? (int)FV3D_PC_BLOCK_JACOBI
+                                                                             : opts.preconditioner;
+  const long long key = (((long long)k * 8 + pc) * 2 + (sizeof(T) == 4 ? 1 : 0)) * 2 + opts.jv_precision;
+  auto it = arnoldi_graphs.find(key);
+  if (it == arnoldi_graphs.end()) {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ICK(cudaStreamBeginCapture(ctx.stream, cudaStreamCaptureModeThreadLocal));
+    fv3d_status st = enqueue_arnoldi<T>(ctx, Vt, Zt, wt, k);
+    cudaError_t ce = cudaStreamEndCapture(ctx.stream, &g);
+    if (st != FV3D_OK) {
+      if (g) cudaGraphDestroy(g);
+      return st;
+    }
+    ICK(ce);
+    ce = cudaGraphInstantiate(&exec, g, 0);
+    cudaGraphDestroy(g);
+    ICK(ce);
+    it = arnoldi_graphs.emplace(key, exec).first;
+  }
+  ICK(cudaGraphLaunch(it->second, ctx.stream));
+  jv_count += 1;
+  return FV3D_OK;
+}
+
+void Implicit::release_graphs() {
+  for (auto& kv : arnoldi_graphs) cudaGraphExecDestroy(kv.second);
+  arnoldi_graphs.clear();
+}
+
 // restarted flexible GMRES on the Newton system with basis V, Z and work
 // vector wt of type T (FP32 for FP32 Jacobian-vector products)
 template <class T>
@@ -691,6 +891,7 @@ fv3d_status Implicit::fgmres_t(Ctx& ctx, T* Vt, T* Zt, T* wt, double rnorm, int*
       // true residual of the current iterate: R - A x (in FP64)
       fv3d_status st = apply_A<double>(ctx, x.p, w.p);
       if (st != FV3D_OK) return st;
+      jv_count += 1;
       k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, 1.0, R.p, -1.0, w.p, Rp.p);
       if ((st = norm(ctx, Rp.p, &beta)) != FV3D_OK) return st;
       if (!(beta > opts.eta * rnorm)) { res = beta; break; }
@@ -703,22 +904,8 @@ fv3d_status Implicit::fgmres_t(Ctx& ctx, T* Vt, T* Zt, T* wt, double rnorm, int*
     int k = 0;
     bool done = false;
     for (; k < m; ++k) {
-      T* vk = Vt + (size_t)k * n;
-      T* zk = Zt + (size_t)k * n;
-      fv3d_status st = precondition<T>(ctx, vk, zk);
-      if (st != FV3D_OK) return st;
-      st = apply_A<T>(ctx, zk, wt);
-      if (st != FV3D_OK) return st;
-      // classical Gram-Schmidt, twice, the norm and the next basis vector on
-      // the device; one host synchronisation for the Hessenberg column
-      if ((st = dots_dev<T>(ctx, wt, Vt, k + 1, hdev.p, false, 0.0)) != FV3D_OK) return st;
-      k_multi_axpy<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, wt, Vt, hdev.p, k + 1, -1.0);
-      if ((st = dots_dev<T>(ctx, wt, Vt, k + 1, hdev.p + 32, false, 0.0)) != FV3D_OK) return st;
-      k_multi_axpy<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, wt, Vt, hdev.p + 32, k + 1, -1.0);
-      if ((st = dots_dev<T>(ctx, wt, wt, 1, hdev.p + 64, true, 1.0)) != FV3D_OK) return st;
-      k_scale_dev<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, wt, hdev.p + 65, Vt + (size_t)(k + 1) * n);
-      ICK(cudaGetLastError());
-      ICK(cudaMemcpyAsync(hpin, hdev.p, sizeof(double) * kHostCoefs, cudaMemcpyDeviceToHost, ctx.stream));
+      fv3d_status st;
+      if ((st = arnoldi_step<T>(ctx, Vt, Zt, wt, k)) != FV3D_OK) return st;
       ICK(cudaStreamSynchronize(ctx.stream));
       const double hn = hpin[64];
       for (int j = 0; j <= k; ++j) H[(size_t)k * (m + 1) + j] = hpin[j] + hpin[32 + j];
@@ -778,6 +965,9 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
   {
     const size_t nv = (size_t)(opts.krylov_dim + 1) * n, nz = (size_t)opts.krylov_dim * n;
     cudaError_t e = cudaSuccess;
+    if ((opts.jv_precision == 1 && (V32.n < nv || Z32.n < nz || w32.n < n)) ||
+        (opts.jv_precision != 1 && (V.n < nv || Z.n < nz)))
+      release_graphs();  // captured steps hold the old basis
     if (opts.jv_precision == 1) {
       if (V32.n < nv) e = V32.alloc(nv);
       if (e == cudaSuccess && Z32.n < nz) e = Z32.alloc(nz);
@@ -804,6 +994,13 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
     if (newton == opts.max_newton) break;
     if (newton > 0) cfl = std::min(opts.cfl_max, std::max(opts.cfl_start, opts.cfl_start * res0 / res));
     if ((st = norm(ctx, ctx.d_U.p, &unorm)) != FV3D_OK) return st;
+    {
+      // c = rel (1 + |U|) for the finite-difference steps of this Newton step
+      const double rel = (opts.jv_precision == 1) ? 5e-4 : opts.fd_eps;
+      hpin[0] = rel * (1.0 + unorm);
+      ICK(cudaMemcpyAsync(hdev.p + 100, hpin, sizeof(double), cudaMemcpyHostToDevice, ctx.stream));
+      ICK(cudaStreamSynchronize(ctx.stream));
+    }
     // Newton step with a CFL back-off on failure
     for (int attempt = 0; attempt < 6; ++attempt) {
       k_local_dt<<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, ctx.d_U.p, ctx.d_vol.p, ctx.d_dx.p,

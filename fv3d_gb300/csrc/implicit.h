@@ -3,6 +3,8 @@
 
 #include <vector>
 
+#include <map>
+
 #include "context.h"
 
 namespace fv3d {
@@ -45,9 +47,17 @@ struct Implicit {
   bool use_block_jacobi = false;  // learned preconditioner fell back this step
   double* hpin = nullptr;         // pinned host copy of the Arnoldi coefficients (kHostCoefs doubles)
 
+  std::map<long long, cudaGraphExec_t> arnoldi_graphs;  // captured Arnoldi steps
+
   ~Implicit() {
+    release_graphs();
     if (hpin) cudaFreeHost(hpin);
   }
+  void release_graphs();
+  template <class T>
+  fv3d_status enqueue_arnoldi(Ctx& ctx, T* Vt, T* Zt, T* wt, int k);
+  template <class T>
+  fv3d_status arnoldi_step(Ctx& ctx, T* Vt, T* Zt, T* wt, int k);
 
   fv3d_status setup(Ctx& ctx, int m);
   fv3d_status solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit_stats* stats);
@@ -61,6 +71,9 @@ struct Implicit {
   fv3d_status build_blocks(Ctx& ctx);
   template <class T>
   fv3d_status dots_dev(Ctx& ctx, const T* w, const T* V, int k, double* dst, bool take_sqrt, double c);
+  template <class T>
+  fv3d_status gs_pass(Ctx& ctx, int pass, T* w, const T* V, int k, const double* h_in, double* dst, double c,
+                      const double* c_dev);
   fv3d_status norm(Ctx& ctx, const double* v, double* out);
   fv3d_status ICK_copy(Ctx& ctx, double* dst, const double* src);
 

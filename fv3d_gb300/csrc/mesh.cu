@@ -11,6 +11,7 @@
 #include <queue>
 
 #include "context.h"
+#include "implicit.h"
 
 namespace fv3d {
 
@@ -84,6 +85,9 @@ std::vector<int> rcm_order(int nc, const std::vector<std::vector<int>>& adj) {
 fv3d_status prepare_mesh(Ctx& ctx, const fv3d_mesh_arrays& m) {
   ctx.mesh_ready = ctx.state_ready = ctx.residual_valid = false;
   ctx.release_graphs();
+  // the implicit solver's buffers and face data belong to the old mesh
+  delete ctx.implicit;
+  ctx.implicit = nullptr;
   const int nc = m.n_cells, nf = m.n_faces, nb = m.n_boundaries, mcf = m.max_cell_faces;
   if (nc <= 0 || nf <= 0 || nb < 0 || mcf <= 0 || mcf > 8 || m.n_regions <= 0 ||
       m.n_regions > MAX_REGIONS)

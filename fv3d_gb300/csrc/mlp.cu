@@ -733,6 +733,7 @@ extern "C" fv3d_status fv3d_mlp_init(fv3d_ctx* handle, unsigned long long seed) 
   if (handle == nullptr) return FV3D_ERR_INVALID_ARG;
   Ctx* ctx = reinterpret_cast<Ctx*>(handle);
   if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "cudaSetDevice");
+  if (ctx->implicit) ctx->implicit->release_graphs();  // captured steps hold the old parameter buffer
   return mlp_of(ctx)->init(*ctx, seed);
 }
 

@@ -161,6 +161,19 @@ def test_navier_stokes_fp64_and_mixed(oracle, maker, steps):
     assert emx.max() < MIXED_STATE_TOL, emx
 
 
+@pytest.mark.parametrize("scheme", ["euler", "rk45", "ssprk3"])
+def test_mixed_precision_other_schemes(oracle, scheme):
+    """The mixed path with forward Euler, Carpenter-Kennedy RK4(5) and
+    SSP-RK3 against the FP64 oracle (RK3 is covered above)."""
+    c = cases.tgv_tet(6)
+    u_ref, t_ref = run_oracle(oracle, c, scheme, 10, 0.5)
+    with api.from_case(c, "mixed") as s:
+        st = s.step_explicit(scheme, 10, cfl=0.5)
+        err = rel_l2(s.get_conserved(), u_ref)
+    assert abs(st["t"] / t_ref - 1) < 1e-5
+    assert err.max() < MIXED_STATE_TOL, err
+
+
 def test_deterministic_and_renumbering_invariant():
     """No atomics in the accumulation: repeated runs are bit-identical, and
     because every cell sums its faces in reference face order the result does

@@ -84,6 +84,7 @@ class NewtonStats(C.Structure):
     _fields_ = [("n_inner", C.c_int), ("err0", C.c_double), ("err", C.c_double)]
 
 
+EXACT_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double))
 ITERATION_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double), C.c_int)
 
 
@@ -140,6 +141,7 @@ EXPORTS = {
     "fv3d_step_newton": ([C.c_void_p, C.POINTER(NewtonOpts), C.c_int, C.c_double, C.c_double,
                           C.POINTER(NewtonStats)], C.c_int),
     "fv3d_timedisc": ([C.c_void_p, C.POINTER(TimedOpts), C.POINTER(TimedStats)], C.c_int),
+    "fv3d_set_exact_function": ([C.c_void_p, EXACT_FN, C.c_void_p, C.c_int, C.c_double], C.c_int),
     "fv3d_mlp_num_params": ([], C.c_int),
     "fv3d_mlp_init": ([C.c_void_p, C.c_ulonglong], C.c_int),
     "fv3d_mlp_get_params": ([C.c_void_p, _f4p], C.c_int),
@@ -319,6 +321,17 @@ class Solver:
         if check:
             self._check(rc)
         return {"n_inner": st.n_inner, "err0": st.err0, "err": st.err, "status": rc}
+
+    def set_exact_function(self, fn, id_=0, t=0.0):
+        """set_exact_function + set_solution: fn(id, t, x[3]) -> phi (10 values,
+        the reference's phi_total row; the conserved entries are used)."""
+        def cb(_user, i, tt, x, phi):
+            out = fn(i, tt, np.array([x[0], x[1], x[2]]))
+            for j in range(min(10, len(out))):
+                phi[j] = float(out[j])
+
+        f = EXACT_FN(cb)
+        self._check(self.lib.fv3d_set_exact_function(self.h, f, None, id_, t))
 
     def timedisc(self, scheme="rk33", implicit=False, max_iter=1000, is_transient=True, abort_residual=1e-10,
                  t_start=0.0, t_end=0.2, cfl=0.5, max_iter_inner=100, check=True):

@@ -558,6 +558,20 @@ static fv3d_status export_soa(Ctx* ctx, const double* src, int m, int with_prims
   return FV3D_OK;
 }
 
+extern "C" fv3d_status fv3d_set_exact_function(fv3d_ctx* handle, fv3d_exact_fn fn, void* user, int id, double t) {
+  if (handle == nullptr || fn == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (!ctx->mesh_ready) return ctx->fail(FV3D_ERR_STATE, "no mesh loaded");
+  std::vector<double> u((size_t)ctx->nc * 5);
+  double phi[10];
+  for (int i = 0; i < ctx->nc; ++i) {
+    for (int j = 0; j < 10; ++j) phi[j] = 0.0;
+    fn(user, id, t, &ctx->h_cell_x[3 * (size_t)i], phi);
+    for (int j = 0; j < 5; ++j) u[5 * (size_t)i + j] = phi[j];
+  }
+  return fv3d_set_state(handle, u.data());
+}
+
 extern "C" fv3d_status fv3d_get_state(fv3d_ctx* handle, double* phi_total) {
   if (handle == nullptr || phi_total == nullptr) return FV3D_ERR_INVALID_ARG;
   Ctx* ctx = reinterpret_cast<Ctx*>(handle);

@@ -58,6 +58,7 @@ struct Ctx {
   std::vector<int> h_fc0, h_fc1, h_cface;
   std::vector<double> h_geo;  // [nf][GEO] FP64 geometry (new order)
   std::vector<double> h_lam, h_lsq, h_vol, h_dx;
+  std::vector<double> h_cell_x;  // cell centres in reference order (for exact-function initial states)
 
   // device mesh
   DevBuf<int> d_iperm, d_perm, d_fc0, d_fc1, d_fregion, d_cface, d_cnbr;

@@ -225,6 +225,7 @@ fv3d_status prepare_mesh(Ctx& ctx, const fv3d_mesh_arrays& m) {
   ctx.h_dx.assign((size_t)nc * 3, 0.0);
   ctx.vol_total = 0.0;
   for (int i = 0; i < nc; ++i) ctx.vol_total += m.cell_volume[i];  // sum_n order (mesh.c:25)
+  ctx.h_cell_x.assign(m.cell_x, m.cell_x + (size_t)nc * 3);
   for (int c = 0; c < nc; ++c) {
     const int old = order[c];
     std::vector<int> fl;

@@ -137,6 +137,13 @@ fv3d_status fv3d_set_region(fv3d_ctx *ctx, int region, int bc_type, const double
 /* conserved state [n_cells*5] in reference order (set_solution,
  * finite_volume.c:189-201, followed by the update routine) */
 fv3d_status fv3d_set_state(fv3d_ctx *ctx, const double *u_con);
+/* set_exact_function + set_solution (finite_volume.c:162-200): the initial
+ * state from a host function evaluated at every cell centre in reference
+ * order, fn(user, id, t, x[3], phi[10]) filling the reference's phi_total row
+ * (conserved entries 0..4 used, the primitives recomputed as ns_update does);
+ * the reference calls it with id 0 and t 0. */
+typedef void (*fv3d_exact_fn)(void *user, int id, double t, const double *x, double *phi);
+fv3d_status fv3d_set_exact_function(fv3d_ctx *ctx, fv3d_exact_fn fn, void *user, int id, double t);
 /* reference phi_total layout [n_cells*10]: rho, rho_u, rho_v, rho_w, rho_e,
  * u, v, w, p, T (navier_stokes.c:107-117) */
 fv3d_status fv3d_get_state(fv3d_ctx *ctx, double *phi_total);

@@ -36,3 +36,18 @@ def test_pinned_and_pageable_round_trips_agree(precision):
         r2 = pinned(u.shape)
         s.get_conserved(out=r2)
     assert np.array_equal(r1, r2)
+
+
+def test_exact_function_initial_state():
+    """set_exact_function + set_solution: a host function of the cell centre
+    gives the same state as uploading it."""
+    c = cases.tgv_tet(4)
+
+    def tgv(_id, _t, x):
+        u, _ = cases.taylor_green(x[None, :], 0.8)
+        return list(u[0]) + [0.0] * 5
+
+    with api.from_case(c, "fp64") as s:
+        s.set_exact_function(tgv)
+        a = s.get_conserved()
+    assert np.allclose(a, c.u0, rtol=1e-15, atol=0.0)

@@ -1,0 +1,137 @@
+"""Gmsh mesh files to processed meshes (the reader half of the reference's
+preprocessor, tools/pyMeshFV3D: pymeshfv3d/readers/gmsh.py reading, process.py
+building faces and geometry).
+
+Reads the ASCII MSH 2.2 format: $PhysicalNames, $Nodes, $Elements.  Volume
+elements become cells (8-node hexahedra, type 5, or 4-node tetrahedra, type
+4; one kind per mesh, as ``meshgen.build_mesh`` assembles), surface elements
+(4-node quadrangles, type 3, or 3-node triangles, type 2) carry the physical
+group of the boundary faces they cover.  Regions are numbered as the
+reference's processed meshes number them: region 0 the flow domain, then the
+boundary physical groups in ascending tag order.  Periodic meshes ($Periodic)
+are rejected: the reference's preprocessor has none either.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import meshgen as mg
+
+_VOLUME = {5: ("hex", 8), 4: ("tet", 4)}
+_SURFACE = {3: 4, 2: 3}
+
+
+def _sections(text):
+    out, lines, i = {}, text.splitlines(), 0
+    while i < len(lines):
+        line = lines[i].strip()
+        if line.startswith("$") and not line.startswith("$End"):
+            name = line[1:]
+            j = i + 1
+            while j < len(lines) and lines[j].strip() != f"$End{name}":
+                j += 1
+            if j == len(lines):
+                raise ValueError(f"unterminated section ${name}")
+            out[name] = lines[i + 1:j]
+            i = j + 1
+        else:
+            i += 1
+    return out
+
+
+def read_msh(path_or_text, name=None, scale=(1.0, 1.0, 1.0)):
+    """A processed ``meshgen.Mesh`` from an ASCII MSH 2.2 file (or its text)."""
+    text = path_or_text
+    if "\n" not in path_or_text:
+        with open(path_or_text) as f:
+            text = f.read()
+    sec = _sections(text)
+    fmt = sec.get("MeshFormat", ["?"])[0].split()
+    if not fmt or not fmt[0].startswith("2"):
+        raise ValueError(f"MSH format {fmt[0] if fmt else '?'} not supported (ASCII 2.2 only)")
+    if len(fmt) > 1 and fmt[1] != "0":
+        raise ValueError("binary MSH files are not supported")
+    if "Periodic" in sec:
+        raise ValueError("periodic Gmsh meshes are not supported")
+    phys_names = {}
+    for line in sec.get("PhysicalNames", [])[1:]:
+        dim, tag, nm = line.split(maxsplit=2)
+        phys_names[(int(dim), int(tag))] = nm.strip().strip('"')
+    node_lines = sec["Nodes"]
+    n_nodes = int(node_lines[0])
+    ids = np.empty(n_nodes, dtype=np.int64)
+    xyz = np.empty((n_nodes, 3))
+    for k, line in enumerate(node_lines[1:1 + n_nodes]):
+        p = line.split()
+        ids[k] = int(p[0])
+        xyz[k] = [float(p[1]), float(p[2]), float(p[3])]
+    xyz *= np.asarray(scale, dtype=float)
+    index = {int(t): k for k, t in enumerate(ids)}
+    cells, cell_kind, surf = [], None, []
+    el_lines = sec["Elements"]
+    for line in el_lines[1:1 + int(el_lines[0])]:
+        p = [int(v) for v in line.split()]
+        etype, ntags = p[1], p[2]
+        tags = p[3:3 + ntags]
+        conn = [index[v] for v in p[3 + ntags:]]
+        phys = tags[0] if ntags > 0 else 0
+        if etype in _VOLUME:
+            kind, nv = _VOLUME[etype]
+            if cell_kind not in (None, kind):
+                raise ValueError("meshes mixing hexahedra and tetrahedra are not supported")
+            cell_kind = kind
+            cells.append(conn[:nv])
+        elif etype in _SURFACE:
+            surf.append((phys, conn[:_SURFACE[etype]]))
+        elif etype in (1, 15):          # lines, points: geometry only
+            continue
+        else:
+            raise ValueError(f"Gmsh element type {etype} not supported")
+    if not cells:
+        raise ValueError("no volume elements")
+    cell_nodes = np.asarray(cells, dtype=np.int64)
+    tags = sorted({t for t, _ in surf})
+    region_of_tag = {t: r + 1 for r, t in enumerate(tags)}
+    names = ["flow"] + [phys_names.get((2, t), f"boundary{t}") for t in tags]
+    # boundary faces are matched to surface elements by their node sets
+    surf_key = {tuple(sorted(c)): region_of_tag[t] for t, c in surf}
+
+    def regions(face_nodes):
+        out = np.empty(face_nodes.shape[0], dtype=np.int64)
+        for i, row in enumerate(face_nodes):
+            r = surf_key.get(tuple(int(v) for v in row))
+            if r is None:
+                raise ValueError(f"boundary face with nodes {[int(ids[v]) for v in row]} has no physical surface")
+            out[i] = r
+        return out
+
+    shift = np.zeros(cell_nodes.shape + (3,))
+    return mg.build_mesh(xyz, cell_nodes, shift, cell_kind,
+                         boundary_region_of_nodes=regions if surf else None,
+                         region_names=tuple(names), region_is_boundary=tuple([0] + [1] * len(tags)),
+                         name=name or "gmsh")
+
+
+def write_msh(path, nodes, cell_nodes, cell_kind, boundary, phys_names):
+    """Write an ASCII MSH 2.2 file: nodes (n, 3), volume connectivity, and the
+    boundary surface elements as (physical tag, node list) pairs."""
+    etype = 5 if cell_kind == "hex" else 4
+    lines = ["$MeshFormat", "2.2 0 8", "$EndMeshFormat", "$PhysicalNames", str(len(phys_names))]
+    for (dim, tag), nm in sorted(phys_names.items()):
+        lines.append(f'{dim} {tag} "{nm}"')
+    lines += ["$EndPhysicalNames", "$Nodes", str(nodes.shape[0])]
+    for k, x in enumerate(nodes):
+        lines.append(f"{k + 1} {float(x[0])!r} {float(x[1])!r} {float(x[2])!r}")
+    lines += ["$EndNodes", "$Elements", str(len(boundary) + cell_nodes.shape[0])]
+    eid = 1
+    for tag, conn in boundary:
+        st = 3 if len(conn) == 4 else 2
+        lines.append(" ".join(str(int(v)) for v in [eid, st, 2, tag, tag] + [int(c) + 1 for c in conn]))
+        eid += 1
+    vol_tag = max([t for (d, t) in phys_names if d == 3], default=0)
+    for conn in cell_nodes:
+        lines.append(" ".join(str(v) for v in [eid, etype, 2, vol_tag, vol_tag] + [int(c) + 1 for c in conn]))
+        eid += 1
+    lines.append("$EndElements")
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")

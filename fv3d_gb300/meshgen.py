@@ -182,7 +182,7 @@ def _tangents(n):
 # generic builder: cells (node ids + per-vertex periodic shifts) -> Mesh
 # ---------------------------------------------------------------------------
 def build_mesh(nodes, cell_nodes, cell_shift, cell_type, boundary_region_of_face=None,
-               region_names=("flow",), region_is_boundary=(0,), name="mesh"):
+               region_names=("flow",), region_is_boundary=(0,), name="mesh", boundary_region_of_nodes=None):
     """Assemble a processed mesh.
 
     nodes:       (n_nodes, 3) unique node coordinates
@@ -192,6 +192,8 @@ def build_mesh(nodes, cell_nodes, cell_shift, cell_type, boundary_region_of_face
     cell_type:   "hex" or "tet"
     boundary_region_of_face: callable(face_x (m,3), face_n (m,3)) -> region ids
                  for the unmatched (boundary) faces
+    boundary_region_of_nodes: alternatively callable(face node ids (m, fv),
+                 each row sorted) -> region ids
     """
     table = HEX_FACES if cell_type == "hex" else TET_FACES
     n_cells, nv = cell_nodes.shape
@@ -280,9 +282,13 @@ def build_mesh(nodes, cell_nodes, cell_shift, cell_type, boundary_region_of_face
     face_boundary = np.full(n_faces, -1, dtype=np.int64)
     face_boundary[bfaces] = np.arange(bfaces.shape[0])
     if bfaces.shape[0] > 0:
-        if boundary_region_of_face is None:
+        if boundary_region_of_nodes is not None:
+            boundary_id = np.asarray(boundary_region_of_nodes(np.sort(lf_nodes[f_first[bfaces]], axis=1)),
+                                     dtype=np.int64)
+        elif boundary_region_of_face is not None:
+            boundary_id = np.asarray(boundary_region_of_face(face_x[bfaces], n[bfaces]), dtype=np.int64)
+        else:
             raise ValueError("mesh has boundary faces but no boundary regions")
-        boundary_id = np.asarray(boundary_region_of_face(face_x[bfaces], n[bfaces]), dtype=np.int64)
     else:
         boundary_id = np.zeros(0, dtype=np.int64)
 

@@ -76,10 +76,15 @@ class Simulation:
     def regions(self, mesh):
         """region_type and region_prim arrays in the mesh's region order."""
         types, prims = [], []
+        flow = self.boundaries.get(mesh.region_names[0], (None, None))[1]
         for name in mesh.region_names:
             if name not in self.boundaries:
                 raise KeyError(f"no boundary condition for region {name!r}")
             t, prim = self.boundaries[name]
+            if t in (mg.BC_OUTFLOW, mg.BC_WALL_ADIABATIC, mg.BC_WALL_SLIP, mg.BC_SYMMETRY) and flow is not None:
+                prim = flow      # no state of their own: a finite placeholder
+            elif t == mg.BC_WALL_ISOTHERMAL and flow is not None:
+                prim = flow[:4] + (prim[4],)
             types.append(t)
             prims.append(prim)
         return np.asarray(types, dtype=np.int64), np.asarray(prims, dtype=np.float64)

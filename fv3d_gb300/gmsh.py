@@ -8,8 +8,16 @@ elements become cells (8-node hexahedra, type 5, or 4-node tetrahedra, type
 (4-node quadrangles, type 3, or 3-node triangles, type 2) carry the physical
 group of the boundary faces they cover.  Regions are numbered as the
 reference's processed meshes number them: region 0 the flow domain, then the
-boundary physical groups in ascending tag order.  Periodic meshes ($Periodic)
-are rejected: the reference's preprocessor has none either.
+boundary physical groups in ascending tag order.
+
+Periodic meshes ($Periodic, translational links) are an extension: the
+reference's preprocessor has none.  Every slave node is replaced by its
+master (chains of links followed to the end) and the cell keeps the
+translation between the two as its vertex shift, so the two cells across a
+periodic surface share the face and see each other's centre through the
+periodic image (the periodic faces of ``meshgen``).  Surface elements on
+periodic surfaces then cover interior faces; physical groups left with no
+boundary face get no region.
 """
 from __future__ import annotations
 
@@ -39,6 +47,50 @@ def _sections(text):
     return out
 
 
+def _periodic_links(lines):
+    """(slave id, master id) node pairs of a $Periodic section, with the link
+    each pair belongs to."""
+    n_links, i, pairs = int(lines[0]), 1, []
+    for link in range(n_links):
+        i += 1                                   # dimension slave-tag master-tag
+        if lines[i].split()[0] == "Affine":      # transformation line (newer writers)
+            i += 1
+        n = int(lines[i]); i += 1
+        for line in lines[i:i + n]:
+            sl, ms = line.split()[:2]
+            pairs.append((int(sl), int(ms), link))
+        i += n
+    return pairs
+
+
+def _resolve_periodic(pairs, index, xyz):
+    """Per node row: its canonical row (the end of its chain of links) and the
+    translation from that node to this one."""
+    master = {}
+    for sl, ms, _ in pairs:
+        if sl != ms:
+            master[index[sl]] = index[ms]
+    n = xyz.shape[0]
+    root = np.arange(n)
+    for v in master:
+        r, seen = v, {v}
+        while r in master:
+            r = master[r]
+            if r in seen:
+                raise ValueError("cyclic periodic links")
+            seen.add(r)
+        root[v] = r
+    span = np.ptp(xyz, axis=0).max() if n else 1.0
+    by_link = {}
+    for sl, ms, link in pairs:
+        by_link.setdefault(link, []).append(xyz[index[sl]] - xyz[index[ms]])
+    for d in by_link.values():
+        d = np.asarray(d)
+        if np.abs(d - d[0]).max() > 1e-9 * max(span, 1e-300):
+            raise ValueError("only translational periodic links are supported")
+    return root
+
+
 def read_msh(path_or_text, name=None, scale=(1.0, 1.0, 1.0)):
     """A processed ``meshgen.Mesh`` from an ASCII MSH 2.2 file (or its text)."""
     text = path_or_text
@@ -51,8 +103,6 @@ def read_msh(path_or_text, name=None, scale=(1.0, 1.0, 1.0)):
         raise ValueError(f"MSH format {fmt[0] if fmt else '?'} not supported (ASCII 2.2 only)")
     if len(fmt) > 1 and fmt[1] != "0":
         raise ValueError("binary MSH files are not supported")
-    if "Periodic" in sec:
-        raise ValueError("periodic Gmsh meshes are not supported")
     phys_names = {}
     for line in sec.get("PhysicalNames", [])[1:]:
         dim, tag, nm = line.split(maxsplit=2)
@@ -90,6 +140,19 @@ def read_msh(path_or_text, name=None, scale=(1.0, 1.0, 1.0)):
     if not cells:
         raise ValueError("no volume elements")
     cell_nodes = np.asarray(cells, dtype=np.int64)
+    shift = np.zeros(cell_nodes.shape + (3,))
+    if "Periodic" in sec:
+        root = _resolve_periodic(_periodic_links(sec["Periodic"]), index, xyz)
+        canon = root[cell_nodes]
+        shift = xyz[cell_nodes] - xyz[canon]
+        cell_nodes = canon
+        surf = [(t, [int(root[v]) for v in c]) for t, c in surf]
+        # surfaces that cover faces between two cells now are not boundaries
+        table = mg.HEX_FACES if cell_kind == "hex" else mg.TET_FACES
+        keys, counts = np.unique(np.sort(cell_nodes[:, table].reshape(-1, table.shape[1]), axis=1),
+                                 axis=0, return_counts=True)
+        single = {tuple(int(v) for v in k) for k in keys[counts == 1]}
+        surf = [(t, c) for t, c in surf if tuple(sorted(c)) in single]
     tags = sorted({t for t, _ in surf})
     region_of_tag = {t: r + 1 for r, t in enumerate(tags)}
     names = ["flow"] + [phys_names.get((2, t), f"boundary{t}") for t in tags]
@@ -105,16 +168,17 @@ def read_msh(path_or_text, name=None, scale=(1.0, 1.0, 1.0)):
             out[i] = r
         return out
 
-    shift = np.zeros(cell_nodes.shape + (3,))
     return mg.build_mesh(xyz, cell_nodes, shift, cell_kind,
                          boundary_region_of_nodes=regions if surf else None,
                          region_names=tuple(names), region_is_boundary=tuple([0] + [1] * len(tags)),
                          name=name or "gmsh")
 
 
-def write_msh(path, nodes, cell_nodes, cell_kind, boundary, phys_names):
-    """Write an ASCII MSH 2.2 file: nodes (n, 3), volume connectivity, and the
-    boundary surface elements as (physical tag, node list) pairs."""
+def write_msh(path, nodes, cell_nodes, cell_kind, boundary, phys_names, periodic=None):
+    """Write an ASCII MSH 2.2 file: nodes (n, 3), volume connectivity, the
+    boundary surface elements as (physical tag, node list) pairs, and
+    optionally periodic links, each a list of (slave node, master node)
+    pairs (0-based) related by one translation."""
     etype = 5 if cell_kind == "hex" else 4
     lines = ["$MeshFormat", "2.2 0 8", "$EndMeshFormat", "$PhysicalNames", str(len(phys_names))]
     for (dim, tag), nm in sorted(phys_names.items()):
@@ -133,5 +197,11 @@ def write_msh(path, nodes, cell_nodes, cell_kind, boundary, phys_names):
         lines.append(" ".join(str(v) for v in [eid, etype, 2, vol_tag, vol_tag] + [int(c) + 1 for c in conn]))
         eid += 1
     lines.append("$EndElements")
+    if periodic:
+        lines += ["$Periodic", str(len(periodic))]
+        for k, link in enumerate(periodic):
+            lines += [f"2 {2 * k + 1} {2 * k + 2}", str(len(link))]
+            lines += [f"{int(a) + 1} {int(b) + 1}" for a, b in link]
+        lines.append("$EndPeriodic")
     with open(path, "w") as f:
         f.write("\n".join(lines) + "\n")

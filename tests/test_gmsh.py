@@ -51,3 +51,121 @@ def test_rejects_unsupported(tmp_path):
     gmsh.write_msh(p, nodes, cn, "hex", bnd[1:], {(2, 1): "a", (2, 2): "b", (2, 3): "c"})
     with pytest.raises(ValueError, match="no physical surface"):
         gmsh.read_msh(p)
+
+
+def unwrap_to_lattice(nodes, cn, sh, dims, periodic):
+    """A periodic structured mesh (unique nodes + vertex shifts, as meshgen
+    builds it) as Gmsh writes one: every lattice node its own node, the
+    periodic surfaces linked slave -> master."""
+    nx, ny, nz = dims
+    mx, my, mz = (n + (0 if p else 1) for n, p in zip(dims, periodic))
+    lengths = [sh[..., a].max() for a in range(3)]
+    u = cn
+    k, j, i = u % mz, (u // mz) % my, u // (mz * my)
+    idx = [i + np.where(sh[..., 0] != 0, nx, 0), j + np.where(sh[..., 1] != 0, ny, 0),
+           k + np.where(sh[..., 2] != 0, nz, 0)]
+    full = (idx[0] * (ny + 1) + idx[1]) * (nz + 1) + idx[2]
+    I, J, K = np.meshgrid(np.arange(nx + 1), np.arange(ny + 1), np.arange(nz + 1), indexing="ij")
+    I, J, K = I.reshape(-1), J.reshape(-1), K.reshape(-1)
+    base = (np.minimum(I, mx - 1) * my + np.minimum(J, my - 1)) * mz + np.minimum(K, mz - 1)
+    wrap = [(I == nx) & periodic[0], (J == ny) & periodic[1], (K == nz) & periodic[2]]
+    base = ((np.where(wrap[0], 0, I) * my + np.where(wrap[1], 0, J)) * mz + np.where(wrap[2], 0, K))
+    lat = nodes[base] + np.stack([np.where(w, L, 0.0) for w, L in zip(wrap, lengths)], axis=1)
+    master_of = ((np.where(wrap[0], 0, I) * (ny + 1) + np.where(wrap[1], 0, J)) * (nz + 1)
+                 + np.where(wrap[2], 0, K))
+    links = [(int(a), int(b)) for a, b in zip(np.arange(lat.shape[0]), master_of) if a != b]
+    return lat, full, links
+
+
+def by_translation(lat, pairs):
+    """Group (slave, master) pairs into links of one translation each."""
+    out = {}
+    for a, b in pairs:
+        out.setdefault(tuple(np.round(lat[a] - lat[b], 9)), []).append((a, b))
+    return list(out.values())
+
+
+def test_periodic_channel_matches_generator(tmp_path):
+    """z-periodic channel: the periodic surfaces' physical group gets no
+    region, the z faces join the cells across the period as the generator's
+    periodic faces do."""
+    nx, ny, nz = 6, 4, 4
+    ref = mg.channel(nx, ny, nz)
+    xs = np.linspace(0, 2, nx + 1)
+    ys = mg.stretched_coords(ny, 1.0, 1.1)
+    zs = np.linspace(0, 1, nz + 1)
+    nodes, cn, sh = mg._structured(nx, ny, nz, xs, ys, zs, (False, False, True), 0.0, 0, (2.0, 1.0, 1.0))
+    lat, full, links = unwrap_to_lattice(nodes, cn, sh, (nx, ny, nz), (False, False, True))
+    count = {}
+    for c in range(full.shape[0]):
+        for lf in mg.HEX_FACES:
+            key = tuple(sorted(full[c, lf]))
+            count.setdefault(key, [0, full[c, lf]])[0] += 1
+
+    def tag(x):
+        if abs(x[0]) < 1e-12:
+            return 1
+        if abs(x[0] - 2.0) < 1e-12:
+            return 2
+        return 5 if (abs(x[2]) < 1e-12 or abs(x[2] - 1.0) < 1e-12) else 3
+
+    bnd = [(tag(lat[list(k)].mean(axis=0)), list(v[1])) for k, v in count.items() if v[0] == 1]
+    p = os.path.join(tmp_path, "pchannel.msh")
+    gmsh.write_msh(p, lat, full, "hex", bnd,
+                   {(2, 1): "inflow", (2, 2): "outlet", (2, 3): "wall", (2, 5): "periodic-z", (3, 4): "fluid"},
+                   periodic=by_translation(lat, links))
+    m = gmsh.read_msh(p)
+    assert m.region_names == ["flow", "inflow", "outlet", "wall"]
+    for f in ("face_cells", "cell_faces", "boundary_id", "boundary_face", "face_boundary"):
+        assert np.array_equal(getattr(m, f), getattr(ref, f)), f
+    for f in ("cell_x", "cell_volume", "cell_dx", "face_x", "face_n", "face_area", "face_lambda",
+              "face_dist_cell_2"):
+        assert np.allclose(getattr(m, f), getattr(ref, f), rtol=0, atol=1e-14), f
+
+
+@pytest.mark.parametrize("kind", ["hex", "tet"])
+def test_fully_periodic_box_matches_generator(tmp_path, kind):
+    """Jittered periodic hex box / Kuhn tet box (links along all three axes,
+    edge and corner nodes reached through chains of links)."""
+    n = 4
+    xs = np.linspace(0.0, 1.0, n + 1)
+    jit = 0.1 if kind == "hex" else 0.0
+    nodes, cn, sh = mg._structured(n, n, n, xs, xs, xs, (True, True, True), jit, 20240601, (1.0, 1.0, 1.0))
+    lat, full, links = unwrap_to_lattice(nodes, cn, sh, (n, n, n), (True, True, True))
+    # chains: link each slave to a node that is itself a slave where possible
+    I = np.arange(lat.shape[0])
+    k, j, i = I % (n + 1), (I // (n + 1)) % (n + 1), I // ((n + 1) ** 2)
+    chained = []
+    for a, b in links:
+        if i[a] == n and (j[a] == n or k[a] == n):
+            b = int(a - n * (n + 1) ** 2)            # only x unwrapped: a slave of the y/z links
+        chained.append((a, b))
+    if kind == "hex":
+        ref = mg.periodic_hex_box(n, jitter=jit)
+        cells = full
+    else:
+        ref = mg.periodic_tet_box(n)
+        cells = full[:, mg.KUHN_TETS].reshape(-1, 4)
+    p = os.path.join(tmp_path, "box.msh")
+    gmsh.write_msh(p, lat, cells, kind, [], {(3, 1): "fluid"}, periodic=by_translation(lat, chained))
+    m = gmsh.read_msh(p)
+    assert m.region_names == ["flow"] and m.n_boundaries == 0
+    for f in ("face_cells", "cell_faces"):
+        assert np.array_equal(getattr(m, f), getattr(ref, f)), f
+    for f in ("cell_x", "cell_volume", "cell_dx", "face_x", "face_n", "face_area", "face_lambda",
+              "face_dist_cell_2"):
+        assert np.allclose(getattr(m, f), getattr(ref, f), rtol=0, atol=1e-13), f
+
+
+def test_rejects_rotational_periodic_links(tmp_path):
+    nx, ny, nz = 2, 2, 2
+    xs = np.linspace(0, 1, 3)
+    nodes, cn, sh = mg._structured(nx, ny, nz, xs, xs, xs, (False, False, True), 0.0, 0, (1.0, 1.0, 1.0))
+    lat, full, links = unwrap_to_lattice(nodes, cn, sh, (nx, ny, nz), (False, False, True))
+    links = [(a, b) for a, b in links]
+    a, b = links[0]
+    links[0] = (a, b + 1)                              # not the common translation
+    p = os.path.join(tmp_path, "rot.msh")
+    gmsh.write_msh(p, lat, full, "hex", [], {(3, 1): "fluid"}, periodic=[links])
+    with pytest.raises(ValueError, match="translational"):
+        gmsh.read_msh(p)

@@ -86,13 +86,15 @@ class NewtonStats(C.Structure):
 
 EXACT_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_double))
 ITERATION_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_double, C.c_double, C.POINTER(C.c_double), C.c_int)
+OUTPUT_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_double)
 
 
 class TimedOpts(C.Structure):
     _fields_ = [("implicit", C.c_int), ("scheme", C.c_int), ("max_iter", C.c_int), ("is_transient", C.c_int),
                 ("abort_residual", C.c_double), ("t_start", C.c_double), ("t_end", C.c_double),
                 ("cfl", C.c_double), ("max_iter_inner", C.c_int), ("on_iteration", ITERATION_FN),
-                ("user", C.c_void_p)]
+                ("user", C.c_void_p), ("iter_start", C.c_int), ("i_output_data", C.c_int),
+                ("on_output", OUTPUT_FN)]
 
 
 class TimedStats(C.Structure):
@@ -125,6 +127,9 @@ EXPORTS = {
     "fv3d_set_state": ([C.c_void_p, _f8p], C.c_int),
     "fv3d_get_state": ([C.c_void_p, _f8p], C.c_int),
     "fv3d_get_conserved": ([C.c_void_p, _f8p], C.c_int),
+    "fv3d_get_time_derivative": ([C.c_void_p, _f8p], C.c_int),
+    "fv3d_get_bdf_history": ([C.c_void_p, C.c_int, _f8p, C.POINTER(C.c_int)], C.c_int),
+    "fv3d_set_bdf_history": ([C.c_void_p, C.c_int, C.c_int, _f8p], C.c_int),
     "fv3d_time_derivative": ([C.c_void_p, C.c_double, _f8p], C.c_int),
     "fv3d_timestep": ([C.c_void_p, C.c_double, _f8p], C.c_int),
     "fv3d_step_explicit": ([C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double,
@@ -245,6 +250,33 @@ class Solver:
         self._check(self.lib.fv3d_get_conserved(self.h, _p(out, _f8p)))
         return out
 
+    def get_time_derivative(self):
+        """phi_dt (n_cells, 5) of the last residual evaluation."""
+        out = np.empty((self.nc, 5))
+        self._check(self.lib.fv3d_get_time_derivative(self.h, _p(out, _f8p)))
+        return out
+
+    def bdf_history(self):
+        """The implicit step's phi_old stages, a list of (n_cells, 5) arrays
+        (empty before the first implicit step)."""
+        n = C.c_int()
+        self._check(self.lib.fv3d_get_bdf_history(self.h, 0, None, C.byref(n)))
+        out = []
+        for k in range(n.value):
+            a = np.empty((self.nc, 5))
+            self._check(self.lib.fv3d_get_bdf_history(self.h, k, _p(a, _f8p), None))
+            out.append(a)
+        return out
+
+    def set_bdf_history(self, scheme, stages):
+        """Restart history: `stages` the phi_old arrays of `scheme` (euler: 1,
+        bdf2: 2), after set_state with the restart state."""
+        a = np.ascontiguousarray(np.stack([np.asarray(x, dtype=np.float64) for x in stages]))
+        if a.shape[1:] != (self.nc, 5):
+            raise ValueError(f"history stages must have shape ({self.nc}, 5)")
+        self._check(self.lib.fv3d_set_bdf_history(self.h, {"euler": 0, "bdf2": 1}[scheme], a.shape[0],
+                                                  _p(a, _f8p)))
+
     def permutation(self):
         out = np.empty(self.nc, dtype=np.int32)
         self._check(self.lib.fv3d_get_permutation(self.h, _p(out, _i4p)))
@@ -334,20 +366,35 @@ class Solver:
         self._check(self.lib.fv3d_set_exact_function(self.h, f, None, id_, t))
 
     def timedisc(self, scheme="rk33", implicit=False, max_iter=1000, is_transient=True, abort_residual=1e-10,
-                 t_start=0.0, t_end=0.2, cfl=0.5, max_iter_inner=100, check=True):
+                 t_start=0.0, t_end=0.2, cfl=0.5, max_iter_inner=100, check=True, iter_start=0,
+                 i_output_data=0, on_output=None):
         """timedisc (timedisc.c:134-222): returns the final stats and the
-        per-iteration rows (iter, t, dt, res[5], n_inner) print_residual prints."""
+        per-iteration rows (iter, t, dt, res[5], n_inner) print_residual prints.
+        on_output(iter, t) is called where the reference calls write_output
+        (i_output_data: -1 first and last, 0 never, k > 0 also every k-th);
+        iter_start > 0 continues a restart."""
         rows = []
 
         def on_iter(_user, it, t, dt, res, n_inner):
             rows.append((it, t, dt, [res[j] for j in range(5)], n_inner))
 
+        errors = []
+
+        def on_out(_user, it, t):
+            try:
+                on_output(it, t)
+            except Exception as e:      # no exception may cross the C frames
+                errors.append(e)
+
         cb = ITERATION_FN(on_iter)
+        ocb = OUTPUT_FN(on_out) if on_output is not None else OUTPUT_FN()
         sch = {"euler": 0, "bdf2": 1}[scheme] if implicit else SCHEMES[scheme]
         o = TimedOpts(int(implicit), sch, max_iter, int(is_transient), abort_residual, t_start, t_end, cfl,
-                      max_iter_inner, cb, None)
+                      max_iter_inner, cb, None, iter_start, i_output_data, ocb)
         st = TimedStats()
         rc = self.lib.fv3d_timedisc(self.h, C.byref(o), C.byref(st))
+        if errors:
+            raise errors[0]
         if check:
             self._check(rc)
         return {"iter": st.iter, "t": st.t, "dt": st.dt, "res": list(st.res), "stop_reason": st.stop_reason,

@@ -558,6 +558,24 @@ static fv3d_status export_soa(Ctx* ctx, const double* src, int m, int with_prims
   return FV3D_OK;
 }
 
+fv3d_status fv3d::export_rows(Ctx& c, const double* src, double* rows) {
+  Ctx* ctx = &c;
+  CK(cudaSetDevice(ctx->cfg.device));
+  return export_soa(ctx, src, 5, 0, rows);
+}
+
+fv3d_status fv3d::import_rows(Ctx& c, const double* rows, double* dst) {
+  Ctx* ctx = &c;
+  CK(cudaSetDevice(ctx->cfg.device));
+  CK(cudaMemcpyAsync(ctx->d_stage.p, rows, sizeof(double) * 5 * (size_t)ctx->nc, cudaMemcpyHostToDevice,
+                     ctx->stream));
+  k_import<<<nblk(ctx->nc), 256, 0, ctx->stream>>>(ctx->nc, ctx->d_perm.p, ctx->d_stage.p, dst, nullptr, nullptr,
+                                                  ctx->phys.km1, ctx->cfg.R_mix);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(ctx->stream));
+  return FV3D_OK;
+}
+
 extern "C" fv3d_status fv3d_set_exact_function(fv3d_ctx* handle, fv3d_exact_fn fn, void* user, int id, double t) {
   if (handle == nullptr || fn == nullptr) return FV3D_ERR_INVALID_ARG;
   Ctx* ctx = reinterpret_cast<Ctx*>(handle);
@@ -586,6 +604,14 @@ extern "C" fv3d_status fv3d_get_conserved(fv3d_ctx* handle, double* u) {
   if (!ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "no state set");
   CK(cudaSetDevice(ctx->cfg.device));
   return export_soa(ctx, ctx->d_U.p, 5, 0, u);
+}
+
+extern "C" fv3d_status fv3d_get_time_derivative(fv3d_ctx* handle, double* phi_dt) {
+  if (handle == nullptr || phi_dt == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (!ctx->residual_valid) return ctx->fail(FV3D_ERR_STATE, "no time derivative evaluated");
+  CK(cudaSetDevice(ctx->cfg.device));
+  return export_soa(ctx, ctx->d_dphi.p, 5, 0, phi_dt);
 }
 
 // ---------------------------------------------------------------------------
@@ -878,6 +904,7 @@ extern "C" fv3d_status fv3d_timedisc(fv3d_ctx* handle, const fv3d_timedisc_opts*
                       : (o->scheme >= 0 && o->scheme <= 3),
           FV3D_ERR_INVALID_ARG, "bad scheme %d", o->scheme);
   REQUIRE(o->max_iter >= 1, FV3D_ERR_INVALID_ARG, "max_iter must be >= 1");
+  REQUIRE(o->iter_start >= 0, FV3D_ERR_INVALID_ARG, "iter_start must be >= 0");
   fv3d_status st = check_ready(ctx);
   if (st != FV3D_OK) return st;
   if (!ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "no state set");
@@ -886,14 +913,27 @@ extern "C" fv3d_status fv3d_timedisc(fv3d_ctx* handle, const fv3d_timedisc_opts*
   const double t_end = o->is_transient ? o->t_end : DBL_MAX;
   double t = o->t_start, dt = 0.0;
   double res[5] = {0, 0, 0, 0, 0};
-  int iter = 0, reason = 0, n_inner = 0;
+  int iter = o->iter_start, reason = 0, n_inner = 0;
   bool finalize = false;
+  const bool output = o->on_output != nullptr && o->i_output_data != 0;
+  if (output && o->iter_start == 0) {
+    // finite_volume_time_derivative(t) then write_output(0, t)
+    if ((st = fv3d_time_derivative(handle, t, nullptr)) != FV3D_OK) return st;
+    o->on_output(o->user, 0, t);
+  }
   const bool dev_dt = !o->implicit && o->cfl > 0.0;
+  // calc_ns_timestep as written after a low-storage step sees the reference's
+  // phi_total: new density, the last stage's input u, v, w, p
+  // (timestep_lserkw2 updates only the conserved entries, explicit.c:136-139).
+  // Its convective bound is the one the last stage fuses (the graph runs it
+  // with CFL 1); the viscous bound needs only the new density.
+  const bool fused_lc = !o->implicit && o->cfl <= 0.0 && o->scheme != FV3D_SSP_RK3;
   cudaGraphExec_t exec = nullptr;
   if (!o->implicit) {
-    if ((st = step_graph(ctx, o->scheme, o->cfl, true, &exec)) != FV3D_OK) return st;
+    if ((st = step_graph(ctx, o->scheme, fused_lc ? 1.0 : o->cfl, true, &exec)) != FV3D_OK) return st;
     DevScalars h0{};
     h0.t = t;
+    h0.lam_bits = 0x7ff0000000000000ull;  // +inf: the fused bound mins into it
     CK(cudaMemcpyAsync(ctx->d_sc.p, &h0, sizeof(h0), cudaMemcpyHostToDevice, ctx->stream));
     if (dev_dt) {  // first dt from the initial state; later ones from each step's last stage
       if ((st = reduce_step_bound(ctx)) != FV3D_OK) return st;
@@ -911,6 +951,19 @@ extern "C" fv3d_status fv3d_timedisc(fv3d_ctx* handle, const fv3d_timedisc_opts*
       CK(cudaStreamSynchronize(ctx->stream));
       if (hs.status & 1) return ctx->fail(FV3D_ERR_NONFINITE, "non-finite state or time step at iteration %d", iter);
       dt = hs.dt;
+    } else if (fused_lc && iter > o->iter_start) {
+      CK(cudaMemcpyAsync(&hs, ctx->d_sc.p, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
+      if ((st = reduce_timestep(ctx, true)) != FV3D_OK) return st;
+      unsigned long long bits[2];
+      CK(cudaMemcpyAsync(bits, ctx->d_bits.p, sizeof(bits), cudaMemcpyDeviceToHost, ctx->stream));
+      CK(cudaStreamSynchronize(ctx->stream));
+      if (hs.status & 1) return ctx->fail(FV3D_ERR_NONFINITE, "non-finite state or time step at iteration %d", iter);
+      double lv;
+      memcpy(&lv, &bits[1], 8);
+      // navier_stokes.c:186-192
+      const double lc = hs.dt * ctx->cfg.cfl_scale;
+      lv *= ctx->cfg.dfl_scale * ctx->cfg.mu_mix * ctx->kappa_pr * lv;
+      dt = (lc < lv) ? lc : lv;
     } else {
       if ((st = fv3d_timestep(handle, o->cfl, &dt)) != FV3D_OK) return st;
     }
@@ -952,11 +1005,13 @@ extern "C" fv3d_status fv3d_timedisc(fv3d_ctx* handle, const fv3d_timedisc_opts*
       finalize = true;
       reason = 1;
     }
-    if (iter >= o->max_iter && !finalize) {
+    const bool cadence = o->i_output_data > 0 && iter % o->i_output_data == 0;
+    if (iter >= o->iter_start + o->max_iter && !finalize) {
       finalize = true;
       reason = 2;
     }
     if (o->on_iteration) o->on_iteration(o->user, iter, t, dt, res, n_inner);
+    if (output && (finalize || cadence)) o->on_output(o->user, iter, t);
     if (finalize) break;
   }
   if (!o->implicit) {

@@ -103,5 +103,9 @@ fv3d_status prepare_mesh(Ctx& ctx, const fv3d_mesh_arrays& m);
 fv3d_status upload_mesh(Ctx& ctx);
 fv3d_status ensure_fp64_path(Ctx& ctx);
 fv3d_status ensure_mixed_path(Ctx& ctx);
+// a [5][nc] FP64 device array from / to n_cells rows of 5 in reference order
+// (host memory; synchronous)
+fv3d_status import_rows(Ctx& ctx, const double* rows, double* dst);
+fv3d_status export_rows(Ctx& ctx, const double* src, double* rows);
 
 }  // namespace fv3d

@@ -1066,19 +1066,44 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
   return FV3D_OK;
 }
 
-// timestep_newton (implicit.c:224-351): U is the state Y; R(U) the FP64
-// time derivative; ten perturbed residuals build the lumped blocks each
-// Newton iteration; the block-diagonal system is solved cell by cell
-fv3d_status Implicit::step_newton(Ctx& ctx, const fv3d_newton_opts& o, int iter, double t, double dt,
-                                  fv3d_newton_stats* stats) {
-  (void)t;  // the implemented boundary conditions do not depend on time
+fv3d_status Implicit::newton_buffers(Ctx& ctx) {
   fv3d_status st = ensure_fp64_path(ctx);
   if (st == FV3D_OK) st = setup(ctx, 1);
   if (st != FV3D_OK) return st;
   cudaError_t e = cudaSuccess;
   for (DevBuf<double>* b : {&old0, &old1, &dYdt, &fY})
     if (e == cudaSuccess && b->n < n) e = b->alloc(n);
-  if ((st = ctx.cuda(e, "implicit step allocation")) != FV3D_OK) return st;
+  return ctx.cuda(e, "implicit step allocation");
+}
+
+// read_restart_data's phi_old (restart.c:50-178) and the time derivative of
+// the restart state (the file's phi_dt)
+fv3d_status Implicit::set_history(Ctx& ctx, int scheme, int n_stages, const double* rows) {
+  const int want = (scheme == FV3D_NEWTON_EULER) ? 1 : 2;
+  if (n_stages != want)
+    return ctx.fail(FV3D_ERR_INVALID_ARG, "%d history stages for a scheme that keeps %d", n_stages, want);
+  fv3d_status st = newton_buffers(ctx);
+  if (st != FV3D_OK) return st;
+  ICK(cudaMemsetAsync(old1.p, 0, sizeof(double) * n, ctx.stream));
+  if ((st = import_rows(ctx, rows, old0.p)) != FV3D_OK) return st;
+  if (n_stages > 1 && (st = import_rows(ctx, rows + 5 * (size_t)ctx.nc, old1.p)) != FV3D_OK) return st;
+  if ((st = residual64(ctx, ctx.d_U.p, dYdt.p)) != FV3D_OK) return st;
+  ICK(cudaStreamSynchronize(ctx.stream));
+  n_bdf = want;
+  newton_ready = true;
+  return FV3D_OK;
+}
+
+// timestep_newton (implicit.c:224-351): U is the state Y; R(U) the FP64
+// time derivative; ten perturbed residuals build the lumped blocks each
+// Newton iteration; the block-diagonal system is solved cell by cell
+fv3d_status Implicit::step_newton(Ctx& ctx, const fv3d_newton_opts& o, int iter, double t, double dt,
+                                  fv3d_newton_stats* stats) {
+  (void)t;  // the implemented boundary conditions do not depend on time
+  if (!newton_ready && iter >= 1 && o.scheme == FV3D_NEWTON_BDF2)
+    return ctx.fail(FV3D_ERR_STATE, "BDF2 step at iteration %d without the history of the steps before it", iter);
+  fv3d_status st = newton_buffers(ctx);
+  if (st != FV3D_OK) return st;
   const int grid = std::min(4096, blocks(n));
   double* U = ctx.d_U.p;
   if (!newton_ready || iter == 0) {
@@ -1230,4 +1255,29 @@ extern "C" fv3d_status fv3d_step_newton(fv3d_ctx* handle, const fv3d_newton_opts
   if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "cudaSetDevice");
   if (!ctx->implicit) ctx->implicit = new Implicit();
   return ctx->implicit->step_newton(*ctx, *opts, iter, t, dt, stats);
+}
+
+extern "C" fv3d_status fv3d_get_bdf_history(fv3d_ctx* handle, int stage, double* phi_old, int* n_stages) {
+  if (handle == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  const Implicit* im = ctx->implicit;
+  const int ns = (im != nullptr && im->newton_ready) ? im->n_bdf : 0;
+  if (n_stages != nullptr) *n_stages = ns;
+  if (phi_old == nullptr) return FV3D_OK;
+  if (stage < 0 || stage >= ns) return ctx->fail(FV3D_ERR_INVALID_ARG, "history stage %d of %d", stage, ns);
+  return export_rows(*ctx, stage == 0 ? im->old0.p : im->old1.p, phi_old);
+}
+
+extern "C" fv3d_status fv3d_set_bdf_history(fv3d_ctx* handle, int scheme, int n_stages, const double* phi_old) {
+  if (handle == nullptr || phi_old == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (!ctx->mesh_ready || !ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "mesh and state required");
+  if (scheme != FV3D_NEWTON_EULER && scheme != FV3D_NEWTON_BDF2)
+    return ctx->fail(FV3D_ERR_INVALID_ARG, "bad implicit scheme %d", scheme);
+  for (int b = 0; b < ctx->nb; ++b)
+    if (!(ctx->region_set & (1u << ctx->h_fregion[b])))
+      return ctx->fail(FV3D_ERR_STATE, "boundary region %d has no condition", ctx->h_fregion[b]);
+  if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "cudaSetDevice");
+  if (!ctx->implicit) ctx->implicit = new Implicit();
+  return ctx->implicit->set_history(*ctx, scheme, n_stages, phi_old);
 }

@@ -83,6 +83,8 @@ struct Implicit {
   bool newton_ready = false;
   fv3d_status step_newton(Ctx& ctx, const fv3d_newton_opts& o, int iter, double t, double dt,
                           fv3d_newton_stats* stats);
+  fv3d_status newton_buffers(Ctx& ctx);
+  fv3d_status set_history(Ctx& ctx, int scheme, int n_stages, const double* rows);
 };
 
 }  // namespace fv3d

@@ -11,9 +11,11 @@ Keys follow the reference's parameter paths:
   TimeDisc/{timestep, max_iter, transient, abort_residual, t_start, t_end}
       (timedisc.c:64-80), TimeDisc/Explicit/scheme (explicit.c:47-60),
       TimeDisc/Implicit/{scheme, max_iter_inner, ...} (implicit.c:77-112)
-  Mesh/mesh_file, Output/i_output_data, Restart/use_restart
-HDF5 mesh and restart files cannot be read in this build (no HDF5 library):
-the mesh is passed in (``meshgen`` / ``gmsh``), and use_restart is rejected.
+  Mesh/mesh_file, Output/i_output_data (output.c:20-23),
+  Restart/{use_restart, restart_file} (restart.c:20-30)
+HDF5 files cannot be read or written in this build (no HDF5 library): the
+mesh is passed in (``meshgen`` / ``gmsh``), and output / restart files are the
+NumPy containers of ``output`` with the same datasets.
 """
 from __future__ import annotations
 
@@ -70,7 +72,9 @@ class Simulation:
     t_start: float
     t_end: float
     max_iter_inner: int = 100
-    i_output_data: int = 0
+    i_output_data: int = -1
+    use_restart: bool = False
+    restart_file: str = ""
     extra: dict = field(default_factory=dict)
 
     def regions(self, mesh):
@@ -128,8 +132,10 @@ def load_simulation(src) -> Simulation:
             raise ValueError("the 'function' boundary type is not supported (the reference cannot configure it)")
         prim = [float(b.get(k, 0.0)) for k in ("u", "v", "w", "p", "T")]
         boundaries[name] = (t, tuple(prim))
-    if _get(tree, "Restart/use_restart", False):
-        raise ValueError("restart files are HDF5: not supported in this build")
+    use_restart = bool(_get(tree, "Restart/use_restart", False))
+    restart_file = str(_get(tree, "Restart/restart_file", ""))
+    if use_restart and restart_file.endswith(".h5"):
+        raise ValueError("HDF5 restart files cannot be read in this build: give the .npz output file")
     implicit = _pick({"Explicit": False, "Implicit": True}, _get(tree, "TimeDisc/timestep", "Explicit"), "timestep")
     if implicit:
         scheme = _pick(IMPLICIT, _get(tree, "TimeDisc/Implicit/scheme", "Euler"), "implicit scheme")
@@ -142,19 +148,39 @@ def load_simulation(src) -> Simulation:
                       transient=bool(_get(tree, "TimeDisc/transient", True)),
                       abort_residual=float(_get(tree, "TimeDisc/abort_residual", 1e-10)),
                       t_start=float(_get(tree, "TimeDisc/t_start", 0.0)), t_end=float(_get(tree, "TimeDisc/t_end", 0.2)),
-                      max_iter_inner=int(inner), i_output_data=int(_get(tree, "Output/i_output_data", 0)))
+                      max_iter_inner=int(inner), i_output_data=int(_get(tree, "Output/i_output_data", -1)),
+                      use_restart=use_restart, restart_file=restart_file)
 
 
-def run(sim: Simulation, mesh, precision="fp64", cfl=0.0, check=True):
+def run(sim: Simulation, mesh, precision="fp64", cfl=0.0, check=True, output_dir=None):
     """The reference's program flow on the GPU: set up the solver from the
-    parameters, set_solution, timedisc.  cfl <= 0 takes calc_ns_timestep as
-    written (cfl_scale, dfl_scale), as the reference does; returns the
-    final conserved state, the timedisc stats and the residual rows."""
-    from . import api
+    parameters, set_solution (or read_restart_data), timedisc with
+    write_output into output_dir (None: no files).  cfl <= 0 takes
+    calc_ns_timestep as written (cfl_scale, dfl_scale), as the reference
+    does; returns the final conserved state, the timedisc stats, the
+    residual rows and the output files written."""
+    from . import api, output
     rt, rp = sim.regions(mesh)
+    written = []
     with api.Solver(mesh, sim.params, rt, rp, precision) as s:
-        s.set_state(sim.initial_state(mesh))
+        iter_start, t_start = 0, sim.t_start
+        if sim.use_restart:
+            r = output.read_restart(sim.restart_file)
+            if r["phi_total"].shape != (mesh.n_cells, 10):
+                raise ValueError("restart file does not match the mesh")
+            s.set_state(r["phi_total"][:, :5])
+            iter_start, t_start = r["iter"], r["t"]
+            if sim.implicit and r["phi_old"]:
+                s.set_bdf_history(sim.scheme, r["phi_old"])
+        else:
+            s.set_state(sim.initial_state(mesh))
+
+        def on_output(it, t):
+            written.append(output.write_output(s, sim.title, it, t, output_dir))
+
         st, rows = s.timedisc(sim.scheme, implicit=sim.implicit, max_iter=sim.max_iter, is_transient=sim.transient,
-                              abort_residual=sim.abort_residual, t_start=sim.t_start, t_end=sim.t_end, cfl=cfl,
-                              max_iter_inner=sim.max_iter_inner, check=check)
-        return s.get_conserved(), st, rows
+                              abort_residual=sim.abort_residual, t_start=t_start, t_end=sim.t_end, cfl=cfl,
+                              max_iter_inner=sim.max_iter_inner, check=check, iter_start=iter_start,
+                              i_output_data=sim.i_output_data if output_dir is not None else 0,
+                              on_output=on_output if output_dir is not None else None)
+        return s.get_conserved(), st, rows, written

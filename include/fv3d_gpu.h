@@ -148,6 +148,9 @@ fv3d_status fv3d_set_exact_function(fv3d_ctx *ctx, fv3d_exact_fn fn, void *user,
  * u, v, w, p, T (navier_stokes.c:107-117) */
 fv3d_status fv3d_get_state(fv3d_ctx *ctx, double *phi_total);
 fv3d_status fv3d_get_conserved(fv3d_ctx *ctx, double *u_con);
+/* phi_dt [n_cells*5] of the last residual evaluation, in reference order:
+ * the time derivative write_output stores (output.c:92-191) */
+fv3d_status fv3d_get_time_derivative(fv3d_ctx *ctx, double *phi_dt);
 
 /* ---- hot path ---------------------------------------------------------------- */
 /* finite_volume_time_derivative (finite_volume.c:81-124): phi_dt [n_cells*5] */
@@ -241,9 +244,22 @@ typedef struct {
     int n_inner;         /* Newton iterations taken (the reference's n_inner) */
     double err0, err;    /* ||f_Y|| before and after */
 } fv3d_newton_stats;
-/* FV3D_ERR_NOT_CONVERGED when it reaches max_iter_inner, as the reference */
+/* FV3D_ERR_NOT_CONVERGED when it reaches max_iter_inner, as the reference.
+ * A BDF2 step with iter >= 1 needs the history of the steps before it (a
+ * run started at iter 0, or fv3d_set_bdf_history): FV3D_ERR_STATE otherwise. */
 fv3d_status fv3d_step_newton(fv3d_ctx *ctx, const fv3d_newton_opts *opts, int iter, double t,
                              double dt, fv3d_newton_stats *stats);
+/* The implicit step's history phi_old (implicit.c:241-250), write_output's
+ * phi_old:<stage> datasets: *n_stages = 1 (backward Euler) or 2 (BDF2), 0
+ * before the first implicit step; phi_old [n_cells*5] of stage < *n_stages in
+ * reference order (phi_old NULL: the count only). */
+fv3d_status fv3d_get_bdf_history(fv3d_ctx *ctx, int stage, double *phi_old, int *n_stages);
+/* read_restart_data's history (restart.c:50-178): n_stages (1 for backward
+ * Euler, 2 for BDF2) arrays phi_old [n_stages*n_cells*5], stage-major, for a
+ * run that fv3d_timedisc continues with iter_start > 0.  Call after
+ * fv3d_set_state with the restart state: the next step's dY/dt, which the
+ * reference takes from the file's phi_dt, is evaluated from that state. */
+fv3d_status fv3d_set_bdf_history(fv3d_ctx *ctx, int scheme, int n_stages, const double *phi_old);
 
 /* ---- time loop ----------------------------------------------------------------- */
 /* timedisc (timedisc.c:134-222) with init_timedisc's options (timedisc.c:45-66):
@@ -259,6 +275,13 @@ fv3d_status fv3d_step_newton(fv3d_ctx *ctx, const fv3d_newton_opts *opts, int it
  * FV3D_ERR_NONFINITE here; the reference loops on without advancing. */
 typedef void (*fv3d_iteration_fn)(void *user, int iter, double t, double dt, const double res[5],
                                   int n_inner);
+/* called where timedisc calls write_output (timedisc.c:155-156, 210-216):
+ * before the first iteration of a run that is not a restart, and after each
+ * iteration that print_residual marks ('*': the last one, and every
+ * i_output_data-th when i_output_data > 0).  It may read the datasets
+ * write_output stores from the same context: fv3d_get_state (phi_total),
+ * fv3d_get_time_derivative (phi_dt), fv3d_get_bdf_history (phi_old:<k>). */
+typedef void (*fv3d_output_fn)(void *user, int iter, double t);
 typedef struct {
     int implicit;           /* 0: explicit (timestep_lserkw2 / SSP-RK3), 1: implicit (timestep_newton) */
     int scheme;             /* explicit: FV3D_RK_*, FV3D_SSP_RK3; implicit: a fv3d_newton_scheme value */
@@ -269,7 +292,10 @@ typedef struct {
     double cfl;             /* see above */
     int max_iter_inner;     /* implicit */
     fv3d_iteration_fn on_iteration;
-    void *user;
+    void *user;             /* passed to on_iteration and on_output */
+    int iter_start;         /* read_restart_data's iter for a restart (t_start its t), else 0 */
+    int i_output_data;      /* Output/i_output_data: -1 first and last, 0 none, k > 0 also every k-th */
+    fv3d_output_fn on_output;  /* may be NULL */
 } fv3d_timedisc_opts;
 typedef struct {
     int iter;               /* iterations taken */

@@ -23,7 +23,9 @@ def oracle_timedisc(c, scheme, t_end, max_iter, is_transient, abort, cfl, implic
     t, it, rows = 0.0, 0, []
     o.time_derivative(t)
     while True:
-        dt = o.timestep_convective(cfl)
+        # cfl <= 0: calc_ns_timestep as written (on the oracle's phi_total,
+        # whose primitives after a low-storage step are the last stage's input)
+        dt = o.timestep_convective(cfl) if cfl > 0 else o.calc_ns_timestep()
         fin = False
         if t + dt > t_end:
             dt, fin = t_end - t, True
@@ -31,6 +33,8 @@ def oracle_timedisc(c, scheme, t_end, max_iter, is_transient, abort, cfl, implic
             ni, _ = o.step_newton(it, t, dt, scheme={"euler": 0, "bdf2": 1}[scheme], solver=1, max_iter_inner=20,
                                   tolerance_lsoe=1e-12, max_iter_lsoe=200, krylov_dims=30, krylov_restarts=10,
                                   is_transient=is_transient)
+        elif scheme == "ssprk3":
+            o.step_ssprk3(t, dt)
         else:
             o.step_lserkw2(SCHEME_ID[scheme], it, t, dt)
         res = o.global_residual(dt)
@@ -109,3 +113,76 @@ def test_implicit_transient(scheme):
     assert st["stop_reason"] == 2 and len(rows) == 4
     compare(rows, rows_ref, 1e-9)
     assert rel_l2(u, u_ref).max() < 1e-10
+
+
+@pytest.mark.parametrize("case,scheme", [("hex4", "rk33"), ("hex4", "rk45"), ("channel", "rk33"), ("hex4", "ssprk3")])
+def test_calc_ns_timestep_as_written(case, scheme):
+    """cfl <= 0: each iteration's dt is calc_ns_timestep on the reference's
+    phi_total.  On the hexes the convective bound decides (after a low-storage
+    step it sees the new density with the last stage's input u, v, w, p); on
+    the channel the viscous bound (new density only)."""
+    c = cases.tgv_hex(4) if case == "hex4" else cases.channel(6, 4, 4)
+    rows_ref, u_ref = oracle_timedisc(c, scheme, 1e9, 6, True, 0.0, 0.0)
+    with api.from_case(c, "fp64") as s:
+        st, rows = s.timedisc(scheme, max_iter=6, is_transient=True, t_end=1e9, cfl=0.0)
+        u = s.get_conserved()
+    assert st["stop_reason"] == 2 and len(rows) == 6
+    compare(rows, rows_ref, 1e-10)
+    assert rel_l2(u, u_ref).max() < 1e-10
+
+
+def test_output_cadence():
+    """on_output where timedisc calls write_output: iteration 0 (after the
+    initial time derivative), every i_output_data-th, the last; none on a
+    restart; the datasets readable from the callback."""
+    c = cases.tgv_hex(4)
+    o = orc.Oracle("restated")
+    o.init(c.mesh, c.params, c.region_type, c.region_prim)
+    o.set_conserved(c.u0)
+    r0 = o.time_derivative(0.0)
+    with api.from_case(c, "fp64") as s:
+        for every, expect in ((2, [0, 2, 4, 5]), (-1, [0, 5]), (0, [])):
+            s.set_state(c.u0)
+            seen = []
+
+            def out(it, t):
+                seen.append((it, t, s.get_state(), s.get_time_derivative()))
+
+            st, rows = s.timedisc("rk33", max_iter=5, is_transient=True, t_end=1e9, cfl=0.5,
+                                  i_output_data=every, on_output=out)
+            assert [x[0] for x in seen] == expect
+            if seen:
+                assert seen[0][1] == 0.0 and rel_l2(seen[0][3], r0).max() < 1e-12
+                assert abs(seen[-1][1] - st["t"]) == 0.0
+                assert np.array_equal(seen[-1][2][:, :5], s.get_conserved())
+        seen = []
+        s.timedisc("rk33", max_iter=3, is_transient=True, t_end=1e9, cfl=0.5, iter_start=5,
+                   i_output_data=2, on_output=lambda it, t: seen.append(it))
+        assert seen == [6, 8]
+
+
+def test_implicit_bdf2_restart_is_exact():
+    """Four BDF2 iterations in one run, or two, an output, and two more
+    continued from the output's state and history (read_restart_data):
+    bitwise the same state."""
+    c = cases.channel(6, 4, 4)
+    kw = dict(implicit=True, is_transient=True, t_end=1e9, cfl=2.0, max_iter_inner=20)
+    with api.from_case(c, "fp64") as s:
+        s.timedisc("bdf2", max_iter=4, **kw)
+        u_full = s.get_conserved()
+    saved = {}
+    with api.from_case(c, "fp64") as s:
+        def out(it, t):
+            saved.update(iter=it, t=t, phi=s.get_state(), hist=s.bdf_history())
+
+        s.timedisc("bdf2", max_iter=2, i_output_data=-1, on_output=out, **kw)
+    assert saved["iter"] == 2 and len(saved["hist"]) == 2
+    with api.from_case(c, "fp64") as s:
+        s.set_state(saved["phi"][:, :5])
+        s.set_bdf_history("bdf2", saved["hist"])
+        st, rows = s.timedisc("bdf2", max_iter=2, iter_start=2, t_start=saved["t"], **kw)
+        assert st["iter"] == 4 and [r[0] for r in rows] == [3, 4]
+        assert np.array_equal(s.get_conserved(), u_full)
+    with api.from_case(c, "fp64") as s:     # BDF2 past its start needs the history
+        st = s.step_newton(3, 0.0, 1e-3, scheme="bdf2", check=False)
+        assert st["status"] != 0

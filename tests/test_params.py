@@ -31,8 +31,12 @@ def test_channel_parameters_map_to_the_channel_case():
 def test_rejections():
     tree = json.load(open(SIM))
     tree["Restart"]["use_restart"]["value"] = True
+    tree["Restart"]["restart_file"] = {"value": "channel.000000100.h5"}
     with pytest.raises(ValueError, match="restart"):
         params.load_simulation(tree)
+    tree["Restart"]["restart_file"] = {"value": "channel.000000100.npz"}
+    sim = params.load_simulation(tree)
+    assert sim.use_restart and sim.restart_file.endswith(".npz")
     tree = json.load(open(SIM))
     tree["Equation"]["Navier-Stokes"]["Flux"]["flux_scheme"]["value"] = "Roe"
     with pytest.raises(ValueError, match="flux"):

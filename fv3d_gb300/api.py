@@ -66,7 +66,7 @@ class ImplicitOpts(C.Structure):
     _fields_ = [("cfl_start", C.c_double), ("cfl_max", C.c_double), ("tol_rel", C.c_double),
                 ("max_newton", C.c_int), ("krylov_dim", C.c_int), ("eta", C.c_double),
                 ("fd_eps", C.c_double), ("jv_precision", C.c_int), ("preconditioner", C.c_int),
-                ("pc_refresh", C.c_int), ("max_restarts", C.c_int)]
+                ("pc_refresh", C.c_int), ("max_restarts", C.c_int), ("sync_every", C.c_int)]
 
 
 class ImplicitStats(C.Structure):

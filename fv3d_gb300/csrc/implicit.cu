@@ -35,7 +35,11 @@ namespace fv3d {
 
 namespace {
 
-constexpr int RED_BLOCKS = 304;   // fixed grid for deterministic reductions (2 per SM)
+constexpr int RED_BLOCKS = 608;   // fixed grid for deterministic reductions (4 per SM)
+// resident Gram-Schmidt blocks per SM the register budget is cut for
+#ifndef FV3D_GS_MINBLOCKS
+#define FV3D_GS_MINBLOCKS 4
+#endif
 // device coefficient slots: h1 [0, 32), h2 [32, 64), |w| and its derived
 // scalars [64, 68), |z|, 1/|z|, eps, 1/eps [68, 72), a host norm [96, 100);
 // FGMRES's y for the solution update at [0, k)
@@ -123,6 +127,47 @@ __global__ void __launch_bounds__(1024) k_dots_final(int nb, int k, const T* __r
   }
 }
 
+// ---- 16-byte groups of basis elements ------------------------------------
+// G consecutive elements: one 16-byte access when G * sizeof(T) == 16 (the
+// address then 16-byte aligned: basis vectors start ldb elements apart, ldb
+// a multiple of 64), else G scalar accesses
+template <int G, class T>
+__device__ __forceinline__ void ldg_group(const T* __restrict__ p, T* x) {
+  if constexpr (G * sizeof(T) == 16) {
+    const uint4 u = __ldg(reinterpret_cast<const uint4*>(p));
+    memcpy(x, &u, 16);
+  } else {
+#pragma unroll
+    for (int l = 0; l < G; ++l) x[l] = __ldg(p + l);
+  }
+}
+template <class T>
+__device__ __forceinline__ void ldg16(const T* __restrict__ p, T* x) {
+  ldg_group<16 / sizeof(T)>(p, x);
+}
+// w is read and rewritten by the same thread: plain loads
+template <int G, class T>
+__device__ __forceinline__ void ld_group(const T* p, T* x) {
+  if constexpr (G * sizeof(T) == 16) {
+    const uint4 u = *reinterpret_cast<const uint4*>(p);
+    memcpy(x, &u, 16);
+  } else {
+#pragma unroll
+    for (int l = 0; l < G; ++l) x[l] = p[l];
+  }
+}
+template <int G, class T>
+__device__ __forceinline__ void st_group(T* p, const T* x) {
+  if constexpr (G * sizeof(T) == 16) {
+    uint4 u;
+    memcpy(&u, x, 16);
+    *reinterpret_cast<uint4*>(p) = u;
+  } else {
+#pragma unroll
+    for (int l = 0; l < G; ++l) p[l] = x[l];
+  }
+}
+
 // ---- fused Gram-Schmidt passes -------------------------------------------
 // One pass over w and the k basis vectors per step of classical Gram-Schmidt
 // with re-orthogonalisation, each ending with a fixed-order reduction done
@@ -176,8 +221,61 @@ __device__ void gs_finalize(const T* __restrict__ partial, int nb, int k, double
   if (threadIdx.x == 0) *counter = 0u;  // ready for the next pass
 }
 
+// one group of G consecutive elements i.. of a Gram-Schmidt pass: G = 16 /
+// sizeof(T) with 16-byte loads (the main loop), G = 1 for the n % G tail.
+// PASS 2 reads each V_j twice (for w - sum h_j V_j, then for the new dots):
+// the second read finds the group in cache
+template <int KMAX, int PASS, int G, class T>
+__device__ __forceinline__ void gs_group(T* __restrict__ w, const T* __restrict__ V, size_t ldb, size_t i, int k,
+                                         const T* hs, T* acc) {
+  T wi[G];
+  ld_group<G>(w + i, wi);
+  if (PASS == 0) {
+#pragma unroll
+    for (int l = 0; l < G; ++l) acc[0] = fmadd(wi[l], wi[l], acc[0]);
+  } else if (PASS == 1) {
+#pragma unroll
+    for (int j = 0; j < KMAX; ++j)
+      if (j < k) {
+        T v[G];
+        ldg_group<G>(V + (size_t)j * ldb + i, v);
+#pragma unroll
+        for (int l = 0; l < G; ++l) acc[j] = fmadd(wi[l], v[l], acc[j]);
+      }
+  } else {
+    T sum[G];
+#pragma unroll
+    for (int l = 0; l < G; ++l) sum[l] = T(0);
+#pragma unroll
+    for (int j = 0; j < KMAX; ++j)
+      if (j < k) {
+        T v[G];
+        ldg_group<G>(V + (size_t)j * ldb + i, v);
+#pragma unroll
+        for (int l = 0; l < G; ++l) sum[l] = fmadd(hs[j], v[l], sum[l]);
+      }
+    T wn[G];
+#pragma unroll
+    for (int l = 0; l < G; ++l) wn[l] = wi[l] - sum[l];
+    st_group<G>(w + i, wn);
+    if (PASS == 2) {
+#pragma unroll
+      for (int j = 0; j < KMAX; ++j)
+        if (j < k) {
+          T v[G];
+          ldg_group<G>(V + (size_t)j * ldb + i, v);
+#pragma unroll
+          for (int l = 0; l < G; ++l) acc[j] = fmadd(wn[l], v[l], acc[j]);
+        }
+    } else {
+#pragma unroll
+      for (int l = 0; l < G; ++l) acc[0] = fmadd(wn[l], wn[l], acc[0]);
+    }
+  }
+}
+
 template <int KMAX, int PASS, class T>
-__global__ void __launch_bounds__(256) k_gs(size_t n, T* __restrict__ w, const T* __restrict__ V, int k,
+__global__ void __launch_bounds__(256, FV3D_GS_MINBLOCKS) k_gs(size_t n, size_t ldb, T* __restrict__ w, const T* __restrict__ V, int k,
                                             const double* __restrict__ h_in, T* __restrict__ partial,
                                             unsigned int* counter, double* __restrict__ out, double c,
                                             const double* __restrict__ c_dev) {
@@ -188,50 +286,14 @@ __global__ void __launch_bounds__(256) k_gs(size_t n, T* __restrict__ w, const T
   if (PASS >= 2 && threadIdx.x < 32) hs[threadIdx.x] = (threadIdx.x < (unsigned)k) ? (T)h_in[threadIdx.x] : T(0);
   __syncthreads();
   constexpr int NA = (PASS == 0 || PASS == 3) ? 1 : KMAX;
-  // elements per thread per iteration: several independent loads in flight
-  constexpr int U = (PASS <= 1) ? (KMAX <= 8 ? 8 : (KMAX <= 16 ? 4 : 2)) : (KMAX <= 8 ? 4 : (KMAX <= 16 ? 2 : 1));
+  constexpr int L = 16 / sizeof(T);
   T acc[NA];
 #pragma unroll
   for (int j = 0; j < NA; ++j) acc[j] = T(0);
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-  for (; i < n; i += U * stride) {
-    T wi[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) wi[u] = (i + u * stride < n) ? w[i + u * stride] : T(0);
-    if (PASS == 0) {
-#pragma unroll
-      for (int u = 0; u < U; ++u) acc[0] = fmadd(wi[u], wi[u], acc[0]);
-    } else if (PASS == 1) {
-#pragma unroll
-      for (int u = 0; u < U; ++u)
-#pragma unroll
-        for (int j = 0; j < KMAX; ++j)
-          if (j < k && i + u * stride < n) acc[j] = fmadd(wi[u], V[(size_t)j * n + i + u * stride], acc[j]);
-    } else {
-      T v[U][KMAX];
-#pragma unroll
-      for (int u = 0; u < U; ++u)
-#pragma unroll
-        for (int j = 0; j < KMAX; ++j) v[u][j] = (j < k && i + u * stride < n) ? V[(size_t)j * n + i + u * stride] : T(0);
-#pragma unroll
-      for (int u = 0; u < U; ++u) {
-        T sum = T(0);
-#pragma unroll
-        for (int j = 0; j < KMAX; ++j)
-          if (j < k) sum = fmadd(hs[j], v[u][j], sum);
-        const T wn = wi[u] - sum;
-        if (i + u * stride < n) w[i + u * stride] = wn;
-        if (PASS == 2) {
-#pragma unroll
-          for (int j = 0; j < KMAX; ++j)
-            if (j < k) acc[j] = fmadd(wn, v[u][j], acc[j]);
-        } else {
-          acc[0] = fmadd(wn, wn, acc[0]);
-        }
-      }
-    }
-  }
+  const size_t stride = (size_t)gridDim.x * blockDim.x, gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t nq = n / L;
+  for (size_t q = gid; q < nq; q += stride) gs_group<KMAX, PASS, L>(w, V, ldb, q * L, k, hs, acc);
+  for (size_t i = nq * L + gid; i < n; i += stride) gs_group<KMAX, PASS, 1>(w, V, ldb, i, k, hs, acc);
   const int kk = (NA == 1) ? 1 : k;
 #pragma unroll
   for (int j = 0; j < NA; ++j) {
@@ -278,30 +340,34 @@ __global__ void k_fd_state(size_t n, const double* __restrict__ U, const T* __re
     W[i] = U[i] + e * (double)z[i];
 }
 
-// w += sign sum_j h_j V_j   (h on the device, FP64; the sum in T)
+// x += sum_j h_j Z_j in FP64 (the Newton correction from the basis, vectors
+// ldb apart): 16-byte groups of Z per thread, then the n % L tail
 template <class T>
-__global__ void k_multi_axpy(size_t n, T* __restrict__ w, const T* __restrict__ V, const double* __restrict__ h,
-                             int k, double sign) {
-  __shared__ T hs[32];
-  if (threadIdx.x < 32) hs[threadIdx.x] = (threadIdx.x < (unsigned)k) ? (T)(sign * h[threadIdx.x]) : T(0);
-  __syncthreads();
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-    T s = T(0);
-    for (int j = 0; j < k; ++j) s = fmadd(hs[j], V[(size_t)j * n + i], s);
-    w[i] = w[i] + s;
-  }
-}
-
-// x += sum_j h_j Z_j in FP64 (the Newton correction from the basis)
-template <class T>
-__global__ void k_axpy_basis(size_t n, double* __restrict__ x, const T* __restrict__ Z, const double* __restrict__ h,
-                             int k) {
+__global__ void k_axpy_basis(size_t n, size_t ldb, double* __restrict__ x, const T* __restrict__ Z,
+                             const double* __restrict__ h, int k) {
+  constexpr int L = 16 / sizeof(T);
   __shared__ double hs[32];
   if (threadIdx.x < 32) hs[threadIdx.x] = (threadIdx.x < (unsigned)k) ? h[threadIdx.x] : 0.0;
   __syncthreads();
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x, gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t nq = n / L;
+  for (size_t q = gid; q < nq; q += stride) {
+    double s[L];
+#pragma unroll
+    for (int l = 0; l < L; ++l) s[l] = 0.0;
+#pragma unroll 4
+    for (int j = 0; j < k; ++j) {
+      T z[L];
+      ldg16(Z + (size_t)j * ldb + q * L, z);
+#pragma unroll
+      for (int l = 0; l < L; ++l) s[l] = fma(hs[j], (double)z[l], s[l]);
+    }
+#pragma unroll
+    for (int l = 0; l < L; ++l) x[q * L + l] += s[l];
+  }
+  for (size_t i = nq * L + gid; i < n; i += stride) {
     double s = 0.0;
-    for (int j = 0; j < k; ++j) s = fma(hs[j], (double)Z[(size_t)j * n + i], s);
+    for (int j = 0; j < k; ++j) s = fma(hs[j], (double)Z[(size_t)j * ldb + i], s);
     x[i] += s;
   }
 }
@@ -649,6 +715,7 @@ fv3d_status Implicit::setup(Ctx& ctx, int m) {
   release_graphs();  // captured steps hold the old buffers
   this->n = n;
   this->m = m;
+  ldb = (n + 63) / 64 * 64;
   auto al = [&](DevBuf<double>& b, size_t cnt) { return ctx.cuda(b.alloc(cnt), "implicit allocation"); };
   fv3d_status st;
   if ((st = al(w, n)) ||
@@ -658,6 +725,9 @@ fv3d_status Implicit::setup(Ctx& ctx, int m) {
     return st;
   if (hpin == nullptr && (st = ctx.cuda(cudaMallocHost((void**)&hpin, sizeof(double) * kHostCoefs),
                                         "implicit host buffer")) != FV3D_OK)
+    return st;
+  if (hcols == nullptr && (st = ctx.cuda(cudaMallocHost((void**)&hcols, sizeof(double) * 32 * kHostCoefs),
+                                         "implicit host buffer")) != FV3D_OK)
     return st;
   if ((st = ctx.cuda(Dinv.alloc(25 * (size_t)ctx.nc), "implicit allocation")) != FV3D_OK) return st;
   if ((st = ctx.cuda(bits.alloc(2), "implicit allocation")) != FV3D_OK) return st;
@@ -739,7 +809,7 @@ fv3d_status Implicit::gs_pass(Ctx& ctx, int pass, T* wv, const T* Vb, int k, con
   const int nb = std::min(RED_BLOCKS, blocks(n));
   T* pt = reinterpret_cast<T*>(part.p);
   unsigned int* ctr = reinterpret_cast<unsigned int*>(bits.p + 1);  // zero between passes
-#define GS_LAUNCH(KM, P) k_gs<KM, P, T><<<nb, 256, 0, ctx.stream>>>(n, wv, Vb, k, h_in, pt, ctr, dst, c, c_dev)
+#define GS_LAUNCH(KM, P) k_gs<KM, P, T><<<nb, 256, 0, ctx.stream>>>(n, ldb, wv, Vb, k, h_in, pt, ctr, dst, c, c_dev)
   if (pass == 0) GS_LAUNCH(1, 0);
   else if (pass == 3) { if (k <= 8) GS_LAUNCH(8, 3); else if (k <= 16) GS_LAUNCH(16, 3); else GS_LAUNCH(32, 3); }
   else if (pass == 1) { if (k <= 8) GS_LAUNCH(8, 1); else if (k <= 16) GS_LAUNCH(16, 1); else GS_LAUNCH(32, 1); }
@@ -828,17 +898,18 @@ fv3d_status Implicit::build_blocks(Ctx& ctx) {
 // kind) once captured: every scalar it needs lives in device memory.
 template <class T>
 fv3d_status Implicit::enqueue_arnoldi(Ctx& ctx, T* Vt, T* Zt, T* wt, int k) {
-  T* vk = Vt + (size_t)k * n;
-  T* zk = Zt + (size_t)k * n;
+  T* vk = Vt + (size_t)k * ldb;
+  T* zk = Zt + (size_t)k * ldb;
   fv3d_status st = precondition<T>(ctx, vk, zk);
   if (st != FV3D_OK) return st;
   if ((st = apply_A<T>(ctx, zk, wt)) != FV3D_OK) return st;
   if ((st = gs_pass<T>(ctx, 1, wt, Vt, k + 1, nullptr, hdev.p, 0.0, nullptr)) != FV3D_OK) return st;
   if ((st = gs_pass<T>(ctx, 2, wt, Vt, k + 1, hdev.p, hdev.p + 32, 0.0, nullptr)) != FV3D_OK) return st;
   if ((st = gs_pass<T>(ctx, 3, wt, Vt, k + 1, hdev.p + 32, hdev.p + 64, 1.0, nullptr)) != FV3D_OK) return st;
-  k_scale_dev<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, wt, hdev.p + 65, Vt + (size_t)(k + 1) * n);
+  k_scale_dev<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, wt, hdev.p + 65, Vt + (size_t)(k + 1) * ldb);
   ICK(cudaGetLastError());
-  ICK(cudaMemcpyAsync(hpin, hdev.p, sizeof(double) * kHostCoefs, cudaMemcpyDeviceToHost, ctx.stream));
+  ICK(cudaMemcpyAsync(hcols + (size_t)k * kHostCoefs, hdev.p, sizeof(double) * kHostCoefs, cudaMemcpyDeviceToHost,
+                      ctx.stream));
   return FV3D_OK;
 }
 
@@ -903,32 +974,41 @@ fv3d_status Implicit::fgmres_t(Ctx& ctx, T* Vt, T* Zt, T* wt, double rnorm, int*
     g[0] = beta;
     int k = 0;
     bool done = false;
-    for (; k < m; ++k) {
-      fv3d_status st;
-      if ((st = arnoldi_step<T>(ctx, Vt, Zt, wt, k)) != FV3D_OK) return st;
-      ICK(cudaStreamSynchronize(ctx.stream));
-      const double hn = hpin[64];
-      for (int j = 0; j <= k; ++j) H[(size_t)k * (m + 1) + j] = hpin[j] + hpin[32 + j];
-      H[(size_t)k * (m + 1) + k + 1] = hn;
-      // Givens rotations on the new column
-      for (int j = 0; j < k; ++j) {
-        const double a = H[(size_t)k * (m + 1) + j], b = H[(size_t)k * (m + 1) + j + 1];
-        H[(size_t)k * (m + 1) + j] = cs[j] * a + sn[j] * b;
-        H[(size_t)k * (m + 1) + j + 1] = -sn[j] * a + cs[j] * b;
+    // chunks of Arnoldi steps run back to back on the device, their
+    // coefficients processed after one synchronisation
+    const int chunk = opts.sync_every > 0 ? opts.sync_every : 10;
+    for (int k1 = 0; k < m && !done;) {
+      k1 = std::min(m, k + chunk);
+      for (int j = k; j < k1; ++j) {
+        fv3d_status st = arnoldi_step<T>(ctx, Vt, Zt, wt, j);
+        if (st != FV3D_OK) return st;
       }
-      const double a = H[(size_t)k * (m + 1) + k], b = H[(size_t)k * (m + 1) + k + 1];
-      const double r = sqrt(a * a + b * b);
-      // a preconditioned direction with no component (a zero or non-finite
-      // preconditioner output): stop without it, leaving the residual unreduced
-      if (!(r > 0.0) || !std::isfinite(r)) { res = fabs(g[k]); done = true; break; }
-      cs[k] = (r > 0.0) ? a / r : 1.0;
-      sn[k] = (r > 0.0) ? b / r : 0.0;
-      H[(size_t)k * (m + 1) + k] = r;
-      H[(size_t)k * (m + 1) + k + 1] = 0.0;
-      g[k + 1] = -sn[k] * g[k];
-      g[k] = cs[k] * g[k];
-      res = fabs(g[k + 1]);
-      if (res <= opts.eta * rnorm || !(hn > 0.0)) { ++k; done = true; break; }
+      ICK(cudaStreamSynchronize(ctx.stream));
+      for (; k < k1; ++k) {
+        const double* hc = hcols + (size_t)k * kHostCoefs;
+        const double hn = hc[64];
+        for (int j = 0; j <= k; ++j) H[(size_t)k * (m + 1) + j] = hc[j] + hc[32 + j];
+        H[(size_t)k * (m + 1) + k + 1] = hn;
+        // Givens rotations on the new column
+        for (int j = 0; j < k; ++j) {
+          const double a = H[(size_t)k * (m + 1) + j], b = H[(size_t)k * (m + 1) + j + 1];
+          H[(size_t)k * (m + 1) + j] = cs[j] * a + sn[j] * b;
+          H[(size_t)k * (m + 1) + j + 1] = -sn[j] * a + cs[j] * b;
+        }
+        const double a = H[(size_t)k * (m + 1) + k], b = H[(size_t)k * (m + 1) + k + 1];
+        const double r = sqrt(a * a + b * b);
+        // a preconditioned direction with no component (a zero or non-finite
+        // preconditioner output): stop without it, leaving the residual unreduced
+        if (!(r > 0.0) || !std::isfinite(r)) { res = fabs(g[k]); done = true; break; }
+        cs[k] = (r > 0.0) ? a / r : 1.0;
+        sn[k] = (r > 0.0) ? b / r : 0.0;
+        H[(size_t)k * (m + 1) + k] = r;
+        H[(size_t)k * (m + 1) + k + 1] = 0.0;
+        g[k + 1] = -sn[k] * g[k];
+        g[k] = cs[k] * g[k];
+        res = fabs(g[k + 1]);
+        if (res <= opts.eta * rnorm || !(hn > 0.0)) { ++k; done = true; break; }
+      }
     }
     for (int i = k - 1; i >= 0; --i) {
       double s = g[i];
@@ -937,7 +1017,7 @@ fv3d_status Implicit::fgmres_t(Ctx& ctx, T* Vt, T* Zt, T* wt, double rnorm, int*
     }
     // x += Z y
     ICK(cudaMemcpyAsync(hdev.p, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, ctx.stream));
-    k_axpy_basis<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, x.p, Zt, hdev.p, k);
+    k_axpy_basis<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, ldb, x.p, Zt, hdev.p, k);
     ICK(cudaGetLastError());
     total += k;
     if (done) break;
@@ -963,7 +1043,7 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
   if (st != FV3D_OK) return st;
   // Krylov basis in the precision of the Jacobian-vector products
   {
-    const size_t nv = (size_t)(opts.krylov_dim + 1) * n, nz = (size_t)opts.krylov_dim * n;
+    const size_t nv = (size_t)(opts.krylov_dim + 1) * ldb, nz = (size_t)opts.krylov_dim * ldb;
     cudaError_t e = cudaSuccess;
     if ((opts.jv_precision == 1 && (V32.n < nv || Z32.n < nz || w32.n < n)) ||
         (opts.jv_precision != 1 && (V.n < nv || Z.n < nz)))
@@ -1197,6 +1277,7 @@ extern "C" fv3d_status fv3d_implicit_default_opts(fv3d_implicit_opts* o) {
   o->preconditioner = FV3D_PC_BLOCK_JACOBI;
   o->pc_refresh = 1;
   o->max_restarts = 0;
+  o->sync_every = 10;
   return FV3D_OK;
 }
 

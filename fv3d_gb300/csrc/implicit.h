@@ -36,6 +36,7 @@ struct Mlp {
 struct Implicit {
   fv3d_implicit_opts opts;
   size_t n = 0;   // 5 * cells
+  size_t ldb = 0; // Krylov basis vectors' stride: n rounded up to 64 (16-byte aligned vectors)
   int m = 0;      // Krylov dimension allocated
   DevBuf<double> V, Z, w, R, Rb, Rp, Wst, x, dtl, idtl, D, part, hdev, fdist;
   DevBuf<float> V32, Z32, w32;    // Krylov basis for FP32 Jacobian-vector products
@@ -45,13 +46,15 @@ struct Implicit {
   int jv_count = 0;
   double unorm = 0.0;
   bool use_block_jacobi = false;  // learned preconditioner fell back this step
-  double* hpin = nullptr;         // pinned host copy of the Arnoldi coefficients (kHostCoefs doubles)
+  double* hpin = nullptr;         // pinned host scalars (kHostCoefs doubles)
+  double* hcols = nullptr;        // pinned: each Arnoldi step's coefficients, [32][kHostCoefs]
 
   std::map<long long, cudaGraphExec_t> arnoldi_graphs;  // captured Arnoldi steps
 
   ~Implicit() {
     release_graphs();
     if (hpin) cudaFreeHost(hpin);
+    if (hcols) cudaFreeHost(hcols);
   }
   void release_graphs();
   template <class T>

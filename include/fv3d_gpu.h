@@ -204,6 +204,9 @@ typedef struct fv3d_implicit_opts {
     int preconditioner;    /* FV3D_PC_* */
     int pc_refresh;        /* rebuild the blocks every pc_refresh Newton steps */
     int max_restarts;      /* FGMRES restarts per Newton step (0: one cycle) */
+    int sync_every;        /* Arnoldi steps launched between host synchronisations (10; 0 takes
+                              10): the Givens rotations of a chunk run after it, so a cycle that
+                              meets eta inside a chunk computes up to sync_every - 1 unused steps */
 } fv3d_implicit_opts;
 typedef struct fv3d_implicit_stats {
     int newton_steps;

@@ -36,7 +36,8 @@ namespace fv3d {
 namespace {
 
 constexpr int RED_BLOCKS = 608;   // fixed grid for deterministic reductions (4 per SM)
-// resident Gram-Schmidt blocks per SM the register budget is cut for
+// resident Gram-Schmidt blocks per SM the register budget is cut for (FP32
+// basis; an FP64 basis keeps 2 so that its 32-vector passes do not spill)
 #ifndef FV3D_GS_MINBLOCKS
 #define FV3D_GS_MINBLOCKS 4
 #endif
@@ -225,11 +226,35 @@ __device__ void gs_finalize(const T* __restrict__ partial, int nb, int k, double
 // sizeof(T) with 16-byte loads (the main loop), G = 1 for the n % G tail.
 // PASS 2 reads each V_j twice (for w - sum h_j V_j, then for the new dots):
 // the second read finds the group in cache
+// w = z / dt_i - (R(U + eps z) - R(U)) / eps (k_jv_combine's arithmetic),
+// formed inside the first Gram-Schmidt pass when z is set
+template <class T>
+struct JvArgs {
+  const T* z = nullptr;
+  const double* Rp = nullptr;
+  const double* Rb = nullptr;
+  const double* idt = nullptr;   // per cell
+  const double* ieps = nullptr;  // device scalar 1/eps
+  size_t nc = 0;
+};
+
 template <int KMAX, int PASS, int G, class T>
 __device__ __forceinline__ void gs_group(T* __restrict__ w, const T* __restrict__ V, size_t ldb, size_t i, int k,
-                                         const T* hs, T* acc) {
+                                         const T* hs, T* acc, const JvArgs<T>& jv, T ieps) {
   T wi[G];
-  ld_group<G>(w + i, wi);
+  if (PASS == 1 && jv.z != nullptr) {
+    T zi[G];
+    ldg_group<G>(jv.z + i, zi);
+#pragma unroll
+    for (int l = 0; l < G; ++l) {
+      const size_t e = i + l;
+      const T id = (T)__ldg(jv.idt + e % jv.nc);
+      wi[l] = zi[l] * id - (T)(__ldg(jv.Rp + e) - __ldg(jv.Rb + e)) * ieps;
+    }
+    st_group<G>(w + i, wi);
+  } else {
+    ld_group<G>(w + i, wi);
+  }
   if (PASS == 0) {
 #pragma unroll
     for (int l = 0; l < G; ++l) acc[0] = fmadd(wi[l], wi[l], acc[0]);
@@ -275,11 +300,12 @@ __device__ __forceinline__ void gs_group(T* __restrict__ w, const T* __restrict_
 }
 
 template <int KMAX, int PASS, class T>
-__global__ void __launch_bounds__(256, FV3D_GS_MINBLOCKS) k_gs(size_t n, size_t ldb, T* __restrict__ w, const T* __restrict__ V, int k,
-                                            const double* __restrict__ h_in, T* __restrict__ partial,
-                                            unsigned int* counter, double* __restrict__ out, double c,
-                                            const double* __restrict__ c_dev) {
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : FV3D_GS_MINBLOCKS)
+    k_gs(size_t n, size_t ldb, T* __restrict__ w, const T* __restrict__ V, int k, const double* __restrict__ h_in,
+         T* __restrict__ partial, unsigned int* counter, double* __restrict__ out, double c,
+         const double* __restrict__ c_dev, const JvArgs<T> jv) {
   if (c_dev != nullptr) c = *c_dev;  // the finite-difference scale, set per Newton step
+  const T ieps = (PASS == 1 && jv.z != nullptr) ? (T)*jv.ieps : T(0);
   __shared__ T hs[32];
   __shared__ T sh[8][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -292,8 +318,8 @@ __global__ void __launch_bounds__(256, FV3D_GS_MINBLOCKS) k_gs(size_t n, size_t 
   for (int j = 0; j < NA; ++j) acc[j] = T(0);
   const size_t stride = (size_t)gridDim.x * blockDim.x, gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   const size_t nq = n / L;
-  for (size_t q = gid; q < nq; q += stride) gs_group<KMAX, PASS, L>(w, V, ldb, q * L, k, hs, acc);
-  for (size_t i = nq * L + gid; i < n; i += stride) gs_group<KMAX, PASS, 1>(w, V, ldb, i, k, hs, acc);
+  for (size_t q = gid; q < nq; q += stride) gs_group<KMAX, PASS, L>(w, V, ldb, q * L, k, hs, acc, jv, ieps);
+  for (size_t i = nq * L + gid; i < n; i += stride) gs_group<KMAX, PASS, 1>(w, V, ldb, i, k, hs, acc, jv, ieps);
   const int kk = (NA == 1) ? 1 : k;
 #pragma unroll
   for (int j = 0; j < NA; ++j) {
@@ -409,6 +435,32 @@ __global__ void k_jv_combine(int nc, const T* __restrict__ z, const double* __re
   }
 }
 
+
+// FP32 state record (rho, m, E, p, T) of a cell's FP64 state w[5]
+__device__ __forceinline__ void put_record(float* __restrict__ Uf, int c, const double* w, float km1, float R) {
+  const float rho = (float)w[0], mx = (float)w[1], my = (float)w[2], mz = (float)w[3];
+  const double E = w[4];
+  const float ir = 1.f / rho;
+  const float ke = 0.5f * (mx * mx + my * my + mz * mz) * ir;
+  const float p = fmaxf(1.00E-10f, (float)((double)km1 * (E - (double)ke)));
+  float4* d = reinterpret_cast<float4*>(Uf) + 2 * (size_t)c;
+  d[0] = make_float4(rho, mx, my, mz);
+  d[1] = make_float4((float)E, p, p * ir / R, 0.f);
+}
+
+// the records of the finite-difference state W = U + eps z (eps on the
+// device), W itself not stored
+template <class T>
+__global__ void k_fd_record(int nc, const double* __restrict__ U, const T* __restrict__ z,
+                            const double* __restrict__ eps, float* __restrict__ Uf, float km1, float R) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  const double e = *eps;
+  double w[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) w[j] = U[(size_t)j * nc + c] + e * (double)z[(size_t)j * nc + c];
+  put_record(Uf, c, w, km1, R);
+}
 
 // FP32 state record (rho, m, E, p, T) of an FP64 state W (renumbered SoA)
 __global__ void k_make_record(int nc, const double* __restrict__ W, float* __restrict__ Uf,
@@ -774,10 +826,8 @@ static fv3d_status residual64(Ctx& ctx, const double* state, double* out) {
 }
 
 // R(state) with the FP32 (mixed) kernels into `out`
-static fv3d_status residual32(Ctx& ctx, const double* state, double* out) {
-  k_make_record<<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, state, ctx.d_Uf.p, ctx.phys.f32[1],
-                                                        ctx.phys.f32[4]);
-  ICK(cudaGetLastError());
+// the FP32 residual of the state whose records are in Uf
+static fv3d_status residual32_records(Ctx& ctx, double* out) {
   MxArgs a = ctx.mx_args();
   a.dphi = out;
   StageCoef co{0, 0, 0, 0, 1, 1};
@@ -785,6 +835,13 @@ static fv3d_status residual32(Ctx& ctx, const double* state, double* out) {
   ICK(launch_mx_sides(a, d, ctx.stream));
   ICK(launch_mx_flux_update(a, d, 0, false, co, ctx.stream));
   return FV3D_OK;
+}
+
+static fv3d_status residual32(Ctx& ctx, const double* state, double* out) {
+  k_make_record<<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, state, ctx.d_Uf.p, ctx.phys.f32[1],
+                                                        ctx.phys.f32[4]);
+  ICK(cudaGetLastError());
+  return residual32_records(ctx, out);
 }
 
 // k inner products w . V_j (j < k <= 32) into dst on the device, no host
@@ -805,11 +862,15 @@ fv3d_status Implicit::dots_dev(Ctx& ctx, const T* wv, const T* Vb, int k, double
 // one fused Gram-Schmidt pass (k_gs) over a fixed grid of RED_BLOCKS blocks
 template <class T>
 fv3d_status Implicit::gs_pass(Ctx& ctx, int pass, T* wv, const T* Vb, int k, const double* h_in, double* dst,
-                              double c, const double* c_dev) {
+                              double c, const double* c_dev, const T* jv_z) {
+  JvArgs<T> jv;
+  if (jv_z != nullptr) {
+    jv.z = jv_z; jv.Rp = Rp.p; jv.Rb = Rb.p; jv.idt = idtl.p; jv.ieps = jv_ieps; jv.nc = (size_t)ctx.nc;
+  }
   const int nb = std::min(RED_BLOCKS, blocks(n));
   T* pt = reinterpret_cast<T*>(part.p);
   unsigned int* ctr = reinterpret_cast<unsigned int*>(bits.p + 1);  // zero between passes
-#define GS_LAUNCH(KM, P) k_gs<KM, P, T><<<nb, 256, 0, ctx.stream>>>(n, ldb, wv, Vb, k, h_in, pt, ctr, dst, c, c_dev)
+#define GS_LAUNCH(KM, P) k_gs<KM, P, T><<<nb, 256, 0, ctx.stream>>>(n, ldb, wv, Vb, k, h_in, pt, ctr, dst, c, c_dev, jv)
   if (pass == 0) GS_LAUNCH(1, 0);
   else if (pass == 3) { if (k <= 8) GS_LAUNCH(8, 3); else if (k <= 16) GS_LAUNCH(16, 3); else GS_LAUNCH(32, 3); }
   else if (pass == 1) { if (k <= 8) GS_LAUNCH(8, 1); else if (k <= 16) GS_LAUNCH(16, 1); else GS_LAUNCH(32, 1); }
@@ -833,7 +894,7 @@ template <class T>
 fv3d_status Implicit::precondition(Ctx& ctx, const T* v, T* z) {
   if (opts.preconditioner == FV3D_PC_LEARNED && !use_block_jacobi) return ctx.mlp->apply(ctx, v, z);
   if (opts.preconditioner == FV3D_PC_NONE) {
-    ICK(cudaMemcpyAsync(z, v, sizeof(T) * n, cudaMemcpyDeviceToDevice, ctx.stream));
+    if (z != v) ICK(cudaMemcpyAsync(z, v, sizeof(T) * n, cudaMemcpyDeviceToDevice, ctx.stream));
     return FV3D_OK;
   }
   k_block_apply<T><<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, Dinv.p, v, z);
@@ -843,18 +904,38 @@ fv3d_status Implicit::precondition(Ctx& ctx, const T* v, T* z) {
 
 // w = (I/dt - J) z: the step eps = rel (1 + |U|) / |z| is formed on the
 // device, so a Jacobian-vector product needs no host synchronisation
+// R(U + eps z) into Rp with eps = c/|z|, c = rel (1 + |U|) from its device
+// slot (set each Newton step), so captured iterations stay valid; a unit z
+// (an unpreconditioned basis vector, |v_k| = 1) takes eps = c without a
+// norm pass.  Sets jv_ieps to the device slot holding 1/eps.
+template <class T>
+fv3d_status Implicit::fd_residual(Ctx& ctx, const T* z, bool unit) {
+  const double* eps = hdev.p + 100;
+  jv_ieps = hdev.p + 101;
+  if (!unit) {
+    fv3d_status st = gs_pass<T>(ctx, 0, const_cast<T*>(z), z, 1, nullptr, hdev.p + 68, 0.0, hdev.p + 100);
+    if (st != FV3D_OK) return st;
+    eps = hdev.p + 70;
+    jv_ieps = hdev.p + 71;
+  }
+  if (opts.jv_precision == 1) {
+    k_fd_record<T><<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, ctx.d_U.p, z, eps, ctx.d_Uf.p, ctx.phys.f32[1],
+                                                          ctx.phys.f32[4]);
+    ICK(cudaGetLastError());
+    return residual32_records(ctx, Rp.p);
+  }
+  k_fd_state<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, ctx.d_U.p, z, eps, Wst.p);
+  ICK(cudaGetLastError());
+  return residual64(ctx, Wst.p, Rp.p);
+}
+
+// w = (I/dt - J) z: the step eps is formed on the device, so a
+// Jacobian-vector product needs no host synchronisation
 template <class T>
 fv3d_status Implicit::apply_A(Ctx& ctx, const T* z, T* out) {
-  // |z| and eps = c/|z| with c = rel (1 + |U|) from its device slot (set by
-  // set_fd_scale each Newton step), so captured iterations stay valid
-  fv3d_status st = gs_pass<T>(ctx, 0, const_cast<T*>(z), z, 1, nullptr, hdev.p + 68, 0.0, hdev.p + 100);
+  fv3d_status st = fd_residual<T>(ctx, z, false);
   if (st != FV3D_OK) return st;
-  k_fd_state<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, ctx.d_U.p, z, hdev.p + 70, Wst.p);
-  ICK(cudaGetLastError());
-  if (opts.jv_precision == 1) st = residual32(ctx, Wst.p, Rp.p);
-  else st = residual64(ctx, Wst.p, Rp.p);
-  if (st != FV3D_OK) return st;
-  k_jv_combine<T><<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, z, Rp.p, Rb.p, idtl.p, hdev.p + 71, out);
+  k_jv_combine<T><<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, z, Rp.p, Rb.p, idtl.p, jv_ieps, out);
   ICK(cudaGetLastError());
   return FV3D_OK;
 }
@@ -899,11 +980,12 @@ fv3d_status Implicit::build_blocks(Ctx& ctx) {
 template <class T>
 fv3d_status Implicit::enqueue_arnoldi(Ctx& ctx, T* Vt, T* Zt, T* wt, int k) {
   T* vk = Vt + (size_t)k * ldb;
-  T* zk = Zt + (size_t)k * ldb;
+  T* zk = (opts.preconditioner == FV3D_PC_NONE) ? vk : Zt + (size_t)k * ldb;  // unpreconditioned: z_k = v_k
   fv3d_status st = precondition<T>(ctx, vk, zk);
   if (st != FV3D_OK) return st;
-  if ((st = apply_A<T>(ctx, zk, wt)) != FV3D_OK) return st;
-  if ((st = gs_pass<T>(ctx, 1, wt, Vt, k + 1, nullptr, hdev.p, 0.0, nullptr)) != FV3D_OK) return st;
+  // w = A z_k formed inside the first Gram-Schmidt pass
+  if ((st = fd_residual<T>(ctx, zk, opts.preconditioner == FV3D_PC_NONE)) != FV3D_OK) return st;
+  if ((st = gs_pass<T>(ctx, 1, wt, Vt, k + 1, nullptr, hdev.p, 0.0, nullptr, zk)) != FV3D_OK) return st;
   if ((st = gs_pass<T>(ctx, 2, wt, Vt, k + 1, hdev.p, hdev.p + 32, 0.0, nullptr)) != FV3D_OK) return st;
   if ((st = gs_pass<T>(ctx, 3, wt, Vt, k + 1, hdev.p + 32, hdev.p + 64, 1.0, nullptr)) != FV3D_OK) return st;
   k_scale_dev<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, wt, hdev.p + 65, Vt + (size_t)(k + 1) * ldb);
@@ -1017,7 +1099,8 @@ fv3d_status Implicit::fgmres_t(Ctx& ctx, T* Vt, T* Zt, T* wt, double rnorm, int*
     }
     // x += Z y
     ICK(cudaMemcpyAsync(hdev.p, y.data(), sizeof(double) * k, cudaMemcpyHostToDevice, ctx.stream));
-    k_axpy_basis<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, ldb, x.p, Zt, hdev.p, k);
+    k_axpy_basis<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(
+        n, ldb, x.p, opts.preconditioner == FV3D_PC_NONE ? Vt : Zt, hdev.p, k);
     ICK(cudaGetLastError());
     total += k;
     if (done) break;
@@ -1078,7 +1161,8 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
       // c = rel (1 + |U|) for the finite-difference steps of this Newton step
       const double rel = (opts.jv_precision == 1) ? 5e-4 : opts.fd_eps;
       hpin[0] = rel * (1.0 + unorm);
-      ICK(cudaMemcpyAsync(hdev.p + 100, hpin, sizeof(double), cudaMemcpyHostToDevice, ctx.stream));
+      hpin[1] = 1.0 / hpin[0];
+      ICK(cudaMemcpyAsync(hdev.p + 100, hpin, 2 * sizeof(double), cudaMemcpyHostToDevice, ctx.stream));
       ICK(cudaStreamSynchronize(ctx.stream));
     }
     // Newton step with a CFL back-off on failure

@@ -70,13 +70,16 @@ struct Implicit {
   template <class T>
   fv3d_status apply_A(Ctx& ctx, const T* z, T* out);
   template <class T>
+  fv3d_status fd_residual(Ctx& ctx, const T* z, bool unit);
+  const double* jv_ieps = nullptr;  // device slot of 1/eps of the last fd_residual
+  template <class T>
   fv3d_status precondition(Ctx& ctx, const T* v, T* z);
   fv3d_status build_blocks(Ctx& ctx);
   template <class T>
   fv3d_status dots_dev(Ctx& ctx, const T* w, const T* V, int k, double* dst, bool take_sqrt, double c);
   template <class T>
   fv3d_status gs_pass(Ctx& ctx, int pass, T* w, const T* V, int k, const double* h_in, double* dst, double c,
-                      const double* c_dev);
+                      const double* c_dev, const T* jv_z = nullptr);
   fv3d_status norm(Ctx& ctx, const double* v, double* out);
   fv3d_status ICK_copy(Ctx& ctx, double* dst, const double* src);
 

@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=20)
     p.add_argument("--cpu-sample-stages", type=int, default=15)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--max-newton", type=int, default=400,
+                   help="channel: Newton step limit per solve (a small value for profiling runs)")
     return p.parse_args()
 
 
@@ -232,14 +234,14 @@ def run_channel(args):
             if args.learned and pc == "block_jacobi":
                 s.mlp_harvest(1024, 400000)
             s.set_state(c.u0)
-            st = s.solve_implicit(preconditioner=pc, max_newton=400, check=False, **kw)
+            st = s.solve_implicit(preconditioner=pc, max_newton=args.max_newton, check=False, **kw)
             runs[pc] = {k: st[k] for k in keys}
             if args.learned:
                 s.mlp_harvest(0, 400000)
         if args.learned:
             tr = s.mlp_train(epochs=30, batch=1024, lr=2e-3)
             s.set_state(c.u0)
-            st = s.solve_implicit(preconditioner="learned", max_newton=400, check=False)
+            st = s.solve_implicit(preconditioner="learned", max_newton=args.max_newton, check=False)
             runs["learned"] = {k: st[k] for k in keys}
             runs["learned"]["train"] = tr
     best = runs["none"]

@@ -84,3 +84,21 @@ def test_lumped_blocks_available():
         b = s.blocks()
     assert np.all(np.isfinite(b))
     assert st["newton_steps"] >= 1
+
+
+@pytest.mark.parametrize("pc", ["none", "block_jacobi"])
+def test_sync_chunk_does_not_change_the_solve(pc):
+    """Arnoldi steps launched in chunks of 1, 7 or 31 between host
+    synchronisations: the same Krylov and Newton counts and bitwise the same
+    state (a chunk only moves the Givens rotations in time; steps computed
+    past a cycle's convergence are discarded)."""
+    c = small_channel()
+    out = []
+    with api.from_case(c, "fp64") as s:
+        for se in (1, 7, 31):
+            s.set_state(c.u0)
+            st = s.solve_implicit(preconditioner=pc, max_newton=6, max_restarts=1, sync_every=se, check=False)
+            out.append(((st["newton_steps"], st["gmres_iterations"], st["rel_res"]), s.get_conserved()))
+    for stats, u in out[1:]:
+        assert stats == out[0][0]
+        assert np.array_equal(u, out[0][1])

@@ -103,6 +103,20 @@ def tgv_tet(n=64) -> Case:
     return Case("tgv_tet", mesh, params, np.array([mg.BC_FLOW]), prim, u0, "rk33", 0.5, 500)
 
 
+def tgv_mixed(n=16, gradient=GREEN_GAUSS, jitter=0.1, seed=20240601) -> Case:
+    """Taylor-Green vortex on the mixed hexahedron / prism / pyramid box
+    (cells of 5 and 6 faces, faces of 3 and 4 nodes): AUSM, Barth-Jespersen,
+    viscous."""
+    kappa, mach = 1.4, 0.3
+    mesh = mg.mixed_box(n, 2 * np.pi, jitter=jitter, seed=seed, name=f"tgv_mixed{n}")
+    u0, p0 = taylor_green(mesh.cell_x, mach, kappa)
+    params = dict(kappa=kappa, R_mix=1.0, mu_mix=1.0 / 1600.0, Pr=0.71, cfl_scale=0.5,
+                  dfl_scale=1.0, flux_scheme=AUSM, reconstruction=LINEAR,
+                  limiter=BARTH_JESPERSEN, gradient=gradient)
+    prim = np.array([[0.0, 0.0, 0.0, p0, p0]])
+    return Case("tgv_mixed", mesh, params, np.array([mg.BC_FLOW]), prim, u0, "rk33", 0.5, 50)
+
+
 def channel(nx=96, ny=48, nz=48, ratio=1.1) -> Case:
     kappa = 1.4
     mesh = mg.channel(nx, ny, nz, 2.0, 1.0, 1.0, ratio)
@@ -125,4 +139,5 @@ def channel(nx=96, ny=48, nz=48, ratio=1.1) -> Case:
 
 
 def make(name: str, **kw) -> Case:
-    return {"euler16": euler16, "tgv_hex": tgv_hex, "tgv_tet": tgv_tet, "channel": channel}[name](**kw)
+    return {"euler16": euler16, "tgv_hex": tgv_hex, "tgv_tet": tgv_tet, "tgv_mixed": tgv_mixed,
+            "channel": channel}[name](**kw)

@@ -3,10 +3,11 @@ preprocessor, tools/pyMeshFV3D: pymeshfv3d/readers/gmsh.py reading, process.py
 building faces and geometry).
 
 Reads the ASCII MSH 2.2 format: $PhysicalNames, $Nodes, $Elements.  Volume
-elements become cells (8-node hexahedra, type 5, or 4-node tetrahedra, type
-4; one kind per mesh, as ``meshgen.build_mesh`` assembles), surface elements
-(4-node quadrangles, type 3, or 3-node triangles, type 2) carry the physical
-group of the boundary faces they cover.  Regions are numbered as the
+elements become cells: 4-node tetrahedra (type 4), 8-node hexahedra (5),
+6-node prisms (6) and 5-node pyramids (7), the element kinds of the
+preprocessor (utilities/element.py), mixed freely; surface elements (4-node
+quadrangles, type 3, or 3-node triangles, type 2) carry the physical group
+of the boundary faces they cover.  Regions are numbered as the
 reference's processed meshes number them: region 0 the flow domain, then the
 boundary physical groups in ascending tag order.
 
@@ -25,7 +26,8 @@ import numpy as np
 
 from . import meshgen as mg
 
-_VOLUME = {5: ("hex", 8), 4: ("tet", 4)}
+_VOLUME = {4: ("tet", 4), 5: ("hex", 8), 6: ("prism", 6), 7: ("pyramid", 5)}
+_ETYPE = {kind: t for t, (kind, _) in _VOLUME.items()}
 _SURFACE = {3: 4, 2: 3}
 
 
@@ -117,7 +119,7 @@ def read_msh(path_or_text, name=None, scale=(1.0, 1.0, 1.0)):
         xyz[k] = [float(p[1]), float(p[2]), float(p[3])]
     xyz *= np.asarray(scale, dtype=float)
     index = {int(t): k for k, t in enumerate(ids)}
-    cells, cell_kind, surf = [], None, []
+    cells, kinds, surf = [], [], []
     el_lines = sec["Elements"]
     for line in el_lines[1:1 + int(el_lines[0])]:
         p = [int(v) for v in line.split()]
@@ -127,10 +129,8 @@ def read_msh(path_or_text, name=None, scale=(1.0, 1.0, 1.0)):
         phys = tags[0] if ntags > 0 else 0
         if etype in _VOLUME:
             kind, nv = _VOLUME[etype]
-            if cell_kind not in (None, kind):
-                raise ValueError("meshes mixing hexahedra and tetrahedra are not supported")
-            cell_kind = kind
-            cells.append(conn[:nv])
+            kinds.append(kind)
+            cells.append(conn[:nv] + [-1] * (8 - nv))
         elif etype in _SURFACE:
             surf.append((phys, conn[:_SURFACE[etype]]))
         elif etype in (1, 15):          # lines, points: geometry only
@@ -140,19 +140,23 @@ def read_msh(path_or_text, name=None, scale=(1.0, 1.0, 1.0)):
     if not cells:
         raise ValueError("no volume elements")
     cell_nodes = np.asarray(cells, dtype=np.int64)
+    width = max(_VOLUME[_ETYPE[k]][1] for k in set(kinds))
+    cell_nodes = cell_nodes[:, :width]
+    valid = cell_nodes >= 0
     shift = np.zeros(cell_nodes.shape + (3,))
     if "Periodic" in sec:
         root = _resolve_periodic(_periodic_links(sec["Periodic"]), index, xyz)
-        canon = root[cell_nodes]
-        shift = xyz[cell_nodes] - xyz[canon]
+        canon = np.where(valid, root[np.maximum(cell_nodes, 0)], -1)
+        shift[valid] = xyz[cell_nodes[valid]] - xyz[canon[valid]]
         cell_nodes = canon
         surf = [(t, [int(root[v]) for v in c]) for t, c in surf]
         # surfaces that cover faces between two cells now are not boundaries
-        table = mg.HEX_FACES if cell_kind == "hex" else mg.TET_FACES
-        keys, counts = np.unique(np.sort(cell_nodes[:, table].reshape(-1, table.shape[1]), axis=1),
-                                 axis=0, return_counts=True)
-        single = {tuple(int(v) for v in k) for k in keys[counts == 1]}
-        surf = [(t, c) for t, c in surf if tuple(sorted(c)) in single]
+        count = {}
+        for c, kind in zip(cell_nodes, kinds):
+            for face in mg.KINDS[kind][1]:
+                key = tuple(sorted(int(v) for v in c[face]))
+                count[key] = count.get(key, 0) + 1
+        surf = [(t, c) for t, c in surf if count.get(tuple(sorted(c)), 0) == 1]
     tags = sorted({t for t, _ in surf})
     region_of_tag = {t: r + 1 for r, t in enumerate(tags)}
     names = ["flow"] + [phys_names.get((2, t), f"boundary{t}") for t in tags]
@@ -162,24 +166,27 @@ def read_msh(path_or_text, name=None, scale=(1.0, 1.0, 1.0)):
     def regions(face_nodes):
         out = np.empty(face_nodes.shape[0], dtype=np.int64)
         for i, row in enumerate(face_nodes):
-            r = surf_key.get(tuple(int(v) for v in row))
+            key = tuple(int(v) for v in row if v >= 0)   # triangles of mixed meshes: leading -1
+            r = surf_key.get(key)
             if r is None:
-                raise ValueError(f"boundary face with nodes {[int(ids[v]) for v in row]} has no physical surface")
+                raise ValueError(f"boundary face with nodes {[int(ids[v]) for v in key]} has no physical surface")
             out[i] = r
         return out
 
-    return mg.build_mesh(xyz, cell_nodes, shift, cell_kind,
+    kind = kinds[0] if len(set(kinds)) == 1 else kinds
+    return mg.build_mesh(xyz, cell_nodes, shift, kind,
                          boundary_region_of_nodes=regions if surf else None,
                          region_names=tuple(names), region_is_boundary=tuple([0] + [1] * len(tags)),
                          name=name or "gmsh")
 
 
 def write_msh(path, nodes, cell_nodes, cell_kind, boundary, phys_names, periodic=None):
-    """Write an ASCII MSH 2.2 file: nodes (n, 3), volume connectivity, the
+    """Write an ASCII MSH 2.2 file: nodes (n, 3), volume connectivity (rows
+    padded with -1 for mixed kinds; cell_kind one kind or one per cell), the
     boundary surface elements as (physical tag, node list) pairs, and
     optionally periodic links, each a list of (slave node, master node)
     pairs (0-based) related by one translation."""
-    etype = 5 if cell_kind == "hex" else 4
+    kinds = [cell_kind] * len(cell_nodes) if isinstance(cell_kind, str) else list(cell_kind)
     lines = ["$MeshFormat", "2.2 0 8", "$EndMeshFormat", "$PhysicalNames", str(len(phys_names))]
     for (dim, tag), nm in sorted(phys_names.items()):
         lines.append(f'{dim} {tag} "{nm}"')
@@ -193,8 +200,10 @@ def write_msh(path, nodes, cell_nodes, cell_kind, boundary, phys_names, periodic
         lines.append(" ".join(str(int(v)) for v in [eid, st, 2, tag, tag] + [int(c) + 1 for c in conn]))
         eid += 1
     vol_tag = max([t for (d, t) in phys_names if d == 3], default=0)
-    for conn in cell_nodes:
-        lines.append(" ".join(str(v) for v in [eid, etype, 2, vol_tag, vol_tag] + [int(c) + 1 for c in conn]))
+    for conn, kind in zip(cell_nodes, kinds):
+        etype = _ETYPE[kind]
+        nv = _VOLUME[etype][1]
+        lines.append(" ".join(str(v) for v in [eid, etype, 2, vol_tag, vol_tag] + [int(c) + 1 for c in conn[:nv]]))
         eid += 1
     lines.append("$EndElements")
     if periodic:

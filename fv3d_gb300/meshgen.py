@@ -6,7 +6,8 @@ generated benchmark meshes: it produces the arrays that
 file that ``write_mesh`` (tools/pyMeshFV3D/pymeshfv3d/write.py:19-201) writes.
 
 Geometry follows tools/pyMeshFV3D/pymeshfv3d/utilities/geometry.py:
-  * cell centre = vertex mean, volume = 5-tet (hex) / 1-tet formula (:50-116)
+  * cell centre = vertex mean, volume = the tetrahedral decompositions of
+    :50-116 (hex 5, prism 3, pyramid 2, tet 1)
   * face centre = vertex mean, area = two-triangle (quad) / triangle (:15-47)
   * normal = normalised cross product of the diagonals (quad) / edges
     (triangle), flipped to point away from cell 0 (:152-183)
@@ -32,6 +33,16 @@ import numpy as np
 HEX_FACES = np.array([[0, 1, 2, 3], [4, 5, 6, 7], [0, 4, 7, 3],
                       [0, 4, 5, 1], [1, 5, 6, 2], [3, 7, 6, 2]], dtype=np.int64)
 TET_FACES = np.array([[0, 1, 2], [0, 3, 1], [0, 3, 2], [2, 3, 1]], dtype=np.int64)
+# element.py:104-122: prism (3 quadrangles, 2 triangles), pyramid (base
+# quadrangle, 4 triangles); rows of mixed width as lists.  The reference's
+# pyramid table lists (v0, v3, v1) as its fifth face, a triangle inside the
+# base, so the side face on the v3-v0 edge is never created and no pyramid
+# closes; the side face (v0, v3, v4) is used here.
+PRISM_FACES = [[0, 1, 4, 3], [1, 2, 5, 4], [0, 2, 5, 3], [0, 1, 2], [3, 4, 5]]
+PYRAMID_FACES = [[0, 1, 2, 3], [0, 1, 4], [1, 2, 4], [2, 3, 4], [0, 3, 4]]
+# element kinds: vertices and local faces, in gmsh vertex order
+KINDS = {"tet": (4, TET_FACES.tolist()), "pyramid": (5, PYRAMID_FACES),
+         "prism": (6, PRISM_FACES), "hex": (8, HEX_FACES.tolist())}
 
 # Kuhn split of a hex (gmsh ordering) into 6 tets along the v0-v6 diagonal;
 # translation invariant, hence conforming between neighbours and across
@@ -151,6 +162,26 @@ def _tet_volume(v):
     return np.abs(_dot(a, _cross(b, c))) * (1.0 / 6.0)
 
 
+def _prism_volume(v):
+    """geometry.py:86-95 (three tetrahedra from vertex 0)."""
+    a, b, c, d, e = (v[:, k] - v[:, 0] for k in range(1, 6))
+    vol = np.abs(_dot(a, _cross(b, e)))
+    vol = vol + np.abs(_dot(a, _cross(e, d)))
+    vol = vol + np.abs(_dot(d, _cross(e, c)))
+    return vol * (1.0 / 6.0)
+
+
+def _pyramid_volume(v):
+    """geometry.py:96-103 (two tetrahedra on the base diagonal)."""
+    a, b, c, d = (v[:, k] - v[:, 0] for k in range(1, 5))
+    vol = np.abs(_dot(a, _cross(b, d)))
+    vol = vol + np.abs(_dot(b, _cross(c, d)))
+    return vol * (1.0 / 6.0)
+
+
+_VOLUME = {"tet": _tet_volume, "pyramid": _pyramid_volume, "prism": _prism_volume, "hex": _hex_volume}
+
+
 def _face_area_normal(v):
     """geometry.py:29-40 (area) and :165-172 (normal, before orientation)."""
     if v.shape[1] == 4:
@@ -186,28 +217,53 @@ def build_mesh(nodes, cell_nodes, cell_shift, cell_type, boundary_region_of_face
     """Assemble a processed mesh.
 
     nodes:       (n_nodes, 3) unique node coordinates
-    cell_nodes:  (n_cells, nv) node ids in gmsh element order
+    cell_nodes:  (n_cells, nv) node ids in gmsh element order (rows of a
+                 mixed mesh padded with -1 to its widest element)
     cell_shift:  (n_cells, nv, 3) translation added to each vertex (periodic
                  unwrapping), zeros for non-periodic meshes
-    cell_type:   "hex" or "tet"
+    cell_type:   "hex", "tet", "prism" or "pyramid", or one of those per cell
     boundary_region_of_face: callable(face_x (m,3), face_n (m,3)) -> region ids
                  for the unmatched (boundary) faces
     boundary_region_of_nodes: alternatively callable(face node ids (m, fv),
-                 each row sorted) -> region ids
+                 each row sorted; with faces of 3 and 4 nodes, triangles
+                 carry a leading -1) -> region ids
     """
-    table = HEX_FACES if cell_type == "hex" else TET_FACES
-    n_cells, nv = cell_nodes.shape
-    nfl = table.shape[0]
-    verts = nodes[cell_nodes] + cell_shift                     # unwrapped vertices
-    cell_x = _mean_vertices(verts)
-    cell_volume = _hex_volume(verts) if cell_type == "hex" else _tet_volume(verts)
-
-    # local faces, in tmp_faces order (cell-major, element-table order)
-    lf_nodes = cell_nodes[:, table].reshape(-1, table.shape[1])      # (n_cells*nfl, fv)
-    lf_verts = verts[:, table, :].reshape(-1, table.shape[1], 3)
-    lf_shift = cell_shift[:, table, :].reshape(-1, table.shape[1], 3)
+    cell_nodes = np.asarray(cell_nodes, dtype=np.int64)
+    n_cells = cell_nodes.shape[0]
+    kinds = np.full(n_cells, cell_type, dtype=object) if isinstance(cell_type, str) else np.asarray(cell_type, dtype=object)
+    if kinds.shape != (n_cells,) or not set(kinds.tolist()) <= set(KINDS):
+        raise ValueError(f"cell kinds must be among {sorted(KINDS)}")
+    # per kind: vertex means and volumes; local faces in tmp_faces order
+    # (cell-major, element-table order), rows padded to 4 nodes
+    nfl = np.array([len(KINDS[k][1]) for k in kinds], dtype=np.int64)
+    lf_start = np.concatenate([[0], np.cumsum(nfl)[:-1]])
+    n_lf = int(nfl.sum())
+    cell_x = np.zeros((n_cells, 3))
+    cell_volume = np.zeros(n_cells)
+    lf_nodes = np.full((n_lf, 4), -1, dtype=np.int64)
+    lf_nv = np.zeros(n_lf, dtype=np.int64)
+    lf_verts = np.zeros((n_lf, 4, 3))
+    lf_shift = np.zeros((n_lf, 4, 3))
     lf_cell = np.repeat(np.arange(n_cells, dtype=np.int64), nfl)
-    key_nodes = np.sort(lf_nodes, axis=1)
+    for kind, (nv, table) in KINDS.items():
+        sel = np.nonzero(kinds == kind)[0]
+        if sel.shape[0] == 0:
+            continue
+        cn = cell_nodes[sel, :nv]
+        verts = nodes[cn] + cell_shift[sel, :nv]               # unwrapped vertices
+        cell_x[sel] = _mean_vertices(verts)
+        cell_volume[sel] = _VOLUME[kind](verts)
+        for j, face in enumerate(table):
+            rows = lf_start[sel] + j
+            w = len(face)
+            lf_nodes[rows, :w] = cn[:, face]
+            lf_nv[rows] = w
+            lf_verts[rows, :w] = verts[:, face]
+            lf_shift[rows, :w] = cell_shift[sel][:, face]
+    fw = 4 if np.any(lf_nv == 4) else 3                         # face width of the mesh
+    if np.all(lf_nv == fw):
+        lf_nodes, lf_verts, lf_shift = lf_nodes[:, :fw], lf_verts[:, :fw], lf_shift[:, :fw]
+    key_nodes = np.sort(lf_nodes, axis=1)                       # triangles: leading -1
     order = np.lexsort(tuple(key_nodes[:, k] for k in range(key_nodes.shape[1] - 1, -1, -1)))
     ks = key_nodes[order]
     same_next = np.zeros(ks.shape[0], dtype=bool)
@@ -230,8 +286,15 @@ def build_mesh(nodes, cell_nodes, cell_shift, cell_type, boundary_region_of_face
     c0 = lf_cell[f_first]
     c1 = np.where(f_second >= 0, lf_cell[np.maximum(f_second, 0)], -1)
     fverts = lf_verts[f_first]
-    face_x = _mean_vertices(fverts)
-    face_area, n = _face_area_normal(fverts)
+    fnv = lf_nv[f_first]
+    face_x = np.zeros((n_faces, 3))
+    face_area = np.zeros(n_faces)
+    n = np.zeros((n_faces, 3))
+    for w in (3, 4):
+        sel = np.nonzero(fnv == w)[0]
+        if sel.shape[0]:
+            face_x[sel] = _mean_vertices(fverts[sel, :w])
+            face_area[sel], n[sel] = _face_area_normal(fverts[sel, :w])
     d = face_x - cell_x[c0]
     cos_angle = _dot(d, n) / (_len(d) * _len(n))
     angle = np.arccos(np.clip(cos_angle, -1.0, 1.0)) * 180 / np.pi
@@ -360,6 +423,55 @@ def periodic_tet_box(n, length=1.0, name=None):
     tn = cn[:, KUHN_TETS].reshape(-1, 4)
     ts = sh[:, KUHN_TETS, :].reshape(-1, 4, 3)
     return build_mesh(nodes, tn, ts, "tet", name=name or f"tet{n}")
+
+
+def mixed_parts(n, length=1.0, jitter=0.0, seed=20240601, periodic=True):
+    """Nodes, cells (rows padded with -1), vertex shifts and kinds of an n^3
+    hex box on [0, length]^3 with two other element kinds mixed in: the
+    columns (i, j) with (i + 2 j) % 5 == 0 split into two prisms per hex
+    along the v0-v2 diagonal (their triangles meet only inside the column,
+    across the periodic wrap too), and outside those columns every hex with
+    (i + j + k) % 4 == 1 split into six pyramids on its faces around its
+    vertex mean (a node of its own).  Every face matches its neighbour's:
+    faces of 3 and 4 nodes, cells of 5 and 6 faces."""
+    xs = np.linspace(0.0, length, n + 1)
+    nodes, cn, sh = _structured(n, n, n, xs, xs, xs, (periodic,) * 3, jitter, seed, (length, length, length))
+    c = np.arange(n ** 3)
+    i, j, k = c % n, (c // n) % n, c // (n * n)
+    prism_col = (i + 2 * j) % 5 == 0
+    pyr = ~prism_col & ((i + j + k) % 4 == 1)
+    rows, shifts, kinds, extra = [], [], [], []
+    n0 = nodes.shape[0]
+    for cell in range(n ** 3):
+        v, d = cn[cell], sh[cell]
+        if prism_col[cell]:
+            for sub in ([0, 1, 2, 4, 5, 6], [0, 2, 3, 4, 6, 7]):
+                rows.append(list(v[sub]) + [-1, -1])
+                shifts.append(np.vstack([d[sub], np.zeros((2, 3))]))
+                kinds.append("prism")
+        elif pyr[cell]:
+            apex = n0 + len(extra)
+            extra.append(_mean_vertices((nodes[v] + d)[None])[0])
+            for f in HEX_FACES:
+                rows.append(list(v[f]) + [apex, -1, -1, -1])
+                shifts.append(np.vstack([d[f], np.zeros((4, 3))]))
+                kinds.append("pyramid")
+        else:
+            rows.append(list(v))
+            shifts.append(d)
+            kinds.append("hex")
+    all_nodes = np.vstack([nodes, np.asarray(extra).reshape(-1, 3)])
+    return all_nodes, np.asarray(rows, dtype=np.int64), np.asarray(shifts), kinds
+
+
+def mixed_box(n, length=1.0, jitter=0.0, seed=20240601, periodic=True, name=None):
+    """The mixed hexahedron / prism / pyramid box of ``mixed_parts``:
+    periodic, or with all outer faces in region 1 ("wall")."""
+    nodes, rows, shifts, kinds = mixed_parts(n, length, jitter, seed, periodic)
+    if periodic:
+        return build_mesh(nodes, rows, shifts, kinds, name=name or f"mixed{n}")
+    return build_mesh(nodes, rows, shifts, kinds, boundary_region_of_face=lambda fx, fn: np.ones(fx.shape[0]),
+                      region_names=("flow", "wall"), region_is_boundary=(0, 1), name=name or f"mixed{n}w")
 
 
 def stretched_coords(n, length, ratio):

@@ -169,3 +169,28 @@ def test_rejects_rotational_periodic_links(tmp_path):
     gmsh.write_msh(p, lat, full, "hex", [], {(3, 1): "fluid"}, periodic=[links])
     with pytest.raises(ValueError, match="translational"):
         gmsh.read_msh(p)
+
+
+@pytest.mark.parametrize("jitter", [0.0, 0.1])
+def test_mixed_elements_round_trip(tmp_path, jitter):
+    """Hexahedra, prisms and pyramids in one Gmsh file (element types 5, 6,
+    7) give the generator's mixed mesh; cells have 5 and 6 faces, faces 3
+    and 4 nodes."""
+    nodes, rows, shifts, kinds = mg.mixed_parts(4, jitter=jitter, periodic=False)
+    ref = mg.mixed_box(4, jitter=jitter, periodic=False)
+    count, first = {}, {}
+    for c, kind in zip(rows, kinds):
+        for face in mg.KINDS[kind][1]:
+            key = tuple(sorted(int(v) for v in c[face]))
+            count[key] = count.get(key, 0) + 1
+            first.setdefault(key, [int(v) for v in c[face]])
+    bnd = [(1, first[k]) for k, n in count.items() if n == 1]
+    p = os.path.join(tmp_path, "mixed.msh")
+    gmsh.write_msh(p, nodes, rows, kinds, bnd, {(2, 1): "wall", (3, 2): "fluid"})
+    m = gmsh.read_msh(p)
+    assert m.region_names == ["flow", "wall"]
+    assert sorted(set(np.bincount(m.cell_n_faces).nonzero()[0])) == [5, 6]
+    for f in ("face_cells", "cell_faces", "cell_n_faces", "boundary_id", "boundary_face", "face_boundary"):
+        assert np.array_equal(getattr(m, f), getattr(ref, f)), f
+    for f in ("cell_x", "cell_volume", "cell_dx", "face_x", "face_n", "face_area", "face_lambda"):
+        assert np.allclose(getattr(m, f), getattr(ref, f), rtol=0, atol=1e-14), f

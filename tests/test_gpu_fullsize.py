@@ -103,3 +103,22 @@ def test_tet64_mixed_bit_identical_repeats(tet64):
             s.step_explicit("rk33", 50, cfl=0.5)
             outs.append(s.get_conserved())
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_mixed_elements_follow_fp64_and_conserve():
+    """Hexahedra, prisms and pyramids (24^3 box, 30,000-odd cells of 5 and
+    6 faces): the mixed path follows the FP64 path over 100 RK3 steps and
+    both conserve mass, momentum and energy on the periodic box."""
+    c = cases.tgv_mixed(24)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with api.from_case(c, prec) as s:
+            s.step_explicit("rk33", 100, cfl=0.5)
+            out[prec] = s.get_conserved()
+    err = rel_l2(out["mixed"], out["fp64"])
+    assert err.max() < MIXED_FULL_TOL, err
+    t0 = totals(c, c.u0)
+    scale = np.abs(c.u0[:, :5] * c.mesh.cell_volume[:, None]).sum(axis=0)
+    scale = np.maximum(scale, scale[0])
+    assert (np.abs(totals(c, out["fp64"]) - t0) / scale).max() < 1e-12
+    assert (np.abs(totals(c, out["mixed"]) - t0) / scale).max() < 1e-6

@@ -38,6 +38,9 @@ SMALL = {
     "tgv_tet3_gg": lambda: cases.tgv_tet(3),
     "tgv_hex4_lsq": lambda: cases.tgv_hex(4),
     "channel_pressure_outlet": lambda: cases.channel(6, 4, 4),
+    # hexahedra, prisms and pyramids: cells of 5 and 6 faces (padded slots)
+    "tgv_mixed5_gg": lambda: cases.tgv_mixed(5),
+    "tgv_mixed5_lsq": lambda: cases.tgv_mixed(5, gradient=cases.LEAST_SQUARES),
 }
 
 
@@ -147,6 +150,8 @@ def test_euler16_low_storage_schemes(oracle, scheme):
 @pytest.mark.parametrize("maker,steps", [
     (lambda: cases.tgv_hex(8), 20),
     (lambda: cases.tgv_tet(8), 20),
+    (lambda: cases.tgv_mixed(6), 20),
+    (lambda: cases.tgv_mixed(6, gradient=cases.LEAST_SQUARES), 20),
 ])
 def test_navier_stokes_fp64_and_mixed(oracle, maker, steps):
     c = maker()

@@ -91,3 +91,21 @@ def test_geometry_matches_reference_preprocessor():
 class types_cell:
     def __init__(self, x):
         self.x_v = np.asarray(x)
+
+
+def test_mixed_element_geometry():
+    """Prism and pyramid geometry (geometry.py:86-103) on the mixed box: with
+    planar faces every cell closes (sum of outward n A = 0) and the volumes
+    tile the box; the pyramids of a split hex add up to the hex."""
+    m = mg.mixed_box(5)
+    assert m.n_boundaries == 0 and sorted(set(m.cell_n_faces.tolist())) == [5, 6]
+    s = np.zeros((m.n_cells, 3))
+    np.add.at(s, m.face_cells[:, 0], m.face_n * m.face_area[:, None])
+    np.add.at(s, m.face_cells[:, 1], -(m.face_n * m.face_area[:, None]))
+    assert np.abs(s).max() < 1e-15
+    assert abs(m.cell_volume.sum() - 1.0) < 1e-14
+    assert np.all((m.face_lambda > 0) & (m.face_lambda < 1))
+    h = 1.0 / 5
+    pyr = m.cell_n_faces == 5
+    assert np.allclose(m.cell_volume[pyr].reshape(-1), np.where(np.isclose(m.cell_volume[pyr], h ** 3 / 6),
+                                                                 h ** 3 / 6, h ** 3 / 2))

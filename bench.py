@@ -45,7 +45,7 @@ def parse():
     p.add_argument("--steps", type=int, default=1000)
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--case", default="tgv_tet", choices=["tgv_tet", "tgv_hex", "euler16", "channel"])
+    p.add_argument("--case", default="tgv_tet", choices=["tgv_tet", "tgv_hex", "tgv_mixed", "euler16", "channel"])
     p.add_argument("--learned", action="store_true",
                    help="channel: also harvest, train and evaluate the learned preconditioner")
     p.add_argument("--n", type=int, default=64)
@@ -64,6 +64,8 @@ def make_case(args):
         return cases.tgv_tet(args.n)
     if args.case == "tgv_hex":
         return cases.tgv_hex(args.n)
+    if args.case == "tgv_mixed":
+        return cases.tgv_mixed(args.n)
     return cases.euler16(args.n)
 
 
@@ -150,7 +152,8 @@ def measured_peaks():
 def cpu_sample(case_args, n_stages, which):
     from oracle import oracle as orc
     from fv3d_gb300 import cases
-    c = {"tgv_tet": cases.tgv_tet, "tgv_hex": cases.tgv_hex, "euler16": cases.euler16}[case_args[0]](case_args[1])
+    c = {"tgv_tet": cases.tgv_tet, "tgv_hex": cases.tgv_hex, "tgv_mixed": cases.tgv_mixed,
+         "euler16": cases.euler16}[case_args[0]](case_args[1])
     o = orc.Oracle(which)
     o.init(c.mesh, c.params, c.region_type, c.region_prim)
     o.set_conserved(c.u0)

@@ -230,6 +230,14 @@ __device__ __forceinline__ void mx_viscous(const float* q, const float* tau, con
   v[3] = ex * nA[0] + ey * nA[1] + ez * nA[2];
 }
 
+// min(1, y) * slope of limiter.c:86-106 without the division: slope capped
+// by max - q when positive, by min - q when negative, 0 when 0.  The
+// cell's own value is part of the neighbourhood min and max, so
+// dmn = min - q <= 0 <= max - q = dmx and the clamp is that selection.
+__device__ __forceinline__ float bj_limited(float slope, float dmn, float dmx) {
+  return fminf(fmaxf(slope, dmn), dmx);
+}
+
 template <int MCF>
 __device__ __forceinline__ void load_cface(const int* __restrict__ cf, int* e) {
   if (MCF == 4) {
@@ -346,8 +354,7 @@ __global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __
       for (int v = 0; v < 8; ++v) {
         const float slope = d.x * g[v][0] + d.y * g[v][1] + d.z * g[v][2];
         float inc = slope;
-        if (LIMIT)  // min(1, y) * slope of limiter.c:86-106 without the division
-          inc = (slope > 0.f) ? fminf(slope, mxv[v] - q[v]) : ((slope < 0.f) ? fmaxf(slope, mn[v] - q[v]) : 0.f);
+        if (LIMIT) inc = bj_limited(slope, mn[v] - q[v], mxv[v] - q[v]);
         r[v] = q[v] + inc;
       }
     } else {
@@ -767,8 +774,7 @@ __device__ __forceinline__ void sides_tile(const MxArgs& a, const unsigned char*
       for (int v = 0; v < 8; ++v) {
         const float slope = d.x * g[v][0] + d.y * g[v][1] + d.z * g[v][2];
         float inc = slope;
-        if (LIMIT)
-          inc = (slope > 0.f) ? fminf(slope, mxv[v] - q[v]) : ((slope < 0.f) ? fmaxf(slope, mn[v] - q[v]) : 0.f);
+        if (LIMIT) inc = bj_limited(slope, mn[v] - q[v], mxv[v] - q[v]);
         r[v] = q[v] + inc;
       }
     } else {

@@ -214,6 +214,24 @@ def test_corrupt_mesh_rejected():
     assert e.value.status == 8  # FV3D_ERR_BOUNDS
 
 
+def test_empty_and_oversized_meshes_rejected():
+    """No cells (empty arrays) and more than 8 face slots per cell are
+    refused with FV3D_ERR_INVALID_ARG before anything reaches the device."""
+    import dataclasses
+    c = cases.euler16(4)
+    m = c.mesh
+    empty = dataclasses.replace(
+        m, cell_x=m.cell_x[:0], cell_volume=m.cell_volume[:0], cell_dx=m.cell_dx[:0],
+        cell_n_faces=m.cell_n_faces[:0], cell_faces=m.cell_faces[:0])
+    with pytest.raises(api.FV3DError) as e:
+        api.Solver(empty, c.params, c.region_type, c.region_prim, "fp64")
+    assert e.value.status == 1  # FV3D_ERR_INVALID_ARG
+    wide = dataclasses.replace(m, cell_faces=np.hstack([m.cell_faces, np.full((m.n_cells, 3), -1, np.int32)]))
+    with pytest.raises(api.FV3DError) as e:
+        api.Solver(wide, c.params, c.region_type, c.region_prim, "fp64")
+    assert e.value.status == 1
+
+
 def test_hdf5_load_unsupported():
     c = cases.euler16(4)
     with api.from_case(c) as s:

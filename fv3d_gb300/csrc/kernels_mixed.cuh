@@ -494,11 +494,11 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
         F[3] += 0.5f * (l1.w + r1.w);
         F[4] += 0.5f * (ve.x + ve.y);
       }
+      // the second cell takes the flux with the opposite sign (sub(x) is
+      // add(-x)): a select, not a divergent branch
+      const float sg = side ? -1.f : 1.f;
 #pragma unroll
-      for (int j = 0; j < 5; ++j) {
-        if (side) s[j].sub(F[j]);
-        else s[j].add(F[j]);
-      }
+      for (int j = 0; j < 5; ++j) s[j].add(sg * F[j]);
     }
     const float rv = __ldg(&a.cgeo[c]).w;
     float rr[5];

@@ -887,49 +887,68 @@ constexpr int sides_buf_stride() {
   return (SidesTile<MCF, GMODE>::total + 127) / 128 * 128;
 }
 
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// persistent staged gradient pass without CTA barriers in the tile loop:
+// each buffer has a "full" mbarrier (the bulk copies' transaction count)
+// and an "empty" one (one arrival per warp after its last read of the
+// tile); only the issuing thread waits for the slowest warp, before it
+// refills a buffer.  Every wait is bounded; a thread that gives up records
+// kStatusStageTimeout, waits (bounded) for the copies of both buffers and
+// leaves.
 template <int MCF, int GMODE, bool LINEAR, bool LIMIT, bool VISC>
 __global__ void __launch_bounds__(kTile) k_mx_sides_tma2(const __grid_constant__ MxArgs a) {
   static_assert(GMODE != 0, "the staged gradient pass needs gradients");
   using L = SidesTile<MCF, GMODE>;
   constexpr int BUF = sides_buf_stride<MCF, GMODE>();
+  constexpr int kWarps = kTile / 32;
   extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) unsigned long long empty_bar[2];
   const int tid = threadIdx.x;
   const int ntiles = a.ncp / kTile;
   int t = blockIdx.x;
   if (t >= ntiles) return;  // whole CTA
   const uint32_t s0 = smem_u32(smem);
-  const uint32_t bar0 = s0 + L::bar, bar1 = s0 + BUF + L::bar;
+  const uint32_t full0 = s0 + L::bar, full1 = s0 + BUF + L::bar;
+  const uint32_t empty0 = smem_u32(&empty_bar[0]), empty1 = smem_u32(&empty_bar[1]);
   if (tid == 0) {
-    mbar_init(bar0, 1);
-    mbar_init(bar1, 1);
+    mbar_init(full0, 1);
+    mbar_init(full1, 1);
+    mbar_init(empty0, kWarps);
+    mbar_init(empty1, kWarps);
     fence_mbar_init();
   }
   __syncthreads();
-  if (tid == 0) sides_issue<MCF, GMODE>(a, s0, bar0, t * kTile);
+  if (tid == 0) sides_issue<MCF, GMODE>(a, s0, full0, t * kTile);
+  constexpr unsigned long long kLimit = 500000000ull;
   for (int i = 0; t < ntiles; ++i, t += gridDim.x) {
     const int b = i & 1;
     const int tn = t + gridDim.x;
+    const uint32_t full = b ? full1 : full0, full_next = b ? full0 : full1;
+    bool ok = true;
     if (tid == 0 && tn < ntiles) {
-      // buffer b^1 was last read in iteration i - 1, which every thread has
-      // finished (the barrier at its end); order those reads before the
-      // asynchronous writes
-      fence_proxy_async_smem();
-      sides_issue<MCF, GMODE>(a, s0 + (b ^ 1) * BUF, b ? bar0 : bar1, tn * kTile);
-    }
-    const uint32_t bar = b ? bar1 : bar0, bar_next = b ? bar0 : bar1;
-    const bool ok = __syncthreads_and(mbar_wait_bounded(bar, (i >> 1) & 1, 500000000ull));
-    if (!ok) {
-      // copies did not land in 0.5 s: report; one more bounded wait on each
-      // buffer still being filled so that no copy outlives the CTA's shared memory
-      if (tid == 0) {
-        atomicOr(&a.sc->status, kStatusStageTimeout);
-        mbar_wait_bounded(bar, (i >> 1) & 1, 500000000ull);
-        if (tn < ntiles) mbar_wait_bounded(bar_next, ((i + 1) >> 1) & 1, 500000000ull);
+      // buffer b^1 held tile i - 1: every warp has arrived on its empty
+      // barrier after reading it
+      if (i >= 1) ok = mbar_wait_bounded(b ? empty0 : empty1, ((i - 1) >> 1) & 1, kLimit);
+      if (ok) {
+        fence_proxy_async_smem();
+        sides_issue<MCF, GMODE>(a, s0 + (b ^ 1) * BUF, full_next, tn * kTile);
       }
+    }
+    if (ok) ok = mbar_wait_bounded(full, (i >> 1) & 1, kLimit);
+    if (!ok) {
+      // no copy may outlive the CTA's shared memory: wait (bounded) for this
+      // tile's and, when it was due, the next tile's
+      atomicOr(&a.sc->status, kStatusStageTimeout);
+      mbar_wait_bounded(full, (i >> 1) & 1, kLimit);
+      if (tn < ntiles) mbar_wait_bounded(full_next, ((i + 1) >> 1) & 1, kLimit);
       return;
     }
     sides_tile<MCF, GMODE, LINEAR, LIMIT, VISC>(a, smem + b * BUF, t * kTile, tid);
-    __syncthreads();  // buffer b is refilled in the next iteration
+    __syncwarp();
+    if ((tid & 31) == 0) mbar_arrive(b ? empty1 : empty0);
   }
 }
 

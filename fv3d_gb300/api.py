@@ -139,6 +139,7 @@ EXPORTS = {
     "fv3d_profile_stage": ([C.c_void_p, C.c_int, C.c_double, _f8p], C.c_int),
     "fv3d_get_stream": ([C.c_void_p, C.POINTER(C.c_void_p)], C.c_int),
     "fv3d_device_state": ([C.c_void_p, C.POINTER(_f8p)], C.c_int),
+    "fv3d_selftest_bounded_wait": ([C.c_void_p, C.c_int, C.POINTER(C.c_int), _f8p], C.c_int),
     "fv3d_implicit_default_opts": ([C.POINTER(ImplicitOpts)], C.c_int),
     "fv3d_solve_implicit": ([C.c_void_p, C.POINTER(ImplicitOpts), C.POINTER(ImplicitStats)], C.c_int),
     "fv3d_implicit_history": ([C.c_void_p, _f8p, C.c_int, C.POINTER(C.c_int)], C.c_int),
@@ -441,6 +442,12 @@ class Solver:
         self._check(self.lib.fv3d_mlp_train(self.h, C.byref(MlpTrainOpts(epochs, batch, lr, seed)),
                                             C.byref(st)))
         return {f: getattr(st, f) for f, _ in MlpTrainStats._fields_}
+
+    def selftest_bounded_wait(self, limit_us: int = 2000):
+        """(timed_out, elapsed_ms) of a bounded wait on a phase nothing completes."""
+        flag, ms = C.c_int(), C.c_double()
+        self._check(self.lib.fv3d_selftest_bounded_wait(self.h, limit_us, C.byref(flag), C.byref(ms)))
+        return flag.value, ms.value
 
     def stream(self) -> int:
         s = C.c_void_p()

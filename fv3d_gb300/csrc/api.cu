@@ -427,6 +427,31 @@ extern "C" fv3d_status fv3d_get_stream(const fv3d_ctx* handle, void** stream) {
   return FV3D_OK;
 }
 
+extern "C" fv3d_status fv3d_selftest_bounded_wait(fv3d_ctx* handle, int limit_us, int* timed_out, double* elapsed_ms) {
+  if (handle == nullptr || timed_out == nullptr || limit_us <= 0 || limit_us > 1000000) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  CK(cudaSetDevice(ctx->cfg.device));
+  DevBuf<int> flag;
+  CK(flag.alloc(1));
+  CK(cudaMemsetAsync(flag.p, 0xff, sizeof(int), ctx->stream));
+  cudaEvent_t ev[2];
+  CK(cudaEventCreate(&ev[0]));
+  CK(cudaEventCreate(&ev[1]));
+  CK(cudaEventRecord(ev[0], ctx->stream));
+  CK(launch_bounded_wait_probe(1000ull * (unsigned long long)limit_us, flag.p, ctx->stream));
+  CK(cudaEventRecord(ev[1], ctx->stream));
+  int h = -1;
+  CK(cudaMemcpyAsync(&h, flag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, ev[0], ev[1]));
+  cudaEventDestroy(ev[0]);
+  cudaEventDestroy(ev[1]);
+  *timed_out = h;
+  if (elapsed_ms) *elapsed_ms = ms;
+  return FV3D_OK;
+}
+
 extern "C" fv3d_status fv3d_device_state(const fv3d_ctx* handle, double** u) {
   if (handle == nullptr || u == nullptr) return FV3D_ERR_INVALID_ARG;
   const Ctx* ctx = reinterpret_cast<const Ctx*>(handle);

@@ -91,6 +91,25 @@ cudaError_t setup_mx_sides() {
 #endif
 }
 
+// self-test of the bounded mbarrier wait the staged gradient pass uses: a
+// phase that expects 16 bytes no copy will deliver; the wait gives up after
+// limit_ns and the kernel records that in *flag (1 = gave up)
+__global__ void k_bounded_wait_probe(unsigned long long limit_ns, int* flag) {
+  __shared__ __align__(8) unsigned long long bar;
+  const uint32_t b = smem_u32(&bar);
+  if (threadIdx.x == 0) {
+    mbar_init(b, 1);
+    fence_mbar_init();
+    mbar_expect_tx(b, 16);  // arrives, leaving 16 bytes outstanding
+    *flag = mbar_wait_bounded(b, 0, limit_ns) ? 0 : 1;
+  }
+}
+
+cudaError_t launch_bounded_wait_probe(unsigned long long limit_ns, int* flag, cudaStream_t s) {
+  k_bounded_wait_probe<<<1, 32, 0, s>>>(limit_ns, flag);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_mx_sides(const MxArgs& a, const Disc& d, cudaStream_t s) {
   const int B = (a.nc + 255) / 256;
   if (a.mcf == 4) sides_mcf<4>(a, d, s, B);

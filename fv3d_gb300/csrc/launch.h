@@ -18,6 +18,7 @@ struct Disc {
 struct MxArgs;
 cudaError_t launch_mx_sides(const MxArgs& a, const Disc& d, cudaStream_t s);
 cudaError_t setup_mx_sides();
+cudaError_t launch_bounded_wait_probe(unsigned long long limit_ns, int* flag, cudaStream_t s);
 cudaError_t launch_mx_flux_update(const MxArgs& a, const Disc& d, int mode, bool dt,
                                   const StageCoef& co, cudaStream_t s);
 

@@ -352,6 +352,13 @@ fv3d_status fv3d_profile_stage(fv3d_ctx *ctx, int n_reps, double cfl, double *ms
 fv3d_status fv3d_get_stream(const fv3d_ctx *ctx, void **stream);
 /* device pointer of the conserved state, [5][n_cells] SoA in renumbered order */
 fv3d_status fv3d_device_state(const fv3d_ctx *ctx, double **u_dev);
+/* No counterpart in the reference.  Self-test of the bounded device waits
+ * (the staged gradient pass's mbarrier waits, which report FV3D_ERR_TIMEOUT
+ * instead of hanging): one wait on a phase that no copy completes, limited
+ * to limit_us (1 .. 1,000,000); *timed_out = 1 when the kernel gave up and
+ * said so, *elapsed_ms the kernel's device time (may be NULL).  Nothing is
+ * left pending: no copy was issued. */
+fv3d_status fv3d_selftest_bounded_wait(fv3d_ctx *ctx, int limit_us, int *timed_out, double *elapsed_ms);
 
 #ifdef __cplusplus
 }

@@ -45,7 +45,7 @@ __global__ void k_import(int nc, const int* __restrict__ perm, const double* __r
     float T = p / (rho * (float)R);
     float4* d = reinterpret_cast<float4*>(Uf) + 2 * (size_t)c;
     d[0] = make_float4(rho, mx, my, mz);
-    d[1] = make_float4((float)u[4], p, T, 0.f);
+    d[1] = make_float4((float)u[4], p, T, 1.0f / rho);
     float4* b = reinterpret_cast<float4*>(UfN) + 2 * (size_t)c;
     b[0] = d[0];
     b[1] = d[1];
@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(kIoRows) k_import_host(int nc, const int* __re
     float T = p / (rho * (float)R);
     float4* d = reinterpret_cast<float4*>(Uf) + 2 * (size_t)c;
     d[0] = make_float4(rho, mx, my, mz);
-    d[1] = make_float4((float)u[4], p, T, 0.f);
+    d[1] = make_float4((float)u[4], p, T, 1.0f / rho);
     float4* b = reinterpret_cast<float4*>(UfN) + 2 * (size_t)c;
     b[0] = d[0];
     b[1] = d[1];

@@ -436,7 +436,7 @@ __global__ void k_jv_combine(int nc, const T* __restrict__ z, const double* __re
 }
 
 
-// FP32 state record (rho, m, E, p, T) of a cell's FP64 state w[5]
+// FP32 state record (rho, m, E, p, T, 1/rho) of a cell's FP64 state w[5]
 __device__ __forceinline__ void put_record(float* __restrict__ Uf, int c, const double* w, float km1, float R) {
   const float rho = (float)w[0], mx = (float)w[1], my = (float)w[2], mz = (float)w[3];
   const double E = w[4];
@@ -445,7 +445,7 @@ __device__ __forceinline__ void put_record(float* __restrict__ Uf, int c, const 
   const float p = fmaxf(1.00E-10f, (float)((double)km1 * (E - (double)ke)));
   float4* d = reinterpret_cast<float4*>(Uf) + 2 * (size_t)c;
   d[0] = make_float4(rho, mx, my, mz);
-  d[1] = make_float4((float)E, p, p * ir / R, 0.f);
+  d[1] = make_float4((float)E, p, p * ir / R, ir);
 }
 
 // the records of the finite-difference state W = U + eps z (eps on the
@@ -462,7 +462,7 @@ __global__ void k_fd_record(int nc, const double* __restrict__ U, const T* __res
   put_record(Uf, c, w, km1, R);
 }
 
-// FP32 state record (rho, m, E, p, T) of an FP64 state W (renumbered SoA)
+// FP32 state record (rho, m, E, p, T, 1/rho) of an FP64 state W (renumbered SoA)
 __global__ void k_make_record(int nc, const double* __restrict__ W, float* __restrict__ Uf,
                               float km1, float R) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -475,7 +475,7 @@ __global__ void k_make_record(int nc, const double* __restrict__ W, float* __res
   const float p = fmaxf(1.00E-10f, (float)((double)km1 * (E - (double)ke)));
   float4* d = reinterpret_cast<float4*>(Uf) + 2 * (size_t)c;
   d[0] = make_float4(rho, mx, my, mz);
-  d[1] = make_float4((float)E, p, p * ir / R, 0.f);
+  d[1] = make_float4((float)E, p, p * ir / R, ir);
 }
 
 // ---- first-order FD diagonal blocks ---------------------------------------

@@ -60,7 +60,7 @@ struct KArgs {
   double* U;                       // [5][nc] conserved state (FP64)
   double* K;                       // [5][nc] low-storage RK register
   double* U0;                      // [5][nc] SSP-RK3 stage-0 state
-  float* Uf;                       // [nc][8] FP32 shadow (rho, m, E, p, T, -)
+  float* Uf;                       // [nc][8] FP32 shadow (rho, m, E, p, T, 1/rho)
   R* rec;                          // [nc][REC]
   R* FA;                           // [nf][FAS]
   double* dphi;                    // [5][nc] residual output
@@ -409,7 +409,7 @@ __global__ void __launch_bounds__(256) k_gather_update(const __grid_constant__ K
           p = fmaxf(1.00E-10f, p);
           float T = p / (rho * (float)a.pc.R_mix);
           sh[0] = make_float4(rho, mx, my, mz);
-          sh[1] = make_float4((float)u[4], p, T, 0.f);
+          sh[1] = make_float4((float)u[4], p, T, 1.0f / rho);
           if (DT) {
             float pu = vx, pv = vy, pw = vz, pp = p;
             if (MODE == 1) { pu = o0.y / o0.x; pv = o0.z / o0.x; pw = o0.w / o0.x; pp = o1.y; }

@@ -86,7 +86,7 @@ struct MxArgs {
   const int* __restrict__ fregion;   // [nf - nf_int]
   const float4* __restrict__ cgeo;   // [ncp] (sum_f s_f n_f A_f, 1/V)
   const float4* __restrict__ cdx;    // [ncp] (dx, V)
-  float* Uf;                         // [nc][8] stage state (rho, m, E, p, T, -)
+  float* Uf;                         // [nc][8] stage state (rho, m, E, p, T, 1/rho)
   float* UfN;                        // [nc][8] float(U_n) + p, T
   float* fs;                         // [nf][FREC]
   float* fsv;                        // [nf][2]
@@ -107,9 +107,11 @@ struct MxPhys {
   }
 };
 
+// record (rho, m, E), (E, p, T, 1/rho): every writer stores the IEEE
+// reciprocal 1.0f / rho in the last word, so readers need no division
 __device__ __forceinline__ void mx_unpack(const float4 x, const float4 y, float* q) {
   q[RHO] = x.x; q[MX] = x.y; q[MY] = x.z; q[MZ] = x.w; q[EN] = y.x; q[PR] = y.y; q[TT] = y.z;
-  const float ir = 1.0f / x.x;
+  const float ir = y.w;
   q[VU] = x.y * ir; q[VV] = x.z * ir; q[VW] = x.w * ir;
 }
 
@@ -456,7 +458,7 @@ __device__ __forceinline__ void mx_make_state(float rho, float mx, float my, flo
   const float ke = 0.5f * (mx * mx + my * my + mz * mz) * ir;
   const float p = fmaxf(1.00E-10f, ph.km1 * (E - ke));
   x = make_float4(rho, mx, my, mz);
-  y = make_float4(E, p, p * ir / ph.R, 0.f);
+  y = make_float4(E, p, p * ir / ph.R, ir);
 }
 
 // MODE 0: residual only; 1: low-storage RK stage; 2: SSP-RK3 stage.
@@ -568,7 +570,7 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
         float pu = un[1] * ir, pv = un[2] * ir, pw = un[3] * ir;
         float pp = fmaxf(1.00E-10f, ph.km1 * (un[4] - 0.5f * (un[1] * pu + un[2] * pv + un[3] * pw)));
         if (MODE == 1) {
-          const float io = 1.f / o0.x;
+          const float io = o1.w;  // 1 / rho of the stage-input record
           pu = o0.y * io; pv = o0.z * io; pw = o0.w * io; pp = o1.y;
         }
         const float cs = sqrtf(ph.kappa * pp * ir);

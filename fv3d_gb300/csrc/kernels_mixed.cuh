@@ -226,10 +226,8 @@ __device__ __forceinline__ void mx_viscous(const float* q, const float* tau, con
   v[0] = -(txx * nA[0] + txy * nA[1] + txz * nA[2]);
   v[1] = -(txy * nA[0] + tyy * nA[1] + tyz * nA[2]);
   v[2] = -(txz * nA[0] + tyz * nA[1] + tzz * nA[2]);
-  const float ex = -txx * q[VU] - txy * q[VV] - txz * q[VW] - k * gT[0];
-  const float ey = -txy * q[VU] - tyy * q[VV] - tyz * q[VW] - k * gT[1];
-  const float ez = -txz * q[VU] - tyz * q[VV] - tzz * q[VW] - k * gT[2];
-  v[3] = ex * nA[0] + ey * nA[1] + ez * nA[2];
+  // (-tau u - k grad T) . nA = u . (-tau nA) - k grad T . nA (tau symmetric)
+  v[3] = q[VU] * v[0] + q[VV] * v[1] + q[VW] * v[2] - k * (gT[0] * nA[0] + gT[1] * nA[1] + gT[2] * nA[2]);
 }
 
 // min(1, y) * slope of limiter.c:86-106 without the division: slope capped

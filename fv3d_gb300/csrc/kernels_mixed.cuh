@@ -9,9 +9,9 @@
 //                    written by its interior cell).
 //  k_mx_flux_update  (flux + update pass, cell-gather) per cell: for each of
 //                    its faces the convective flux from both side records
-//                    plus the averaged viscous flux, summed with Kahan
-//                    compensation in ascending reference face id, -sum/V,
-//                    RK stage update, FP32 stage state, next time step.
+//                    plus the averaged viscous flux, summed in ascending
+//                    reference face id, -sum/V, RK stage update, FP32
+//                    stage state, next time step.
 //
 // Each face flux is evaluated by both of its cells from identical inputs with
 // identical instructions, so the two contributions cancel exactly and the
@@ -463,9 +463,11 @@ __device__ __forceinline__ void mx_make_state(float rho, float mx, float my, flo
 // co.first / co.last mark the step's first and last stage.
 // STORE: also store the stage's time derivative in dphi (co.store_r; a
 // template flag: a run-time test of it costs the hot instantiations 2 %)
+// resident blocks: 5 (48 registers) for 4 face slots, where the gathers
+// need the warps (-4 % per stage); wider cells keep their registers
 template <int MCF, int MODE, bool DT, bool VISC, bool STORE = false>
-__global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(const __grid_constant__ MxArgs a,
-                                                        StageCoef co) {
+__global__ void __launch_bounds__(256, MCF == 4 ? 5 : FV3D_FLUX_MINBLOCKS)
+    k_mx_flux_update(const __grid_constant__ MxArgs a, StageCoef co) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long lam_bits = 0x7ff0000000000000ull;
   bool finite = true;
@@ -474,7 +476,11 @@ __global__ void __launch_bounds__(256, FV3D_FLUX_MINBLOCKS) k_mx_flux_update(con
     ph.load(a.pc);
     int e[MCF];
     load_cface<MCF>(a.cface + (size_t)c * MCF, e);
-    Acc<float, true> s[5];
+    // plain FP32 sums in slot order (ascending reference face id): with 4
+    // to 8 terms a compensated sum changed the state after 500 steps by
+    // nothing measurable (the faces' FP32 arithmetic dominates) and cost
+    // the registers that keep 5 blocks of the 4-face kernel resident
+    Acc<float, false> s[5];
 #pragma unroll kFluxUnroll
     for (int k = 0; k < MCF; ++k) {
       if (e[k] < 0) continue;

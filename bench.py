@@ -308,8 +308,12 @@ def main():
     ms = max_over_ranks(st["elapsed_ms"], dist)
     n_stages = args.steps * nst
     value = whole_job_value(case.mesh.n_cells, n_stages, ms, world)
-    # per-kernel durations (CUDA events around each launch on the context stream)
-    kms = s.profile_stage(20, 0.5)
+    # per-kernel durations (CUDA events around each launch on the context
+    # stream), weighted as a step runs them: the last stage's flux pass also
+    # computes the next time step, the other stages' do not
+    k_last = [float(x) for x in s.profile_stage(20, 0.5)]
+    k_inner = [float(x) for x in s.profile_stage(20, 0.0)]
+    kms = [(a + (nst - 1) * b) / nst for a, b in zip(k_last, k_inner)]
     model = byte_model(case, args.precision)
     if args.precision == "mixed":
         # two launches per stage: k_mx_sides (gradient pass), k_mx_flux_update
@@ -336,6 +340,8 @@ def main():
                 "unit": "GB/s", "frac": round(achieved / peak, 4), "traffic": traffic,
                 "peak_kind": peak_kind, "algorithmic_bytes": kbytes[dom],
                 "kernel_ms": {k: round(t, 5) for k, t in zip(kernels, kt)},
+                "kernel_ms_last_stage": [round(x, 5) for x in k_last[:2]],
+                "kernel_ms_inner_stage": [round(x, 5) for x in k_inner[:2]],
                 "stage_ms": round(stage_ms, 5),
                 "stage_frac": round(model["stage"] / (stage_ms * 1e-3) / 1e9 / peak, 4),
                 "stage_bytes": model["stage"]}

@@ -170,19 +170,22 @@ __device__ __forceinline__ void st_group(T* p, const T* x) {
 }
 
 // ---- fused Gram-Schmidt passes -------------------------------------------
-// One pass over w and the k basis vectors per step of classical Gram-Schmidt
-// with re-orthogonalisation, each ending with a fixed-order reduction done
-// by the grid's last block (an atomic ticket; the block partials are summed
-// in block order, so the result does not depend on which block is last):
+// Classical Gram-Schmidt with one re-orthogonalisation in three passes over
+// w and the k basis vectors; a pass with sums ends with a fixed-order
+// reduction by the grid's last block (an atomic ticket; the block partials
+// are summed in block order, so the result does not depend on which block
+// is last):
 //   PASS 1  h_j = w . V_j
-//   PASS 2  w <- w - sum_j h_j V_j, then h'_j = w . V_j of the new w
-//   PASS 3  w <- w - sum_j h'_j V_j, then |w| (and 1/|w|)
+//   PASS 2  w <- w - sum_j h_j V_j, then h'_j = w . V_j and |w|^2 of the
+//           new w; the last block also forms |w - sum_j h'_j V_j| =
+//           sqrt(|w|^2 - sum_j h'_j^2) (V orthonormal) and its inverse
+//   PASS 3  v_{k+1} = (w - sum_j h'_j V_j) / that norm, no sums
 //   PASS 0  |w| alone
 // Products and sums in T (FP32 basis: FP32 pipe), the final sums and the
 // coefficients in FP64.
 template <class T>
 __device__ void gs_finalize(const T* __restrict__ partial, int nb, int k, double* __restrict__ out, bool norm,
-                            double c, unsigned int* counter) {
+                            double c, unsigned int* counter, double* __restrict__ out2 = nullptr) {
   __shared__ bool last;
   // the threads that wrote this block's partials make them visible, then
   // one thread takes the ticket
@@ -219,13 +222,27 @@ __device__ void gs_finalize(const T* __restrict__ partial, int nb, int k, double
       }
     }
   }
+  if (out2 != nullptr) {
+    // column 31: |w|^2; the norm of w - sum_j out_j V_j by Pythagoras
+    __syncthreads();
+    if (warp == 0) {
+      T s0 = T(0);
+      for (int b = lane; b < nb; b += 32) s0 += __ldcg(partial + (size_t)b * 32 + 31);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+      if (lane == 0) {
+        double hh = 0.0;
+        for (int j = 0; j < k; ++j) hh += out[j] * out[j];
+        const double b2 = (double)s0 - hh;
+        const double r = (b2 > 0.0) ? sqrt(b2) : 0.0;
+        out2[0] = r;
+        out2[1] = (r > 0.0) ? 1.0 / r : 0.0;
+      }
+    }
+  }
   if (threadIdx.x == 0) *counter = 0u;  // ready for the next pass
 }
 
-// one group of G consecutive elements i.. of a Gram-Schmidt pass: G = 16 /
-// sizeof(T) with 16-byte loads (the main loop), G = 1 for the n % G tail.
-// PASS 2 reads each V_j twice (for w - sum h_j V_j, then for the new dots):
-// the second read finds the group in cache
 // w = z / dt_i - (R(U + eps z) - R(U)) / eps (k_jv_combine's arithmetic),
 // formed inside the first Gram-Schmidt pass when z is set
 template <class T>
@@ -238,9 +255,15 @@ struct JvArgs {
   size_t nc = 0;
 };
 
+// one group of G consecutive elements i.. of a Gram-Schmidt pass: G = 16 /
+// sizeof(T) with 16-byte loads (the main loop), G = 1 for the n % G tail.
+// PASS 2 reads each V_j twice (for w - sum h_j V_j, then for the new dots):
+// the second read finds the group in cache.  acc: PASS 1 / 2 the dots (and
+// for PASS 2 |w|^2 at KMAX), PASS 0 the norm; PASS 3 writes vout * scale.
 template <int KMAX, int PASS, int G, class T>
 __device__ __forceinline__ void gs_group(T* __restrict__ w, const T* __restrict__ V, size_t ldb, size_t i, int k,
-                                         const T* hs, T* acc, const JvArgs<T>& jv, T ieps) {
+                                         const T* hs, T* acc, const JvArgs<T>& jv, T ieps, T* __restrict__ vout,
+                                         T scale) {
   T wi[G];
   if (PASS == 1 && jv.z != nullptr) {
     T zi[G];
@@ -282,8 +305,8 @@ __device__ __forceinline__ void gs_group(T* __restrict__ w, const T* __restrict_
     T wn[G];
 #pragma unroll
     for (int l = 0; l < G; ++l) wn[l] = wi[l] - sum[l];
-    st_group<G>(w + i, wn);
     if (PASS == 2) {
+      st_group<G>(w + i, wn);
 #pragma unroll
       for (int j = 0; j < KMAX; ++j)
         if (j < k) {
@@ -292,9 +315,12 @@ __device__ __forceinline__ void gs_group(T* __restrict__ w, const T* __restrict_
 #pragma unroll
           for (int l = 0; l < G; ++l) acc[j] = fmadd(wn[l], v[l], acc[j]);
         }
+#pragma unroll
+      for (int l = 0; l < G; ++l) acc[KMAX] = fmadd(wn[l], wn[l], acc[KMAX]);
     } else {
 #pragma unroll
-      for (int l = 0; l < G; ++l) acc[0] = fmadd(wn[l], wn[l], acc[0]);
+      for (int l = 0; l < G; ++l) wn[l] *= scale;
+      st_group<G>(vout + i, wn);
     }
   }
 }
@@ -303,51 +329,50 @@ template <int KMAX, int PASS, class T>
 __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : FV3D_GS_MINBLOCKS)
     k_gs(size_t n, size_t ldb, T* __restrict__ w, const T* __restrict__ V, int k, const double* __restrict__ h_in,
          T* __restrict__ partial, unsigned int* counter, double* __restrict__ out, double c,
-         const double* __restrict__ c_dev, const JvArgs<T> jv) {
+         const double* __restrict__ c_dev, const JvArgs<T> jv, double* __restrict__ out2, T* __restrict__ vout,
+         const double* __restrict__ scale_p) {
+  static_assert(KMAX <= 32, "at most 32 basis vectors");
   if (c_dev != nullptr) c = *c_dev;  // the finite-difference scale, set per Newton step
   const T ieps = (PASS == 1 && jv.z != nullptr) ? (T)*jv.ieps : T(0);
+  const T scale = (PASS == 3) ? (T)*scale_p : T(0);
   __shared__ T hs[32];
   __shared__ T sh[8][32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (PASS >= 2 && threadIdx.x < 32) hs[threadIdx.x] = (threadIdx.x < (unsigned)k) ? (T)h_in[threadIdx.x] : T(0);
   __syncthreads();
-  constexpr int NA = (PASS == 0 || PASS == 3) ? 1 : KMAX;
+  constexpr int NA = (PASS == 0 || PASS == 3) ? 1 : (PASS == 2 ? KMAX + 1 : KMAX);
   constexpr int L = 16 / sizeof(T);
   T acc[NA];
 #pragma unroll
   for (int j = 0; j < NA; ++j) acc[j] = T(0);
   const size_t stride = (size_t)gridDim.x * blockDim.x, gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   const size_t nq = n / L;
-  for (size_t q = gid; q < nq; q += stride) gs_group<KMAX, PASS, L>(w, V, ldb, q * L, k, hs, acc, jv, ieps);
-  for (size_t i = nq * L + gid; i < n; i += stride) gs_group<KMAX, PASS, 1>(w, V, ldb, i, k, hs, acc, jv, ieps);
-  const int kk = (NA == 1) ? 1 : k;
+  for (size_t q = gid; q < nq; q += stride)
+    gs_group<KMAX, PASS, L>(w, V, ldb, q * L, k, hs, acc, jv, ieps, vout, scale);
+  for (size_t i = nq * L + gid; i < n; i += stride)
+    gs_group<KMAX, PASS, 1>(w, V, ldb, i, k, hs, acc, jv, ieps, vout, scale);
+  if (PASS == 3) return;  // no sums
+  const int kk = (PASS == 0) ? 1 : k;
+  // PASS 2: |w|^2 goes to column 31 (k <= 31 vectors use columns 0 .. 30)
 #pragma unroll
   for (int j = 0; j < NA; ++j) {
-    if (j >= kk) break;
+    const bool take = (PASS == 2 && j == KMAX) || j < kk;
+    if (!take) continue;
     T v = acc[j];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) sh[warp][j] = v;
+    if (lane == 0) sh[warp][(PASS == 2 && j == KMAX) ? 31 : j] = v;
   }
   __syncthreads();
-  if (threadIdx.x < 32 && (int)threadIdx.x < kk) {
+  if (threadIdx.x < 32 && ((int)threadIdx.x < kk || (PASS == 2 && threadIdx.x == 31))) {
     T s = T(0);
 #pragma unroll
     for (int wv = 0; wv < 8; ++wv) s += sh[wv][threadIdx.x];
     partial[(size_t)blockIdx.x * 32 + threadIdx.x] = s;
   }
-  gs_finalize<T>(partial, gridDim.x, kk, out, PASS == 0 || PASS == 3, c, counter);
+  gs_finalize<T>(partial, gridDim.x, kk, out, PASS == 0, c, counter, PASS == 2 ? out2 : nullptr);
 }
 
-// out = x * (*s) when *s > 0 (s = 1/|x| from k_dots_final: the new Arnoldi vector)
-template <class T>
-__global__ void k_scale_dev(size_t n, const T* __restrict__ x, const double* __restrict__ s, T* __restrict__ out) {
-  const double r = *s;
-  if (!(r > 0.0)) return;
-  const T rt = (T)r;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    out[i] = x[i] * rt;
-}
 
 // out = a x + b y (FP64 inputs) stored as T
 template <class T>
@@ -862,7 +887,9 @@ fv3d_status Implicit::dots_dev(Ctx& ctx, const T* wv, const T* Vb, int k, double
 // one fused Gram-Schmidt pass (k_gs) over a fixed grid of RED_BLOCKS blocks
 template <class T>
 fv3d_status Implicit::gs_pass(Ctx& ctx, int pass, T* wv, const T* Vb, int k, const double* h_in, double* dst,
-                              double c, const double* c_dev, const T* jv_z) {
+                              double c, const double* c_dev, const T* jv_z, double* dst2, T* vout,
+                              const double* scale) {
+  if (pass == 2 && k > 31) return ctx.fail(FV3D_ERR_INVALID_ARG, "Gram-Schmidt pass over %d > 31 vectors", k);
   JvArgs<T> jv;
   if (jv_z != nullptr) {
     jv.z = jv_z; jv.Rp = Rp.p; jv.Rb = Rb.p; jv.idt = idtl.p; jv.ieps = jv_ieps; jv.nc = (size_t)ctx.nc;
@@ -870,7 +897,9 @@ fv3d_status Implicit::gs_pass(Ctx& ctx, int pass, T* wv, const T* Vb, int k, con
   const int nb = std::min(RED_BLOCKS, blocks(n));
   T* pt = reinterpret_cast<T*>(part.p);
   unsigned int* ctr = reinterpret_cast<unsigned int*>(bits.p + 1);  // zero between passes
-#define GS_LAUNCH(KM, P) k_gs<KM, P, T><<<nb, 256, 0, ctx.stream>>>(n, ldb, wv, Vb, k, h_in, pt, ctr, dst, c, c_dev, jv)
+#define GS_LAUNCH(KM, P)                                                                                   \
+  k_gs<KM, P, T><<<nb, 256, 0, ctx.stream>>>(n, ldb, wv, Vb, k, h_in, pt, ctr, dst, c, c_dev, jv, dst2, vout, \
+                                             scale)
   if (pass == 0) GS_LAUNCH(1, 0);
   else if (pass == 3) { if (k <= 8) GS_LAUNCH(8, 3); else if (k <= 16) GS_LAUNCH(16, 3); else GS_LAUNCH(32, 3); }
   else if (pass == 1) { if (k <= 8) GS_LAUNCH(8, 1); else if (k <= 16) GS_LAUNCH(16, 1); else GS_LAUNCH(32, 1); }
@@ -986,10 +1015,13 @@ fv3d_status Implicit::enqueue_arnoldi(Ctx& ctx, T* Vt, T* Zt, T* wt, int k) {
   // w = A z_k formed inside the first Gram-Schmidt pass
   if ((st = fd_residual<T>(ctx, zk, opts.preconditioner == FV3D_PC_NONE)) != FV3D_OK) return st;
   if ((st = gs_pass<T>(ctx, 1, wt, Vt, k + 1, nullptr, hdev.p, 0.0, nullptr, zk)) != FV3D_OK) return st;
-  if ((st = gs_pass<T>(ctx, 2, wt, Vt, k + 1, hdev.p, hdev.p + 32, 0.0, nullptr)) != FV3D_OK) return st;
-  if ((st = gs_pass<T>(ctx, 3, wt, Vt, k + 1, hdev.p + 32, hdev.p + 64, 1.0, nullptr)) != FV3D_OK) return st;
-  k_scale_dev<T><<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, wt, hdev.p + 65, Vt + (size_t)(k + 1) * ldb);
-  ICK(cudaGetLastError());
+  // h' into slots 32.., |w - V h'| and its inverse into 64, 65
+  if ((st = gs_pass<T>(ctx, 2, wt, Vt, k + 1, hdev.p, hdev.p + 32, 0.0, nullptr, nullptr, hdev.p + 64)) != FV3D_OK)
+    return st;
+  // v_{k+1} = (w - V h') / |w - V h'|
+  if ((st = gs_pass<T>(ctx, 3, wt, Vt, k + 1, hdev.p + 32, nullptr, 0.0, nullptr, nullptr, nullptr,
+                       Vt + (size_t)(k + 1) * ldb, hdev.p + 65)) != FV3D_OK)
+    return st;
   ICK(cudaMemcpyAsync(hcols + (size_t)k * kHostCoefs, hdev.p, sizeof(double) * kHostCoefs, cudaMemcpyDeviceToHost,
                       ctx.stream));
   return FV3D_OK;

@@ -79,7 +79,8 @@ struct Implicit {
   fv3d_status dots_dev(Ctx& ctx, const T* w, const T* V, int k, double* dst, bool take_sqrt, double c);
   template <class T>
   fv3d_status gs_pass(Ctx& ctx, int pass, T* w, const T* V, int k, const double* h_in, double* dst, double c,
-                      const double* c_dev, const T* jv_z = nullptr);
+                      const double* c_dev, const T* jv_z = nullptr, double* dst2 = nullptr, T* vout = nullptr,
+                      const double* scale = nullptr);
   fv3d_status norm(Ctx& ctx, const double* v, double* out);
   fv3d_status ICK_copy(Ctx& ctx, double* dst, const double* src);
 

@@ -132,6 +132,8 @@ EXPORTS = {
     "fv3d_set_bdf_history": ([C.c_void_p, C.c_int, C.c_int, _f8p], C.c_int),
     "fv3d_time_derivative": ([C.c_void_p, C.c_double, _f8p], C.c_int),
     "fv3d_timestep": ([C.c_void_p, C.c_double, _f8p], C.c_int),
+    "fv3d_step_explicit_io": ([C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double, _f8p, _f8p,
+                               C.POINTER(StepStats)], C.c_int),
     "fv3d_step_explicit": ([C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_double,
                             C.POINTER(StepStats)], C.c_int),
     "fv3d_global_residual": ([C.c_void_p, C.c_double, _f8p], C.c_int),
@@ -298,6 +300,21 @@ class Solver:
         st = StepStats()
         self._check(self.lib.fv3d_step_explicit(self.h, SCHEMES[scheme], n_steps, cfl, dt_fixed,
                                                 C.byref(st)))
+        return {"t": st.t, "dt": st.dt, "steps": st.steps, "elapsed_ms": st.elapsed_ms}
+
+    def step_explicit_io(self, scheme: str, n_steps: int, cfl: float = 0.0, u_in=None, u_out=None,
+                         dt_fixed: float = 0.0):
+        """Host state in, n_steps explicit steps, host state out, in one call
+        with one synchronisation (u_in / u_out: C-contiguous float64 arrays
+        of shape (n_cells, 5), page-locked for direct access; may be the same
+        array; None keeps the state on the device)."""
+        for u in (u_in, u_out):
+            if u is not None and (u.shape != (self.nc, 5) or u.dtype != np.float64 or not u.flags.c_contiguous):
+                raise ValueError("host states must be C-contiguous float64 arrays of shape (n_cells, 5)")
+        st = StepStats()
+        self._check(self.lib.fv3d_step_explicit_io(
+            self.h, SCHEMES[scheme], n_steps, cfl, dt_fixed, None if u_in is None else _p(u_in, _f8p),
+            None if u_out is None else _p(u_out, _f8p), C.byref(st)))
         return {"t": st.t, "dt": st.dt, "steps": st.steps, "elapsed_ms": st.elapsed_ms}
 
     def global_residual(self, dt: float):

@@ -372,7 +372,12 @@ extern "C" fv3d_status fv3d_create(const fv3d_config* config, fv3d_ctx** out) {
     return FV3D_ERR_DEVICE;
   }
   if (cudaSetDevice(c.device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+      cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess ||
+      cudaMallocHost((void**)&ctx->h_sc, sizeof(DevScalars)) != cudaSuccess) {
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
     delete ctx;
     return FV3D_ERR_DEVICE;
   }
@@ -411,6 +416,7 @@ extern "C" fv3d_status fv3d_destroy(fv3d_ctx* handle) {
   ctx->free_device();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->h_sc) cudaFreeHost(ctx->h_sc);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return FV3D_OK;
@@ -770,17 +776,15 @@ static fv3d_status step_graph(Ctx* ctx, int scheme, double cfl, bool store_r, cu
   return FV3D_OK;
 }
 
-extern "C" fv3d_status fv3d_step_explicit(fv3d_ctx* handle, int scheme, int n_steps, double cfl,
-                                          double dt_fixed, fv3d_step_stats* stats) {
-  if (handle == nullptr) return FV3D_ERR_INVALID_ARG;
-  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+// n_steps explicit steps enqueued on the context stream (no synchronisation);
+// the caller reads the device scalars afterwards (finish_explicit)
+static fv3d_status enqueue_explicit(Ctx* ctx, int scheme, int n_steps, double cfl, double dt_fixed) {
   REQUIRE(scheme >= 0 && scheme <= 3, FV3D_ERR_INVALID_ARG, "bad explicit scheme %d", scheme);
   REQUIRE(n_steps >= 0, FV3D_ERR_INVALID_ARG, "negative step count");
   REQUIRE(cfl > 0.0 || dt_fixed > 0.0, FV3D_ERR_INVALID_ARG, "need cfl > 0 or dt_fixed > 0");
   fv3d_status st = check_ready(ctx);
   if (st != FV3D_OK) return st;
   if (!ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "no state set");
-  CK(cudaSetDevice(ctx->cfg.device));
   // initial dt from the current state (timedisc.c:163-165 at the first step)
   CK(cudaMemsetAsync(ctx->d_sc.p, 0, sizeof(DevScalars), ctx->stream));
   if (cfl > 0.0) {
@@ -795,12 +799,15 @@ extern "C" fv3d_status fv3d_step_explicit(fv3d_ctx* handle, int scheme, int n_st
   CK(cudaEventRecord(ctx->ev0, ctx->stream));
   for (int i = 0; i < n_steps; ++i) CK(cudaGraphLaunch(exec, ctx->stream));
   CK(cudaEventRecord(ctx->ev1, ctx->stream));
-  DevScalars hs;
-  CK(cudaMemcpyAsync(&hs, ctx->d_sc.p, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
-  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->residual_valid = false;
+  return FV3D_OK;
+}
+
+// after the enqueued steps (and anything enqueued behind them) completed:
+// the step statistics and status from the device scalars read into hs
+static fv3d_status finish_explicit(Ctx* ctx, const DevScalars& hs, fv3d_step_stats* stats) {
   float ms = 0.f;
   CK(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-  ctx->residual_valid = false;
   if (stats != nullptr) {
     stats->t = hs.t;
     stats->dt = hs.dt;
@@ -811,6 +818,39 @@ extern "C" fv3d_status fv3d_step_explicit(fv3d_ctx* handle, int scheme, int n_st
     return ctx->fail(FV3D_ERR_TIMEOUT, "gradient pass: a tile's staged copies did not arrive within 0.5 s");
   if (hs.status & 1) return ctx->fail(FV3D_ERR_NONFINITE, "non-finite state or time step after %d steps", hs.step);
   return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_step_explicit(fv3d_ctx* handle, int scheme, int n_steps, double cfl,
+                                          double dt_fixed, fv3d_step_stats* stats) {
+  if (handle == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  CK(cudaSetDevice(ctx->cfg.device));
+  fv3d_status st = enqueue_explicit(ctx, scheme, n_steps, cfl, dt_fixed);
+  if (st != FV3D_OK) return st;
+  DevScalars hs;
+  CK(cudaMemcpyAsync(&hs, ctx->d_sc.p, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return finish_explicit(ctx, hs, stats);
+}
+
+extern "C" fv3d_status fv3d_step_explicit_io(fv3d_ctx* handle, int scheme, int n_steps, double cfl,
+                                             double dt_fixed, const double* u_in, double* u_out,
+                                             fv3d_step_stats* stats) {
+  if (handle == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  fv3d_status st;
+  if (u_in != nullptr && (st = fv3d_set_state(handle, u_in)) != FV3D_OK) return st;
+  CK(cudaSetDevice(ctx->cfg.device));
+  if ((st = enqueue_explicit(ctx, scheme, n_steps, cfl, dt_fixed)) != FV3D_OK) return st;
+  // scalars into page-locked memory (asynchronous), then the export, which
+  // synchronises the stream once for both
+  CK(cudaMemcpyAsync(ctx->h_sc, ctx->d_sc.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream));
+  if (u_out != nullptr) {
+    if ((st = export_soa(ctx, ctx->d_U.p, 5, 0, u_out)) != FV3D_OK) return st;
+  } else {
+    CK(cudaStreamSynchronize(ctx->stream));
+  }
+  return finish_explicit(ctx, *ctx->h_sc, stats);
 }
 
 extern "C" fv3d_status fv3d_global_residual(fv3d_ctx* handle, double dt, double res[5]) {

@@ -40,6 +40,7 @@ struct Ctx {
   std::string err;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  DevScalars* h_sc = nullptr;  // page-locked copy of the device scalars (asynchronous reads)
   PhysConst phys;
   double kappa_pr = 0.0;
   unsigned region_set = 0;

@@ -164,6 +164,13 @@ fv3d_status fv3d_timestep(fv3d_ctx *ctx, double cfl, double *dt);
  * replayed as one CUDA graph per step.  stats may be NULL. */
 fv3d_status fv3d_step_explicit(fv3d_ctx *ctx, int scheme, int n_steps, double cfl,
                                double dt_fixed, fv3d_step_stats *stats);
+/* fv3d_set_state(u_in) + fv3d_step_explicit + fv3d_get_conserved(u_out) in
+ * one call with one synchronisation: the host-state form of a time step
+ * (u_in / u_out [n_cells*5] in reference order, may be the same array;
+ * either may be NULL to keep the state on the device). */
+fv3d_status fv3d_step_explicit_io(fv3d_ctx *ctx, int scheme, int n_steps, double cfl,
+                                  double dt_fixed, const double *u_in, double *u_out,
+                                  fv3d_step_stats *stats);
 /* calc_global_residual (analyze.c:37-61) of the last residual evaluation */
 fv3d_status fv3d_global_residual(fv3d_ctx *ctx, double dt, double res[5]);
 /* No counterpart in the reference.  fv3d_global_residual for callers that

@@ -718,7 +718,10 @@ __device__ __forceinline__ void sides_tile(const MxArgs& a, const unsigned char*
       const float n[3] = {nA.x, nA.y, nA.z};
       mx_ghost(q, a.fregion[f - a.nf_int], n, a.pc, ph, qo);
     } else {
-      ld_unpack(a.Uf + 8 * (size_t)o[k], qo);
+      // a neighbour inside this tile is already in shared memory
+      const unsigned lo = (unsigned)(o[k] - c0);
+      if (lo < (unsigned)kTile) mx_unpack(sUf[2 * lo], sUf[2 * lo + 1], qo);
+      else ld_unpack(a.Uf + 8 * (size_t)o[k], qo);
     }
     if (GMODE == 1) {
       const float w = sD[k * kTile + tid].w * nA.w;

@@ -139,6 +139,7 @@ EXPORTS = {
     "fv3d_global_residual": ([C.c_void_p, C.c_double, _f8p], C.c_int),
     "fv3d_global_residual_noalloc": ([C.c_void_p, C.c_double, _f8p], C.c_int),
     "fv3d_profile_stage": ([C.c_void_p, C.c_int, C.c_double, _f8p], C.c_int),
+    "fv3d_profile_step": ([C.c_void_p, C.c_int, C.c_int, C.c_double, _f8p], C.c_int),
     "fv3d_get_stream": ([C.c_void_p, C.POINTER(C.c_void_p)], C.c_int),
     "fv3d_device_state": ([C.c_void_p, C.POINTER(_f8p)], C.c_int),
     "fv3d_selftest_bounded_wait": ([C.c_void_p, C.c_int, C.POINTER(C.c_int), _f8p], C.c_int),
@@ -325,6 +326,13 @@ class Solver:
     def profile_stage(self, n_reps: int = 10, cfl: float = 0.5):
         out = np.empty(3)
         self._check(self.lib.fv3d_profile_stage(self.h, n_reps, cfl, _p(out, _f8p)))
+        return out
+
+    def profile_step(self, scheme: str = "rk33", n_steps: int = 10, cfl: float = 0.5):
+        """Per-launch kernel times (ms) of real steps: [gradient pass, flux pass
+        (both averaged over every stage), last stage's flux pass]."""
+        out = np.empty(3)
+        self._check(self.lib.fv3d_profile_step(self.h, SCHEMES[scheme], n_steps, cfl, _p(out, _f8p)))
         return out
 
     # ---- implicit steady solve ----

@@ -958,6 +958,86 @@ extern "C" fv3d_status fv3d_profile_stage(fv3d_ctx* handle, int n_reps, double c
   return FV3D_OK;
 }
 
+// the kernels of n_steps real explicit steps (the launches a step graph
+// replays, same coefficients, the dt computed on the device), each launch
+// bracketed by CUDA events on the context stream: ms[0] the gradient pass,
+// ms[1] the flux + update pass (FP64 path: face flux + gather), averaged
+// over every stage, ms[2] the flux pass of the last stage alone.  The
+// state advances by n_steps.
+extern "C" fv3d_status fv3d_profile_step(fv3d_ctx* handle, int scheme, int n_steps, double cfl, double* ms) {
+  if (handle == nullptr || ms == nullptr || n_steps <= 0) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  REQUIRE(scheme >= 0 && scheme <= 3, FV3D_ERR_INVALID_ARG, "bad explicit scheme %d", scheme);
+  REQUIRE(cfl > 0.0, FV3D_ERR_INVALID_ARG, "need cfl > 0");
+  fv3d_status st = check_ready(ctx);
+  if (st != FV3D_OK) return st;
+  if (!ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "no state set");
+  CK(cudaSetDevice(ctx->cfg.device));
+  CK(cudaMemsetAsync(ctx->d_sc.p, 0, sizeof(DevScalars), ctx->stream));
+  if ((st = reduce_step_bound(ctx)) != FV3D_OK) return st;
+  k_set_dt<<<1, 1, 0, ctx->stream>>>(ctx->d_sc.p, ctx->d_bits.p, cfl, 0.0);
+  CK(cudaGetLastError());
+  // one step captured as a graph with an event node at every launch
+  // boundary (external events, recorded when the graph runs): the kernels
+  // run exactly as the step graph runs them; one synchronisation per step
+  const int ns = (scheme == FV3D_SSP_RK3) ? 3 : RK_S[scheme];
+  cudaEvent_t ev[2 * 5 + 1] = {};
+  for (int i = 0; i < 2 * ns + 1; ++i) CK(cudaEventCreate(&ev[i]));
+  const int flux_mask = ctx->fp64() ? 6 : 4;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  cudaError_t ce = cudaEventRecordWithFlags(ev[0], ctx->stream, cudaEventRecordExternal);
+  for (int s = 0; s < ns && ce == cudaSuccess; ++s) {
+    const bool last = s == ns - 1;
+    int mode = 1;
+    StageCoef co{0, 0, 0, 0, s == 0, last, 0};
+    if (scheme == FV3D_SSP_RK3) {
+      const double c0[3] = {0.0, 0.75, 1.0 / 3.0}, c1[3] = {1.0, 0.25, 2.0 / 3.0};
+      mode = 2;
+      co.c0 = c0[s];
+      co.c1 = c1[s];
+    } else {
+      co.a = RK_A[scheme][s];
+      co.g = RK_G[scheme][s];
+    }
+    ce = ctx->launch_stage_kernels(mode, last, co, 1);
+    if (ce == cudaSuccess) ce = cudaEventRecordWithFlags(ev[2 * s + 1], ctx->stream, cudaEventRecordExternal);
+    if (ce == cudaSuccess) ce = ctx->launch_stage_kernels(mode, last, co, flux_mask);
+    if (ce == cudaSuccess) ce = cudaEventRecordWithFlags(ev[2 * s + 2], ctx->stream, cudaEventRecordExternal);
+  }
+  if (ce == cudaSuccess) {
+    k_finish_step<<<1, 1, 0, ctx->stream>>>(ctx->d_sc.p, cfl);
+    ce = cudaGetLastError();
+  }
+  cudaError_t ee = cudaStreamEndCapture(ctx->stream, &g);
+  if (ce == cudaSuccess) ce = ee;
+  if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, g, 0);
+  if (g) cudaGraphDestroy(g);
+  double acc[3] = {0, 0, 0};
+  for (int r = 0; r < n_steps && ce == cudaSuccess; ++r) {
+    ce = cudaGraphLaunch(exec, ctx->stream);
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(ev[2 * ns]);
+    for (int s = 0; s < ns && ce == cudaSuccess; ++s) {
+      float t0 = 0.f, t1 = 0.f;
+      ce = cudaEventElapsedTime(&t0, ev[2 * s], ev[2 * s + 1]);
+      if (ce == cudaSuccess) ce = cudaEventElapsedTime(&t1, ev[2 * s + 1], ev[2 * s + 2]);
+      acc[0] += t0;
+      acc[1] += t1;
+      if (s == ns - 1) acc[2] += t1;
+    }
+  }
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(ctx->stream);
+  if (exec) cudaGraphExecDestroy(exec);
+  for (int i = 0; i < 2 * ns + 1; ++i) cudaEventDestroy(ev[i]);
+  CK(ce);
+  ms[0] = acc[0] / (n_steps * ns);
+  ms[1] = acc[1] / (n_steps * ns);
+  ms[2] = acc[2] / n_steps;
+  ctx->residual_valid = false;
+  return FV3D_OK;
+}
+
 // ---------------------------------------------------------------------------
 // timedisc (timedisc.c:134-222): the step loop with its stop criteria
 // ---------------------------------------------------------------------------

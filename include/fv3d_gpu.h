@@ -355,6 +355,11 @@ fv3d_status fv3d_mlp_train(fv3d_ctx *ctx, const fv3d_mlp_train_opts *opts,
  * n_reps stages, each bracketed by CUDA events on the context stream:
  * ms[0] gradients, ms[1] face flux, ms[2] gather+update */
 fv3d_status fv3d_profile_stage(fv3d_ctx *ctx, int n_reps, double cfl, double *ms);
+/* the kernels of n_steps real explicit steps of scheme (the launches a step
+ * replays, dt on the device from cfl > 0), each launch bracketed by CUDA
+ * events: ms[0] gradient pass and ms[1] flux + update pass, each averaged
+ * over every stage; ms[2] the last stage's flux pass.  Advances the state. */
+fv3d_status fv3d_profile_step(fv3d_ctx *ctx, int scheme, int n_steps, double cfl, double *ms);
 /* CUDA stream (cudaStream_t) the context launches on, for event timing */
 fv3d_status fv3d_get_stream(const fv3d_ctx *ctx, void **stream);
 /* device pointer of the conserved state, [5][n_cells] SoA in renumbered order */

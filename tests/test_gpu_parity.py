@@ -237,3 +237,18 @@ def test_hdf5_load_unsupported():
     with api.from_case(c) as s:
         st = s.lib.fv3d_mesh_load_h5(s.h, b"mesh.h5")
         assert st == 2  # FV3D_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_profile_step_runs_the_step(precision):
+    """fv3d_profile_step times the launches of real steps: the state it
+    leaves is bitwise the one the step graphs give, and its per-launch
+    times are positive."""
+    c = cases.tgv_tet(4)
+    with api.from_case(c, precision) as s:
+        s.step_explicit("rk33", 3, cfl=0.5)
+        u_graph = s.get_conserved()
+    with api.from_case(c, precision) as s:
+        ms = s.profile_step("rk33", 3, 0.5)
+        assert np.all(ms > 0)
+        assert np.array_equal(s.get_conserved(), u_graph)

@@ -230,19 +230,22 @@ def run_channel(args):
             "fallbacks")
     runs = {}
     with api.Solver(c.mesh, c.params, c.region_type, c.region_prim, "fp64", "morton") as s:
-        if args.learned:
-            s.mlp_init(5)
         plans = [("none", dict(max_restarts=3)), ("block_jacobi", {})]
         for pc, kw in plans:
-            if args.learned and pc == "block_jacobi":
-                s.mlp_harvest(1024, 400000)
             s.set_state(c.u0)
             st = s.solve_implicit(preconditioner=pc, max_newton=args.max_newton, check=False, **kw)
             runs[pc] = {k: st[k] for k in keys}
-            if args.learned:
-                s.mlp_harvest(0, 400000)
         if args.learned:
-            tr = s.mlp_train(epochs=30, batch=1024, lr=2e-3)
+            # training pairs from plain Newton-Krylov steps (a separate,
+            # untimed solve harvesting 100,000 cells per Newton step, up to
+            # 2e7 pairs), a few epochs of Adam, then the learned solve
+            s.mlp_init(5)
+            s.mlp_harvest(100000, 20000000)
+            s.set_state(c.u0)
+            hv = s.solve_implicit(preconditioner="none", max_newton=200, max_restarts=3, check=False)
+            s.mlp_harvest(0, 20000000)
+            tr = s.mlp_train(epochs=4, batch=16384, lr=2e-3)
+            tr["harvest_newton_steps"] = hv["newton_steps"]
             s.set_state(c.u0)
             st = s.solve_implicit(preconditioner="learned", max_newton=args.max_newton, check=False)
             runs["learned"] = {k: st[k] for k in keys}

@@ -970,7 +970,9 @@ fv3d_status Implicit::apply_A(Ctx& ctx, const T* z, T* out) {
 }
 
 fv3d_status Implicit::build_blocks(Ctx& ctx) {
-  if (opts.preconditioner == FV3D_PC_NONE) return FV3D_OK;
+  // no preconditioner: no blocks, unless a harvest wants them as features
+  const bool harvesting = ctx.mlp && ctx.mlp->ready && ctx.mlp->harvest_per_step > 0;
+  if (opts.preconditioner == FV3D_PC_NONE && !harvesting) return FV3D_OK;
   if (opts.preconditioner == FV3D_PC_LUMPED) {
     // every cell perturbed at once by +-eps/2, eps = 1e-4 ||U_v||_2 (implicit.c:65-117)
     std::vector<double> slice(ctx.nc);

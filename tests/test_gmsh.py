@@ -194,3 +194,14 @@ def test_mixed_elements_round_trip(tmp_path, jitter):
         assert np.array_equal(getattr(m, f), getattr(ref, f)), f
     for f in ("cell_x", "cell_volume", "cell_dx", "face_x", "face_n", "face_area", "face_lambda"):
         assert np.allclose(getattr(m, f), getattr(ref, f), rtol=0, atol=1e-14), f
+
+
+def test_rejects_cyclic_periodic_links(tmp_path):
+    xs = np.linspace(0, 1, 3)
+    nodes, cn, sh = mg._structured(2, 2, 2, xs, xs, xs, (False, False, True), 0.0, 0, (1.0, 1.0, 1.0))
+    lat, full, links = unwrap_to_lattice(nodes, cn, sh, (2, 2, 2), (False, False, True))
+    a, b = links[0]
+    p = os.path.join(tmp_path, "cyc.msh")
+    gmsh.write_msh(p, lat, full, "hex", [], {(3, 1): "fluid"}, periodic=[[(a, b), (b, a)]])
+    with pytest.raises(ValueError, match="cyclic"):
+        gmsh.read_msh(p)

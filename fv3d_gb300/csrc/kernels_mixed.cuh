@@ -55,6 +55,10 @@ namespace fv3d {
 #ifndef FV3D_FLUX_MINBLOCKS
 #define FV3D_FLUX_MINBLOCKS 1
 #endif
+// resident blocks of the 4-slot flux pass (48 registers at 5)
+#ifndef FV3D_FLUX4_MINBLOCKS
+#define FV3D_FLUX4_MINBLOCKS 5
+#endif
 #ifndef FV3D_FLUX_UNROLL
 #define FV3D_FLUX_UNROLL 8
 #endif
@@ -466,7 +470,7 @@ __device__ __forceinline__ void mx_make_state(float rho, float mx, float my, flo
 // resident blocks: 5 (48 registers) for 4 face slots, where the gathers
 // need the warps (-4 % per stage); wider cells keep their registers
 template <int MCF, int MODE, bool DT, bool VISC, bool STORE = false>
-__global__ void __launch_bounds__(256, MCF == 4 ? 5 : FV3D_FLUX_MINBLOCKS)
+__global__ void __launch_bounds__(256, MCF == 4 ? FV3D_FLUX4_MINBLOCKS : FV3D_FLUX_MINBLOCKS)
     k_mx_flux_update(const __grid_constant__ MxArgs a, StageCoef co) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   unsigned long long lam_bits = 0x7ff0000000000000ull;

@@ -351,9 +351,12 @@ fv3d_status fv3d_mlp_train(fv3d_ctx *ctx, const fv3d_mlp_train_opts *opts,
                            fv3d_mlp_train_stats *stats);
 
 /* ---- measurement helpers ------------------------------------------------------ */
-/* average device time (ms) per launch of each explicit-stage kernel over
- * n_reps stages, each bracketed by CUDA events on the context stream:
- * ms[0] gradients, ms[1] face flux, ms[2] gather+update */
+/* average device time (ms) per launch of each kernel of one explicit stage
+ * repeated n_reps times, each bracketed by CUDA events on the context
+ * stream: a step's first stage (its RK register written, not read) with
+ * dt = 0, so the state does not change; cfl > 0 selects the variant that
+ * also computes the next dt.  ms[0] gradients, ms[1] face flux (mixed
+ * path: flux + update), ms[2] gather+update (mixed path: 0) */
 fv3d_status fv3d_profile_stage(fv3d_ctx *ctx, int n_reps, double cfl, double *ms);
 /* the kernels of n_steps real explicit steps of scheme (the launches a step
  * replays, dt on the device from cfl > 0), each launch bracketed by CUDA

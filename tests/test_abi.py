@@ -44,3 +44,46 @@ def test_create_rejects_bad_config(lib):
     h = C.c_void_p()
     assert lib.fv3d_create(C.byref(cfg), C.byref(h)) == 1  # FV3D_ERR_INVALID_ARG
     assert lib.fv3d_destroy(None) == 0
+
+
+STRUCTS = {  # C struct -> its ctypes mirror in fv3d_gb300.api
+    "fv3d_config": "Config", "fv3d_mesh_arrays": "MeshArrays", "fv3d_step_stats": "StepStats",
+    "fv3d_implicit_opts": "ImplicitOpts", "fv3d_implicit_stats": "ImplicitStats",
+    "fv3d_newton_opts": "NewtonOpts", "fv3d_newton_stats": "NewtonStats",
+    "fv3d_timedisc_opts": "TimedOpts", "fv3d_timedisc_stats": "TimedStats",
+    "fv3d_mlp_train_opts": "MlpTrainOpts", "fv3d_mlp_train_stats": "MlpTrainStats",
+}
+
+
+def test_header_is_c99_and_matches_the_bindings(lib, tmp_path):
+    """A C99 program that includes the header, takes the address of every
+    declared entry point (so each must link) and prints every struct's size
+    and field offsets: they must equal the ctypes mirrors'."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    fields = {c: [f for f, _ in getattr(api, py)._fields_] for c, py in STRUCTS.items()}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "fv3d_gpu.h"', 'int main(void) {',
+             '  void *fns[] = {']
+    lines += [f'    (void *)&{n},' for n in declared_functions()]
+    lines += ['  };', '  (void)fns;']
+    for c, fl in fields.items():
+        lines.append(f'  printf("{c} %zu\\n", sizeof({c}));')
+        for f in fl:
+            lines.append(f'  printf("{c}.{f} %zu\\n", offsetof({c}, {f}));')
+    lines += ['  printf("version %s\\n", fv3d_version());', '  return 0;', '}']
+    src = tmp_path / "abi_check.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "abi_check"
+    libdir = os.path.dirname(api.LIB_PATH)
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src),
+                    "-o", str(exe), "-L", libdir, "-lfv3d_gb300", f"-Wl,-rpath,{libdir}"], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = dict(line.rsplit(" ", 1) for line in out if line and not line.startswith("version"))
+    for c, py in STRUCTS.items():
+        cls = getattr(api, py)
+        assert int(got[c]) == C.sizeof(cls), c
+        for f in fields[c]:
+            assert int(got[f"{c}.{f}"]) == getattr(cls, f).offset, f"{c}.{f}"

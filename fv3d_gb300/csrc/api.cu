@@ -315,7 +315,7 @@ MxArgs Ctx::mx_args() const {
   a.nc = nc; a.nf = nf; a.nf_int = nf_int; a.mcf = mcf; a.ncp = ncp;
   a.cface = d_cface.p; a.cnbr = d_cnbr.p; a.fcell = d_fcell.p; a.slotN = d_slotN.p;
   a.slotD = d_slotD.p; a.slotW = d_slotW.p; a.slotNk = d_slotNk.p; a.slotDk = d_slotDk.p; a.slotWk = d_slotWk.p; a.fregion = d_fregion.p; a.cgeo = d_cgeo.p; a.cdx = d_cdx.p;
-  a.Uf = d_Uf.p; a.UfN = d_UfN.p; a.fs = d_fs.p; a.fsv = d_fsv.p;
+  a.Uf = d_Uf.p; a.UfN = d_UfN.p; a.fs = d_fs.p; a.fsv = d_fsv.p; a.cother = d_cother.p;
   a.U = d_U.p; a.kf = d_kf.p; a.dU = d_dU.p; a.dphi = d_dphi.p; a.sc = d_sc.p;
   a.pc = phys;
   return a;

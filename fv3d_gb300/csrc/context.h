@@ -62,7 +62,7 @@ struct Ctx {
   std::vector<double> h_cell_x;  // cell centres in reference order (for exact-function initial states)
 
   // device mesh
-  DevBuf<int> d_iperm, d_perm, d_fc0, d_fc1, d_fregion, d_cface, d_cnbr;
+  DevBuf<int> d_iperm, d_perm, d_fc0, d_fc1, d_fregion, d_cface, d_cnbr, d_cother;
   DevBuf<char> d_geo, d_lam, d_lsq, d_rvol;  // FP64-path geometry (double)
   DevBuf<double> d_vol, d_dx;
   // device solution data
@@ -91,7 +91,7 @@ struct Ctx {
     d_U.release(); d_K.release(); d_U0.release(); d_dphi.release(); d_stage.release(); d_part.release();
     d_Uf.release(); d_rec.release(); d_FA.release(); d_sc.release(); d_bits.release();
     d_fcell.release(); d_slotN.release(); d_slotD.release(); d_slotW.release(); d_slotNk.release(); d_slotDk.release(); d_slotWk.release(); d_fs.release();
-    d_fsv.release();
+    d_fsv.release(); d_cother.release();
     d_cgeo.release(); d_cdx.release(); d_UfN.release(); d_kf.release(); d_dU.release();
   }
   template <class R> KArgs<R> args() const;

@@ -65,10 +65,13 @@ namespace fv3d {
 constexpr int kSidesUnroll = FV3D_SIDES_UNROLL;
 constexpr int kFluxUnroll = FV3D_FLUX_UNROLL;
 
-// face record: side s at float4 [2s, 2s+1] = (rho, mx, my, mz), (E, vmx, vmy, vmz)
-// (two full 32-byte sectors per face); the viscous energy flux of side s in
-// fsv[2f + s].  v* = viscous normal flux times A.
-constexpr int FREC = 16;
+// face-side record: one full 32-byte sector (rho, mx, my, mz), (E, vmx,
+// vmy, vmz), v* = viscous normal flux times A; the side's viscous energy
+// flux in fsv at the same index.  A cell's own sides are stored slot-major
+// (record k * ncp + c for slot k of cell c), so the gradient pass writes and
+// the flux pass reads them with contiguous warp accesses; the ghost side of
+// boundary face nf_int + b is record mcf * ncp + b; cother gives each slot
+// the index of its face's other side.
 
 // cells per tile of the staged gradient pass (k_mx_sides_tma): one thread per
 // cell; the per-cell arrays it stages are padded to whole tiles (ncp rows)
@@ -92,8 +95,10 @@ struct MxArgs {
   const float4* __restrict__ cdx;    // [ncp] (dx, V)
   float* Uf;                         // [nc][8] stage state (rho, m, E, p, T, 1/rho)
   float* UfN;                        // [nc][8] float(U_n) + p, T
-  float* fs;                         // [nf][FREC]
-  float* fsv;                        // [nf][2]
+  const int* __restrict__ cother;    // [ncp][mcf] (the other side's record << 1) | side, -1 none
+  float* fs;                         // [mcf * ncp + nb][8] face-side records: a cell's own sides
+                                     // slot-major ([k][ncp]), then the ghost sides by boundary
+  float* fsv;                        // [mcf * ncp + nb] viscous energy flux of each side, same index
   double* U;                         // [5][nc] conserved state U_n (FP64)
   float* kf;                         // [5][ncp] RK register (FP32)
   float* dU;                         // [5][ncp] U_stage - U_n (FP32)
@@ -366,11 +371,13 @@ __global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __
       for (int v = 0; v < 8; ++v) r[v] = q[v];
     }
     if (VISC) mx_viscous(r, tau, g[8], nA, ph, &r[8]);
-    float* rec = a.fs + (size_t)f * FREC;
-    st_rec(rec + 8 * side, make_float4(r[0], r[1], r[2], r[3]),
+    (void)side;
+    const size_t own = (size_t)k * a.ncp + c;  // this side, slot-major
+    st_rec(a.fs + own * 8, make_float4(r[0], r[1], r[2], r[3]),
            VISC ? make_float4(r[4], r[8], r[9], r[10]) : make_float4(r[4], 0.f, 0.f, 0.f));
-    if (VISC) a.fsv[2 * (size_t)f + side] = r[11];
+    if (VISC) a.fsv[own] = r[11];
     if (o[k] == -1) {
+      const size_t gi = (size_t)MCF * a.ncp + (f - a.nf_int);  // the ghost side's record
       // ghost side: unlimited ghost of the cell-centre state
       // (reconstruction.c:249-253), gradient = interior gradient with the
       // normal part removed on slip walls / symmetry (boundary.c:377-405)
@@ -400,9 +407,9 @@ __global__ void __launch_bounds__(256, FV3D_SIDES_MINBLOCKS) k_mx_sides(const __
           gT[0] = gm[9]; gT[1] = gm[10]; gT[2] = gm[11];
         }
         mx_viscous(gq, tg, gT, nA, ph, vg);
-        a.fsv[2 * (size_t)f + 1] = vg[3];
+        a.fsv[gi] = vg[3];
       }
-      st_rec(rec + 8, make_float4(gq[0], gq[1], gq[2], gq[3]), make_float4(gq[4], vg[0], vg[1], vg[2]));
+      st_rec(a.fs + gi * 8, make_float4(gq[0], gq[1], gq[2], gq[3]), make_float4(gq[4], vg[0], vg[1], vg[2]));
     }
   }
 }
@@ -479,7 +486,7 @@ __global__ void __launch_bounds__(256, MCF == 4 ? FV3D_FLUX4_MINBLOCKS : FV3D_FL
     MxPhys ph;
     ph.load(a.pc);
     int e[MCF];
-    load_cface<MCF>(a.cface + (size_t)c * MCF, e);
+    load_cface<MCF>(a.cother + (size_t)c * MCF, e);
     // plain FP32 sums in slot order (ascending reference face id): with 4
     // to 8 terms a compensated sum changed the state after 500 steps by
     // nothing measurable (the faces' FP32 arithmetic dominates) and cost
@@ -488,17 +495,23 @@ __global__ void __launch_bounds__(256, MCF == 4 ? FV3D_FLUX4_MINBLOCKS : FV3D_FL
 #pragma unroll kFluxUnroll
     for (int k = 0; k < MCF; ++k) {
       if (e[k] < 0) continue;
-      const int f = e[k] >> 1, side = e[k] & 1;
-      float4 l0, l1, r0, r1;
-      ld_rec_nc(a.fs + (size_t)f * FREC, l0, l1);
-      ld_rec_nc(a.fs + (size_t)f * FREC + 8, r0, r1);
+      const int side = e[k] & 1;
+      const size_t own = (size_t)k * a.ncp + c, oth = (size_t)(e[k] >> 1);
+      float4 m0, m1, o0, o1;
+      ld_rec_nc(a.fs + own * 8, m0, m1);  // this cell's side (a warp's loads contiguous)
+      ld_rec_nc(a.fs + oth * 8, o0, o1);  // the other side
+      // cell 0's side left, cell 1's right: both cells evaluate the face
+      // from the same operands in the same order
+      const float4 l0 = side ? o0 : m0, l1 = side ? o1 : m1;
+      const float4 r0 = side ? m0 : o0, r1 = side ? m1 : o1;
       const float l[5] = {l0.x, l0.y, l0.z, l0.w, l1.x};
       const float r[5] = {r0.x, r0.y, r0.z, r0.w, r1.x};
       const float4 nA = __ldg(&a.slotNk[(size_t)k * a.ncp + c]);
       float F[5];
       mx_conv_flux(l, r, nA, ph, F);
       if (VISC) {
-        const float2 ve = __ldg(reinterpret_cast<const float2*>(a.fsv) + f);
+        const float vm = __ldg(a.fsv + own), vo = __ldg(a.fsv + oth);
+        const float2 ve = side ? make_float2(vo, vm) : make_float2(vm, vo);
         F[1] += 0.5f * (l1.y + r1.y);
         F[2] += 0.5f * (l1.z + r1.z);
         F[3] += 0.5f * (l1.w + r1.w);
@@ -795,11 +808,13 @@ __device__ __forceinline__ void sides_tile(const MxArgs& a, const unsigned char*
       for (int v = 0; v < 8; ++v) r[v] = q[v];
     }
     if (VISC) mx_viscous(r, tau, g[8], nA, ph, &r[8]);
-    float* rec = a.fs + (size_t)f * FREC;
-    st_rec(rec + 8 * side, make_float4(r[0], r[1], r[2], r[3]),
+    (void)side;
+    const size_t own = (size_t)k * a.ncp + c;  // this side, slot-major
+    st_rec(a.fs + own * 8, make_float4(r[0], r[1], r[2], r[3]),
            VISC ? make_float4(r[4], r[8], r[9], r[10]) : make_float4(r[4], 0.f, 0.f, 0.f));
-    if (VISC) a.fsv[2 * (size_t)f + side] = r[11];
+    if (VISC) a.fsv[own] = r[11];
     if (o[k] == -1) {  // ghost side, as in k_mx_sides
+      const size_t gi = (size_t)MCF * a.ncp + (f - a.nf_int);
       const int region = a.fregion[f - a.nf_int];
       const float n[3] = {nA4.x, nA4.y, nA4.z};
       float gq[10];
@@ -825,9 +840,9 @@ __device__ __forceinline__ void sides_tile(const MxArgs& a, const unsigned char*
           gT[0] = gm[9]; gT[1] = gm[10]; gT[2] = gm[11];
         }
         mx_viscous(gq, tg, gT, nA, ph, vg);
-        a.fsv[2 * (size_t)f + 1] = vg[3];
+        a.fsv[gi] = vg[3];
       }
-      st_rec(rec + 8, make_float4(gq[0], gq[1], gq[2], gq[3]), make_float4(gq[4], vg[0], vg[1], vg[2]));
+      st_rec(a.fs + gi * 8, make_float4(gq[0], gq[1], gq[2], gq[3]), make_float4(gq[4], vg[0], vg[1], vg[2]));
     }
   }
 }

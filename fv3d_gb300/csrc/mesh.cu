@@ -406,9 +406,34 @@ fv3d_status ensure_mixed_path(Ctx& ctx) {
       const int f = e >> 1;
       nbr[(size_t)c * ctx.mcf + k] = (f >= ctx.nf_int) ? -1 : ((e & 1) ? ctx.h_fc0[f] : ctx.h_fc1[f]);
     }
+  // the record of each slot's other side: the neighbour's own side in the
+  // slot that lists the same face, or the ghost side of a boundary face
+  std::vector<int> oth((size_t)ctx.ncp * ctx.mcf, -1);
+  for (int c = 0; c < nc; ++c)
+    for (int k = 0; k < ctx.mcf; ++k) {
+      const int e = ctx.h_cface[(size_t)c * ctx.mcf + k];
+      if (e < 0) break;
+      const int f = e >> 1, side = e & 1;
+      long long idx;
+      if (f >= ctx.nf_int) {
+        idx = (long long)ctx.mcf * ctx.ncp + (f - ctx.nf_int);
+      } else {
+        const int n = side ? ctx.h_fc0[f] : ctx.h_fc1[f];
+        int kn = -1;
+        for (int j = 0; j < ctx.mcf; ++j) {
+          const int en = ctx.h_cface[(size_t)n * ctx.mcf + j];
+          if (en < 0) break;
+          if ((en >> 1) == f) { kn = j; break; }
+        }
+        if (kn < 0) return ctx.fail(FV3D_ERR_INVALID_ARG, "face %d missing from its cell %d", f, n);
+        idx = (long long)kn * ctx.ncp + n;
+      }
+      oth[(size_t)c * ctx.mcf + k] = (int)((idx << 1) | side);
+    }
   UP(ctx.d_cgeo, cg.data(), cg.size());
   UP(ctx.d_cdx, cd.data(), cd.size());
   UP(ctx.d_cnbr, nbr.data(), nbr.size());
+  UP(ctx.d_cother, oth.data(), oth.size());
   UP(ctx.d_fcell, fcell.data(), (size_t)nf);
   UP(ctx.d_slotN, sN.data(), sN.size());
   UP(ctx.d_slotD, sD.data(), sD.size());
@@ -437,8 +462,10 @@ fv3d_status ensure_mixed_path(Ctx& ctx) {
   ALLOC(ctx.d_UfN, (size_t)ctx.ncp * 8);
   ALLOC(ctx.d_kf, (size_t)ctx.ncp * 5);
   ALLOC(ctx.d_dU, (size_t)ctx.ncp * 5);
-  ALLOC(ctx.d_fs, (size_t)nf * FREC);
-  ALLOC(ctx.d_fsv, (size_t)nf * 2);
+  // face-side records: every cell's own sides slot-major, then the ghost sides
+  const size_t nrec = (size_t)ctx.mcf * ctx.ncp + (size_t)(nf - ctx.nf_int);
+  ALLOC(ctx.d_fs, nrec * 8);
+  ALLOC(ctx.d_fsv, nrec);
   return FV3D_OK;
 }
 

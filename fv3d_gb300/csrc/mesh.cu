@@ -93,6 +93,15 @@ fv3d_status prepare_mesh(Ctx& ctx, const fv3d_mesh_arrays& m) {
       m.n_regions > MAX_REGIONS)
     return ctx.fail(FV3D_ERR_INVALID_ARG, "bad mesh sizes (cells %d faces %d boundaries %d max faces %d regions %d)",
                     nc, nf, nb, mcf, m.n_regions);
+  // face slots carry (face << 1) | side and the mixed path's other-side
+  // index (record << 1) | side in an int: faces and face-side records
+  // (max_cell_faces x cells rounded up to whole tiles, plus boundaries)
+  // must stay below 2^30
+  constexpr long long kIndexLimit = 1LL << 30;
+  const long long slots = (mcf <= 4) ? 4 : (mcf <= 6 ? 6 : 8);   // the padded slot stride below
+  if (nf >= kIndexLimit || slots * ((nc + kTile - 1LL) / kTile * kTile) + nb >= kIndexLimit)
+    return ctx.fail(FV3D_ERR_UNSUPPORTED, "mesh too large for 31-bit face-side indices (cells %d faces %d max faces %d)",
+                    nc, nf, mcf);
   if (!m.cell_x || !m.cell_volume || !m.cell_dx || !m.cell_n_faces || !m.cell_faces || !m.face_cells ||
       !m.face_boundary || !m.face_area || !m.face_lambda || !m.face_x || !m.face_n || !m.face_t1 ||
       !m.face_t2 || (nb > 0 && (!m.boundary_id || !m.boundary_face)) || !m.region_is_boundary)

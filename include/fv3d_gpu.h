@@ -121,7 +121,11 @@ const char *fv3d_version(void);
 /* ---- mesh ------------------------------------------------------------------ */
 /* replaces init_mesh(mesh_file) (mesh.c:98-106): takes the arrays that
  * read_mesh_file would load, runs calc_mesh_metrics (mesh.c:19-83),
- * validates indices, renumbers and uploads structure-of-arrays */
+ * validates indices, renumbers and uploads structure-of-arrays.
+ * FV3D_ERR_UNSUPPORTED for a mesh of 2^30 faces or more, or whose face
+ * slots (4, 6 or 8 per cell as max_cell_faces rounds up, cells rounded up
+ * to a multiple of 128) plus boundaries reach 2^30: face-side indices are
+ * carried with the side bit in an int (2^30 slots = 268 million tetrahedra) */
 fv3d_status fv3d_mesh_from_arrays(fv3d_ctx *ctx, const fv3d_mesh_arrays *mesh);
 /* replaces read_mesh_file (mesh.c:121-630); FV3D_ERR_UNSUPPORTED when this
  * build has no HDF5 library */

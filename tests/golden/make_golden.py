@@ -2,7 +2,8 @@
 own C sources (oracle/_ref/libfv3d_ref.so, built by oracle/Makefile.ref from
 the reference tree) on small synthetic meshes.
 
-Run where the reference tree exists:  python tests/golden/make_golden.py
+Run where the reference tree exists:  python tests/golden/make_golden.py [name ...]
+(no names: every fixture).
 Each .npz holds the mesh arrays, physics settings, the input state and the
 reference outputs, so the fixtures are self-contained on machines without the
 reference tree.
@@ -43,11 +44,33 @@ def golden_cases():
     c.region_type[2] = mg.BC_OUTFLOW             # the reference's own outlet type
     c.params["mu_mix"] = 0.01
     yield "channel_6x4x4", c, dict(rk=[(1, 2)], newton=3)
+    # the other boundary types of boundary.c:252-307 on the outlet (and, for
+    # the isothermal wall, the walls), viscous; slip wall and symmetry share
+    # one treatment there (boundary.c:280-281, 377-378), so their fixtures
+    # differ only in the type code
+    for label, btype in (("isothermal", mg.BC_WALL_ISOTHERMAL), ("slip", mg.BC_WALL_SLIP),
+                         ("symmetry", mg.BC_SYMMETRY), ("state", mg.BC_STATE)):
+        yield f"channel_4x4x3_{label}", boundary_case(btype), dict(rk=[(1, 2)], newton=0)
+    # hexahedra, prisms and pyramids (cells of 5 and 6 faces)
+    yield "tgv_mixed3", cases.tgv_mixed(3), dict(rk=[(1, 3)], newton=0)
 
 
-def main():
+def boundary_case(btype):
+    c = cases.channel(4, 4, 3)
+    c.params["mu_mix"] = 0.01
+    c.region_type[2] = btype
+    c.region_prim[2] = [0.2, 0.01, 0.0, 1 / 1.4, 0.9 / 1.4]
+    if btype == mg.BC_WALL_ISOTHERMAL:
+        c.region_type[3] = btype
+        c.region_prim[3] = [0.0, 0.0, 0.0, 1 / 1.4, 0.8 / 1.4]
+    return c
+
+
+def main(only=()):
     ref = orc.Oracle("reference")
     for name, c, what in golden_cases():
+        if only and name not in only:
+            continue
         ref.init(c.mesh, c.params, c.region_type, c.region_prim)
         u_in = perturbed(c)
         ref.set_conserved(u_in)
@@ -92,4 +115,4 @@ PARAM_KEYS = ["kappa", "R_mix", "mu_mix", "Pr", "cfl_scale", "dfl_scale", "flux_
               "reconstruction", "limiter", "gradient"]
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

@@ -69,6 +69,7 @@ def test_reference_quirk_dt_zero_without_viscosity(restated):
     lambda: cases.tgv_tet(3),
     lambda: cases.tgv_hex(3),
     lambda: cases.channel(4, 4, 4),
+    lambda: cases.tgv_mixed(3),
 ])
 def test_restated_matches_reference_build(restated, maker):
     ref = orc.Oracle("reference")

@@ -5,11 +5,12 @@
 //                    Barth-Jespersen bounds in registers, then for each of the
 //                    cell's faces the limited reconstructed conserved state
 //                    and that side's viscous normal flux, written into the
-//                    face's record (the ghost side of a boundary face is
-//                    written by its interior cell).
+//                    cell's face-side record of that slot (the ghost side of
+//                    a boundary face is written by its interior cell).
 //  k_mx_flux_update  (flux + update pass, cell-gather) per cell: for each of
 //                    its faces the convective flux from both side records
-//                    plus the averaged viscous flux, summed in ascending
+//                    (its own, and the other side's through cother) plus
+//                    the averaged viscous flux, summed in ascending
 //                    reference face id, -sum/V, RK stage update, FP32
 //                    stage state, next time step.
 //

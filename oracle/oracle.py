@@ -64,16 +64,23 @@ def _ptr(a, t):
     return a.ctypes.data_as(t)
 
 
+# the instance whose init() last set up each library's global state
+_ACTIVE = {}
+
+
 class Oracle:
-    """One oracle instance (the libraries keep global state, as the reference does)."""
+    """One oracle instance.  The libraries keep global state, as the
+    reference does, so instances of one library share it: only the instance
+    initialised last may be used (any other raises instead of computing on
+    the other instance's mesh and settings)."""
 
     def __init__(self, which: str = "restated"):
         path = LIBS[which]
         if not os.path.exists(path):
             build(which)
         self.which = which
-        self.lib = C.CDLL(path)
-        L = self.lib
+        self._lib = C.CDLL(path)
+        L = self._lib
         L.orc_init.argtypes = [C.POINTER(OrcMesh), C.POINTER(OrcParams), _i4p, _f8p]
         L.orc_error.restype = C.c_char_p
         for name in ("orc_set_conserved", "orc_get_total", "orc_get_flux"):
@@ -92,6 +99,13 @@ class Oracle:
                                       _i4p, _i4p]
         L.orc_get_jacobian.argtypes = [_f8p]
         self._keep = None
+
+    @property
+    def lib(self):
+        if _ACTIVE.get(self.which) is not self:
+            raise RuntimeError(f"oracle[{self.which}]: another instance of this library was initialised "
+                               "since this one (they share its global state), or this one never was")
+        return self._lib
 
     def _check(self, rc):
         if rc != 0:
@@ -112,6 +126,7 @@ class Oracle:
         rt = np.ascontiguousarray(region_type, dtype=np.int32)
         rp = np.ascontiguousarray(region_prim, dtype=np.float64).reshape(-1)
         self._keep2 = (m, p, rt, rp)
+        _ACTIVE[self.which] = self
         self._check(self.lib.orc_init(C.byref(m), C.byref(p), _ptr(rt, _i4p), _ptr(rp, _f8p)))
 
     def set_conserved(self, u):

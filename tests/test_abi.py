@@ -46,6 +46,36 @@ def test_create_rejects_bad_config(lib):
     assert lib.fv3d_destroy(None) == 0
 
 
+def _null_args(argtypes):
+    """Zero / NULL for every parameter type of an entry point."""
+    out = []
+    for t in argtypes:
+        if t in (C.c_int, C.c_uint, C.c_longlong, C.c_ulonglong):
+            out.append(0)
+        elif t in (C.c_double, C.c_float):
+            out.append(0.0)
+        elif isinstance(t, type) and issubclass(t, C._CFuncPtr):
+            out.append(t())         # a NULL callback
+        else:                       # handles, pointers
+            out.append(None)
+    return out
+
+
+def test_every_entry_point_refuses_a_null_handle(lib):
+    """Each entry point checks its handle and pointers before anything else:
+    called with NULL for every pointer it returns FV3D_ERR_INVALID_ARG
+    (fv3d_destroy(NULL) is a no-op, as free(NULL)), touching no device."""
+    checked = 0
+    for name, (args, res) in api.EXPORTS.items():
+        if res is not C.c_int or not args:
+            continue
+        st = getattr(lib, name)(*_null_args(args))
+        expect = 0 if name == "fv3d_destroy" else 1
+        assert st == expect, (name, st)
+        checked += 1
+    assert checked >= 35
+
+
 STRUCTS = {  # C struct -> its ctypes mirror in fv3d_gb300.api
     "fv3d_config": "Config", "fv3d_mesh_arrays": "MeshArrays", "fv3d_step_stats": "StepStats",
     "fv3d_implicit_opts": "ImplicitOpts", "fv3d_implicit_stats": "ImplicitStats",

@@ -46,3 +46,31 @@ def test_rejections():
     sim = params.load_simulation(tree)
     with pytest.raises(KeyError, match="wall"):
         sim.regions(cases.channel(6, 4, 4).mesh)
+
+
+NACA = "/root/reference/misc/gmsh/naca0012/naca0012_simulation.json"
+
+
+@pytest.mark.skipif(not os.path.exists(NACA), reason="reference tree absent")
+def test_reference_example_simulation_file_loads():
+    """The parameter file the reference ships with its NACA 0012 example:
+    every key the reference's modules read maps to its value."""
+    tree = json.load(open(NACA))
+    sim = params.load_simulation(NACA)
+    ns = tree["Equation"]["Navier-Stokes"]
+    for k in ("kappa", "R_mix", "mu_mix", "Pr", "cfl_scale", "dfl_scale"):
+        assert sim.params[k] == ns[k]["value"], k
+    assert sim.params["flux_scheme"] == cases.AUSM
+    assert (sim.params["reconstruction"], sim.params["limiter"]) == (cases.LINEAR, cases.BARTH_JESPERSEN)
+    td = tree["TimeDisc"]
+    assert (sim.implicit, sim.scheme) == (False, "rk33")
+    assert (sim.max_iter, sim.transient, sim.abort_residual, sim.t_start, sim.t_end) == (
+        td["max_iter"]["value"], td["transient"]["value"], td["abort_residual"]["value"],
+        td["t_start"]["value"], td["t_end"]["value"])
+    assert sim.i_output_data == tree["Output"]["i_output_data"]["value"]
+    assert sim.use_restart is False and sim.mesh_file == "naca0012.mesh.h5"
+    bnd = {name: b["type"] for name, b in ns["Boundary"].items()}      # plain objects
+    assert {name: t for name, (t, _) in sim.boundaries.items()} == {
+        name: params.BOUNDARY_TYPES[t] for name, t in bnd.items()}
+    # the isothermal profile keeps its wall temperature
+    assert sim.boundaries["profile"][1][4] == ns["Boundary"]["profile"]["T"]

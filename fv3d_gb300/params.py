@@ -13,6 +13,10 @@ Keys follow the reference's parameter paths:
       TimeDisc/Implicit/{scheme, max_iter_inner, ...} (implicit.c:77-112)
   Mesh/mesh_file, Output/i_output_data (output.c:20-23),
   Restart/{use_restart, restart_file} (restart.c:20-30)
+and, for settings the reference does not have, a GPU subtree:
+  GPU/precision ("FP64" | "Mixed"), GPU/renumbering ("None" | "Morton" |
+  "RCM"), GPU/cfl (explicit steps' CFL number; 0 or less: calc_ns_timestep
+  with cfl_scale / dfl_scale, as the reference)
 HDF5 files cannot be read or written in this build (no HDF5 library): the
 mesh is passed in (``meshgen`` / ``gmsh``), and output / restart files are the
 NumPy containers of ``output`` with the same datasets.
@@ -37,6 +41,8 @@ RECONSTRUCTION = {"First-Order": cases.FIRST_ORDER, "Linear": cases.LINEAR}
 LIMITER = {"Barth-Jespersenn": cases.BARTH_JESPERSEN, "None": cases.NO_LIMITER}
 EXPLICIT = {"Euler": "euler", "RK3-3": "rk33", "RK4-5": "rk45"}
 IMPLICIT = {"Euler": "euler", "BDF-2": "bdf2"}
+PRECISION = {"FP64": "fp64", "Mixed": "mixed"}
+RENUMBERING = {"None": "none", "Morton": "morton", "RCM": "rcm"}
 
 
 def _get(tree, path, default=_MISSING):
@@ -75,6 +81,9 @@ class Simulation:
     i_output_data: int = -1
     use_restart: bool = False
     restart_file: str = ""
+    precision: str = "fp64"
+    renumbering: str = "morton"
+    cfl: float = 0.0
     extra: dict = field(default_factory=dict)
 
     def regions(self, mesh):
@@ -149,20 +158,26 @@ def load_simulation(src) -> Simulation:
                       abort_residual=float(_get(tree, "TimeDisc/abort_residual", 1e-10)),
                       t_start=float(_get(tree, "TimeDisc/t_start", 0.0)), t_end=float(_get(tree, "TimeDisc/t_end", 0.2)),
                       max_iter_inner=int(inner), i_output_data=int(_get(tree, "Output/i_output_data", -1)),
-                      use_restart=use_restart, restart_file=restart_file)
+                      use_restart=use_restart, restart_file=restart_file,
+                      precision=_pick(PRECISION, _get(tree, "GPU/precision", "FP64"), "precision"),
+                      renumbering=_pick(RENUMBERING, _get(tree, "GPU/renumbering", "Morton"), "renumbering"),
+                      cfl=float(_get(tree, "GPU/cfl", 0.0)))
 
 
-def run(sim: Simulation, mesh, precision="fp64", cfl=0.0, check=True, output_dir=None):
+def run(sim: Simulation, mesh, precision=None, cfl=None, check=True, output_dir=None):
     """The reference's program flow on the GPU: set up the solver from the
     parameters, set_solution (or read_restart_data), timedisc with
-    write_output into output_dir (None: no files).  cfl <= 0 takes
-    calc_ns_timestep as written (cfl_scale, dfl_scale), as the reference
-    does; returns the final conserved state, the timedisc stats, the
-    residual rows and the output files written."""
+    write_output into output_dir (None: no files).  precision and cfl
+    default to the file's GPU settings; cfl <= 0 takes calc_ns_timestep as
+    written (cfl_scale, dfl_scale), as the reference does; returns the
+    final conserved state, the timedisc stats, the residual rows and the
+    output files written."""
     from . import api, output
+    precision = sim.precision if precision is None else precision
+    cfl = sim.cfl if cfl is None else cfl
     rt, rp = sim.regions(mesh)
     written = []
-    with api.Solver(mesh, sim.params, rt, rp, precision) as s:
+    with api.Solver(mesh, sim.params, rt, rp, precision, sim.renumbering) as s:
         iter_start, t_start = 0, sim.t_start
         if sim.use_restart:
             r = output.read_restart(sim.restart_file)

@@ -48,6 +48,20 @@ def test_rejections():
         sim.regions(cases.channel(6, 4, 4).mesh)
 
 
+def test_gpu_subtree():
+    """Settings the reference has no keys for live under GPU/: absent, the
+    run is FP64, Morton-renumbered, with calc_ns_timestep's dt."""
+    tree = json.load(open(SIM))
+    sim = params.load_simulation(tree)
+    assert (sim.precision, sim.renumbering, sim.cfl) == ("fp64", "morton", 0.0)
+    tree["GPU"] = {"precision": {"value": "Mixed"}, "renumbering": {"value": "RCM"}, "cfl": {"value": 0.5}}
+    sim = params.load_simulation(tree)
+    assert (sim.precision, sim.renumbering, sim.cfl) == ("mixed", "rcm", 0.5)
+    tree["GPU"]["precision"]["value"] = "FP16"
+    with pytest.raises(ValueError, match="precision"):
+        params.load_simulation(tree)
+
+
 NACA = "/root/reference/misc/gmsh/naca0012/naca0012_simulation.json"
 
 

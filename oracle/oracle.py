@@ -21,6 +21,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIBS = {
     "restated": os.path.join(HERE, "liboracle.so"),
     "reference": os.path.join(HERE, "_ref", "libfv3d_ref.so"),
+    # the restatement under AddressSanitizer / UndefinedBehaviorSanitizer:
+    # load only in a process started with libasan preloaded
+    "restated_san": os.path.join(HERE, "_san", "liboracle_san.so"),
 }
 REFERENCE_TREE = os.environ.get("FV3D_REFERENCE_TREE", "/root/reference")
 
@@ -48,10 +51,12 @@ class OrcParams(C.Structure):
 
 def build(which: str = "restated", quiet: bool = True) -> str:
     """Compile the oracle library (gcc).  "reference" needs the reference tree."""
-    mk = "Makefile" if which == "restated" else "Makefile.ref"
+    mk = "Makefile.ref" if which == "reference" else "Makefile"
     args = ["make", "-s", "-f", os.path.join(HERE, mk)]
     if which == "reference":
         args.append(f"REF={REFERENCE_TREE}")
+    elif which == "restated_san":
+        args.append("sanitize")
     subprocess.run(args, check=True, capture_output=quiet)
     return LIBS[which]
 

@@ -6,6 +6,7 @@ import os
 import numpy as np
 import pytest
 
+from conftest import REFERENCE
 from fv3d_gb300 import cases, meshgen as mg, params
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -62,7 +63,7 @@ def test_gpu_subtree():
         params.load_simulation(tree)
 
 
-NACA = "/root/reference/misc/gmsh/naca0012/naca0012_simulation.json"
+NACA = os.path.join(REFERENCE, "misc", "gmsh", "naca0012", "naca0012_simulation.json")
 
 
 @pytest.mark.skipif(not os.path.exists(NACA), reason="reference tree absent")

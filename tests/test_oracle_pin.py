@@ -97,3 +97,30 @@ def test_oracle_rejects_corrupt_mesh(restated):
     c.mesh.face_boundary = bad
     with pytest.raises(RuntimeError, match="boundary index"):
         restated.init(c.mesh, c.params, c.region_type, c.region_prim)
+
+
+@pytest.mark.skipif(not reference_tree_present(), reason="reference tree absent")
+@pytest.mark.parametrize("scheme", [0, 1])            # backward Euler, BDF2 (implicit.c:37-38)
+@pytest.mark.parametrize("maker", [
+    lambda: cases.channel(4, 4, 3),
+    lambda: cases.tgv_mixed(3),
+])
+def test_restated_newton_matches_reference_build(restated, maker, scheme):
+    """timestep_newton (implicit.c:224-351) with calc_jacobian_numerical:
+    the same inner iteration counts, states and Jacobian blocks, bitwise."""
+    ref = orc.Oracle("reference")
+    c = maker()
+    if c.name == "channel":
+        c.region_type[2] = mg.BC_OUTFLOW
+        c.params["mu_mix"] = 0.01
+    c.params["gradient"] = cases.GREEN_GAUSS
+    for o in (ref, restated):
+        o.init(c.mesh, c.params, c.region_type, c.region_prim)
+        o.set_conserved(c.u0)
+    for it in range(3):
+        dt = ref.timestep_convective(1.0)
+        a = ref.step_newton(it, 0.0, dt, scheme=scheme, solver=1, krylov_dims=15, krylov_restarts=2)
+        b = restated.step_newton(it, 0.0, dt, scheme=scheme, solver=1, krylov_dims=15, krylov_restarts=2)
+        assert a == b, it
+        assert np.array_equal(ref.conserved(), restated.conserved()), it
+    assert np.array_equal(ref.jacobian(), restated.jacobian())

@@ -147,6 +147,7 @@ EXPORTS = {
     "fv3d_solve_implicit": ([C.c_void_p, C.POINTER(ImplicitOpts), C.POINTER(ImplicitStats)], C.c_int),
     "fv3d_implicit_history": ([C.c_void_p, _f8p, C.c_int, C.POINTER(C.c_int)], C.c_int),
     "fv3d_get_blocks": ([C.c_void_p, _f8p], C.c_int),
+    "fv3d_jacobian_vector": ([C.c_void_p, C.c_int, C.c_double, _f8p, _f8p], C.c_int),
     "fv3d_step_newton": ([C.c_void_p, C.POINTER(NewtonOpts), C.c_int, C.c_double, C.c_double,
                           C.POINTER(NewtonStats)], C.c_int),
     "fv3d_timedisc": ([C.c_void_p, C.POINTER(TimedOpts), C.POINTER(TimedStats)], C.c_int),
@@ -362,6 +363,18 @@ class Solver:
         self._check(self.lib.fv3d_implicit_history(self.h, None, 0, C.byref(n)))
         out = np.empty(n.value)
         self._check(self.lib.fv3d_implicit_history(self.h, _p(out, _f8p), n.value, C.byref(n)))
+        return out
+
+    def jacobian_vector(self, z, precision: str = "fp64", fd_eps: float = 1e-7):
+        """J z of the implicit solve's finite differences at the current
+        state ((n_cells, 5) in and out, reference order): FP64 or FP32
+        residuals ("fp64" / "fp32")."""
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        if z.shape != (self.nc, 5):
+            raise ValueError(f"z must have shape ({self.nc}, 5)")
+        out = np.empty((self.nc, 5))
+        self._check(self.lib.fv3d_jacobian_vector(self.h, {"fp64": 0, "fp32": 1}[precision], fd_eps,
+                                                  _p(z, _f8p), _p(out, _f8p)))
         return out
 
     def blocks(self):

@@ -1378,6 +1378,33 @@ fv3d_status Implicit::ICK_copy(Ctx& ctx, double* dst, const double* src) {
   return FV3D_OK;
 }
 
+// J z = (R(U + eps z) - R(U)) / eps at the current state, with the solve's
+// steps: FP32 residuals and eps = 5e-4 (1 + |U|) / |z|, or FP64 residuals
+// and eps = fd_eps (1 + |U|) / |z|
+fv3d_status Implicit::jacobian_vector(Ctx& ctx, int prec, double fd_eps, const double* z_rows, double* out_rows) {
+  fv3d_status st = ensure_fp64_path(ctx);
+  if (st == FV3D_OK && prec == 1) st = ensure_mixed_path(ctx);
+  if (st == FV3D_OK) st = setup(ctx, 1);
+  if (st == FV3D_OK) st = import_rows(ctx, z_rows, x.p);
+  if (st != FV3D_OK) return st;
+  opts.jv_precision = prec;
+  st = (prec == 1) ? residual32(ctx, ctx.d_U.p, Rb.p) : residual64(ctx, ctx.d_U.p, Rb.p);
+  if (st == FV3D_OK) st = norm(ctx, ctx.d_U.p, &unorm);
+  if (st != FV3D_OK) return st;
+  hpin[0] = ((prec == 1) ? 5e-4 : fd_eps) * (1.0 + unorm);
+  hpin[1] = 1.0 / hpin[0];
+  ICK(cudaMemcpyAsync(hdev.p + 100, hpin, 2 * sizeof(double), cudaMemcpyHostToDevice, ctx.stream));
+  if ((st = fd_residual<double>(ctx, x.p, false)) != FV3D_OK) return st;
+  // w = 0 * z - (Rp - Rb) / eps = -J z (idtl zeroed first)
+  ICK(cudaMemsetAsync(idtl.p, 0, sizeof(double) * ctx.nc, ctx.stream));
+  k_jv_combine<double><<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, x.p, Rp.p, Rb.p, idtl.p, jv_ieps, w.p);
+  ICK(cudaGetLastError());
+  k_lincomb<<<std::min(4096, blocks(n)), 256, 0, ctx.stream>>>(n, -1.0, w.p, 0.0, nullptr, Wst.p);
+  ICK(cudaGetLastError());
+  if ((st = refresh_records(ctx)) != FV3D_OK) return st;  // the perturbed records overwrote the state's
+  return export_rows(ctx, Wst.p, out_rows);
+}
+
 }  // namespace fv3d
 
 using namespace fv3d;
@@ -1413,6 +1440,21 @@ extern "C" fv3d_status fv3d_solve_implicit(fv3d_ctx* handle, const fv3d_implicit
   if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "cudaSetDevice");
   if (!ctx->implicit) ctx->implicit = new Implicit();
   return ctx->implicit->solve(*ctx, *opts, stats);
+}
+
+extern "C" fv3d_status fv3d_jacobian_vector(fv3d_ctx* handle, int jv_precision, double fd_eps, const double* z,
+                                            double* jz) {
+  if (handle == nullptr || z == nullptr || jz == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (!ctx->mesh_ready || !ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "mesh and state required");
+  for (int b = 0; b < ctx->nb; ++b)
+    if (!(ctx->region_set & (1u << ctx->h_fregion[b])))
+      return ctx->fail(FV3D_ERR_STATE, "boundary region %d has no condition", ctx->h_fregion[b]);
+  if ((jv_precision != 0 && jv_precision != 1) || !(fd_eps > 0.0))
+    return ctx->fail(FV3D_ERR_INVALID_ARG, "bad Jacobian-vector arguments");
+  if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "cudaSetDevice");
+  if (!ctx->implicit) ctx->implicit = new Implicit();
+  return ctx->implicit->jacobian_vector(*ctx, jv_precision, fd_eps, z, jz);
 }
 
 extern "C" fv3d_status fv3d_implicit_history(const fv3d_ctx* handle, double* res, int max, int* count) {

@@ -83,6 +83,7 @@ struct Implicit {
                       const double* scale = nullptr);
   fv3d_status norm(Ctx& ctx, const double* v, double* out);
   fv3d_status ICK_copy(Ctx& ctx, double* dst, const double* src);
+  fv3d_status jacobian_vector(Ctx& ctx, int prec, double fd_eps, const double* z_rows, double* out_rows);
 
   // the reference's implicit time step (timestep_newton)
   DevBuf<double> old0, old1, dYdt, fY;

@@ -238,6 +238,14 @@ fv3d_status fv3d_implicit_history(const fv3d_ctx *ctx, double *res, int max, int
 /* 5x5 blocks of the last preconditioner build, [n_cells][25] column-major,
  * reference cell order (lumped blocks: compare with calc_jacobian_numerical) */
 fv3d_status fv3d_get_blocks(fv3d_ctx *ctx, double *blocks);
+/* The implicit solve's matrix-free Jacobian-vector product at the current
+ * state, J z = (R(U + eps z) - R(U)) / eps (the product the reference forms
+ * from its lumped blocks in matrix_vector_numerical, implicit.c:362-384,
+ * here of the full residual): jv_precision 1 takes FP32 residuals and
+ * eps = 5e-4 (1 + |U|) / |z|, 0 FP64 residuals and eps = fd_eps (1 + |U|) / |z|.
+ * z and jz are [n_cells][5] rows in reference cell order. */
+fv3d_status fv3d_jacobian_vector(fv3d_ctx *ctx, int jv_precision, double fd_eps, const double *z,
+                                 double *jz);
 
 /* ---- the reference's implicit time step -------------------------------------- */
 /* timestep_newton (implicit.c:224-351) with the lumped Jacobian of

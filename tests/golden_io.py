@@ -12,7 +12,9 @@ PARAM_KEYS = ["kappa", "R_mix", "mu_mix", "Pr", "cfl_scale", "dfl_scale", "flux_
 
 
 def names():
-    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "golden", "*.npz")))
+    """The small fixtures (the full-run fixtures fullrun_*.npz hold no mesh)."""
+    return sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "golden", "*.npz"))
+                  if not os.path.basename(p).startswith("fullrun_"))
 
 
 def load(name):

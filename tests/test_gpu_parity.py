@@ -85,6 +85,72 @@ def test_boundary_types_fp64(oracle, label, btype):
         assert rel_max(s.time_derivative(0.0), r_ref) < FP64_RESIDUAL_TOL
 
 
+def walled_channel(btype, nx, ny, nz, limiter=None):
+    """The channel (inflow, adiabatic walls, pressure outlet, periodic z)
+    with its outlet region replaced by `btype` (None keeps the pressure
+    outlet; an isothermal outlet makes the walls isothermal too), viscous."""
+    c = cases.channel(nx, ny, nz)
+    c.params["mu_mix"] = 0.01
+    if limiter is not None:
+        c.params["limiter"] = limiter
+    if btype is not None:
+        c.region_type[2] = btype
+        c.region_prim[2] = [0.2, 0.01, 0.0, 1 / 1.4, 0.9 / 1.4]
+        if btype == mg.BC_WALL_ISOTHERMAL:
+            c.region_type[3] = btype
+            c.region_prim[3] = [0.0, 0.0, 0.0, 1 / 1.4, 0.8 / 1.4]
+    return c
+
+
+# every boundary type the GPU implements, on the outlet region; the inflow
+# and the adiabatic walls are in every variant
+MIXED_BOUNDARY_VARIANTS = [("pressure_outlet", None), ("outflow", mg.BC_OUTFLOW),
+                           ("isothermal", mg.BC_WALL_ISOTHERMAL), ("slip", mg.BC_WALL_SLIP),
+                           ("symmetry", mg.BC_SYMMETRY), ("state", mg.BC_STATE)]
+# the mixed residual against the FP64 oracle, relative to its largest entry
+# (FP32 face arithmetic on a residual that is O(1 %) of the face fluxes)
+MIXED_RESIDUAL_TOL = 1e-5
+
+
+@pytest.mark.parametrize("size", [(6, 4, 4), (12, 8, 4)])
+@pytest.mark.parametrize("label,btype", MIXED_BOUNDARY_VARIANTS)
+def test_boundary_types_mixed_residual(oracle, label, btype, size):
+    """The production (mixed FP32/FP64) kernels on boundary faces: ghost
+    states (boundary.c:188-320), ghost gradients (boundary.c:325-412) and
+    the ghost side's viscous flux, against the FP64 oracle."""
+    c = walled_channel(btype, *size)
+    u = perturbed(c)
+    oracle.init(c.mesh, c.params, c.region_type, c.region_prim)
+    oracle.set_conserved(u)
+    r_ref = oracle.time_derivative(0.0)
+    with api.Solver(c.mesh, c.params, c.region_type, c.region_prim, "mixed") as s:
+        s.set_state(u)
+        err = rel_max(s.time_derivative(0.0), r_ref)
+    print(label, size, "mixed residual rel max err", err)
+    assert err < MIXED_RESIDUAL_TOL, err
+
+
+@pytest.mark.parametrize("limiter", [cases.NO_LIMITER, cases.BARTH_JESPERSEN])
+@pytest.mark.parametrize("label,btype", MIXED_BOUNDARY_VARIANTS)
+def test_boundary_types_mixed_20_rk3_steps(oracle, label, btype, limiter):
+    """20 RK3 steps at CFL 0.5 on the 12x8x4 walled channel: FP64 GPU and
+    mixed against the oracle."""
+    c = walled_channel(btype, 12, 8, 4, limiter)
+    c.u0 = perturbed(c)
+    u_ref, t_ref = run_oracle(oracle, c, "rk33", 20, 0.5)
+    with api.from_case(c, "fp64") as s:
+        st = s.step_explicit("rk33", 20, cfl=0.5)
+        e64 = rel_l2(s.get_conserved(), u_ref, u_ref=0.3)
+        assert abs(st["t"] / t_ref - 1) < 1e-12
+    with api.from_case(c, "mixed") as s:
+        st = s.step_explicit("rk33", 20, cfl=0.5)
+        emx = rel_l2(s.get_conserved(), u_ref, u_ref=0.3)
+        assert abs(st["t"] / t_ref - 1) < 1e-5
+    print(label, limiter, "fp64", e64.max(), "mixed", emx.max())
+    assert e64.max() < FP64_STATE_TOL, e64
+    assert emx.max() < MIXED_STATE_TOL, emx
+
+
 @pytest.mark.parametrize("name", golden_io.names())
 def test_residual_fp64_matches_reference_golden(name):
     """Against outputs of the reference's own C code (committed fixtures)."""

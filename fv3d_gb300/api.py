@@ -66,7 +66,8 @@ class ImplicitOpts(C.Structure):
     _fields_ = [("cfl_start", C.c_double), ("cfl_max", C.c_double), ("tol_rel", C.c_double),
                 ("max_newton", C.c_int), ("krylov_dim", C.c_int), ("eta", C.c_double),
                 ("fd_eps", C.c_double), ("jv_precision", C.c_int), ("preconditioner", C.c_int),
-                ("pc_refresh", C.c_int), ("max_restarts", C.c_int), ("sync_every", C.c_int)]
+                ("pc_refresh", C.c_int), ("max_restarts", C.c_int), ("sync_every", C.c_int),
+                ("inner_dim", C.c_int), ("inner_sweeps", C.c_int)]
 
 
 class ImplicitStats(C.Structure):
@@ -113,7 +114,7 @@ class MlpTrainStats(C.Structure):
 
 _f4p = C.POINTER(C.c_float)
 
-PRECONDITIONERS = {"block_jacobi": 0, "lumped": 1, "learned": 2, "none": 3}
+PRECONDITIONERS = {"block_jacobi": 0, "lumped": 1, "learned": 2, "none": 3, "coupled": 4}
 
 EXPORTS = {
     "fv3d_create": ([C.POINTER(Config), C.POINTER(C.c_void_p)], C.c_int),
@@ -148,6 +149,7 @@ EXPORTS = {
     "fv3d_implicit_history": ([C.c_void_p, _f8p, C.c_int, C.POINTER(C.c_int)], C.c_int),
     "fv3d_get_blocks": ([C.c_void_p, _f8p], C.c_int),
     "fv3d_jacobian_vector": ([C.c_void_p, C.c_int, C.c_double, _f8p, _f8p], C.c_int),
+    "fv3d_get_coupled_blocks": ([C.c_void_p, C.c_int, _f8p, _f8p, _i4p, C.POINTER(C.c_int)], C.c_int),
     "fv3d_step_newton": ([C.c_void_p, C.POINTER(NewtonOpts), C.c_int, C.c_double, C.c_double,
                           C.POINTER(NewtonStats)], C.c_int),
     "fv3d_timedisc": ([C.c_void_p, C.POINTER(TimedOpts), C.POINTER(TimedStats)], C.c_int),
@@ -376,6 +378,21 @@ class Solver:
         self._check(self.lib.fv3d_jacobian_vector(self.h, {"fp64": 0, "fp32": 1}[precision], fd_eps,
                                                   _p(z, _f8p), _p(out, _f8p)))
         return out
+
+    def coupled_blocks(self, which: str = "ausm"):
+        """Blocks of the last coupled-preconditioner build: (diag (n_cells, 5,
+        5), slots (n_cells, max_slots, 5, 5), neighbour (n_cells, max_slots)),
+        row-major blocks, reference order; which "ausm" (P_A) or "rusanov"
+        (P_R: inverted diagonal blocks)."""
+        w = {"ausm": 0, "rusanov": 1}[which]
+        ms = C.c_int()
+        self._check(self.lib.fv3d_get_coupled_blocks(self.h, w, None, None, None, C.byref(ms)))
+        d = np.empty((self.nc, 5, 5))
+        o = np.empty((self.nc, ms.value, 5, 5))
+        nb = np.empty((self.nc, ms.value), dtype=np.int32)
+        self._check(self.lib.fv3d_get_coupled_blocks(self.h, w, _p(d, _f8p), _p(o, _f8p), _p(nb, _i4p),
+                                                     C.byref(ms)))
+        return d, o, nb
 
     def blocks(self):
         out = np.empty((self.nc, 5, 5))

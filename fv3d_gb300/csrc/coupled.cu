@@ -1,0 +1,598 @@
+// Cell-coupling preconditioner of the implicit steady solve (sm_103a).
+//
+// The Newton system of the pseudo-transient solve is (I/dt - dR/dU) x = R,
+// R the second-order viscous residual.  Block Jacobi (one 5x5 block per
+// cell) cannot carry information between cells, which is what limits this
+// solve; this preconditioner approximates the whole system by the Jacobian of
+// the first-order inviscid residual R1 (cell-centre face states, the case's
+// own flux: AUSM or Rusanov, flux.c:320-406):
+//
+//   P_A = I/dt - dR1/dU,   block (c, c) and one block per face slot of c
+//
+// and applies z = M v as a short inner GMRES on P_A from x = 0 (a fixed
+// number of iterations), right-preconditioned by block-Jacobi sweeps of the
+// first-order Rusanov Jacobian with the wave speed frozen,
+//
+//   P_R = I/dt + (1/V_c) sum_f s_f A_f dF_f/dU,   dF/dU_0 = (A(U_0) + lam I) / 2,
+//                                                dF/dU_1 = (A(U_1) - lam I) / 2,
+//
+// lam = max(|u.n| + c) + 2 mu / (rho d) (A(U) the Euler flux Jacobian along
+// n; at a boundary face the ghost's dependence on its cell is included),
+// whose sweeps converge where sweeps on P_A diverge.  The outer solve is
+// flexible GMRES, so the inner solve may differ from one application to the
+// next without changing the answer.
+//
+// Storage: FP32 blocks, row-major within a block, element-major over cells
+// ([e][nc]: a warp's loads of element e are contiguous); slot blocks
+// [slot][e][nc].  Blocks are built per Newton step in FP64: P_A's by forward
+// finite differences of each face flux (h = 1e-7 max(|U_v|, 1e-3)), P_R's
+// analytically.  Every product and sweep is a cell gather: no atomics, no
+// face buffers.  The inner Krylov basis, its Gram-Schmidt passes and the
+// sweeps run in FP32; the inner least-squares problem in FP64 on the device,
+// so an application needs no host synchronisation and is captured in the
+// outer Arnoldi step's CUDA graph.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "context.h"
+#include "fo_flux.cuh"
+#include "implicit.h"
+
+namespace fv3d {
+
+namespace {
+
+inline int nblk(size_t n, int t = 256) { return (int)((n + t - 1) / t); }
+constexpr int kHcol = 72;  // per inner column: h [0, 32), h' [32, 64), |w| and 1/|w| at 64, 65
+
+// neighbour of each face slot: the other cell, -1 for a boundary face or an
+// unused slot
+__global__ void k_cpl_nbr(int nc, int mcf, const int* __restrict__ cface, const int* __restrict__ fc0,
+                          const int* __restrict__ fc1, int* __restrict__ nbr) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  for (int k = 0; k < mcf; ++k) {
+    const int e = cface[(size_t)c * mcf + k];
+    int o = -1;
+    if (e >= 0) {
+      const int f = e >> 1;
+      o = (e & 1) ? fc0[f] : fc1[f];
+      if (o >= nc) o = -1;  // ghost index of a boundary face
+    }
+    nbr[(size_t)k * nc + c] = o;
+  }
+}
+
+// Euler flux Jacobian d(F.n)/dU (row-major) of a conserved state, with
+// |u.n| + c and rho
+__device__ void euler_jacobian(const double* U, const double* n, double kappa, double* A, double* lam) {
+  const double rho = U[0], ir = 1.0 / rho;
+  const double u[3] = {U[1] * ir, U[2] * ir, U[3] * ir};
+  const double q2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+  const double p = (kappa - 1.0) * (U[4] - 0.5 * rho * q2);
+  const double H = (U[4] + p) * ir;
+  const double un = u[0] * n[0] + u[1] * n[1] + u[2] * n[2];
+  const double phi = 0.5 * (kappa - 1.0) * q2;
+  A[0] = 0.0;
+  A[1] = n[0]; A[2] = n[1]; A[3] = n[2];
+  A[4] = 0.0;
+  for (int i = 0; i < 3; ++i) {
+    A[(1 + i) * 5] = phi * n[i] - u[i] * un;
+    for (int j = 0; j < 3; ++j)
+      A[(1 + i) * 5 + 1 + j] = u[i] * n[j] - (kappa - 1.0) * u[j] * n[i] + (i == j ? un : 0.0);
+    A[(1 + i) * 5 + 4] = (kappa - 1.0) * n[i];
+  }
+  A[20] = un * (phi - H);
+  for (int j = 0; j < 3; ++j) A[21 + j] = H * n[j] - (kappa - 1.0) * u[j] * un;
+  A[24] = kappa * un;
+  *lam = fabs(un) + sqrt(kappa * fmax(p, 1.00E-10) * ir);
+}
+
+__device__ __forceinline__ void store_block(float* __restrict__ dst, size_t nc, const double* B) {
+#pragma unroll
+  for (int e = 0; e < 25; ++e) dst[(size_t)e * nc] = (float)B[e];
+}
+
+__device__ __forceinline__ void zero_block(float* __restrict__ dst, size_t nc) {
+#pragma unroll
+  for (int e = 0; e < 25; ++e) dst[(size_t)e * nc] = 0.f;
+}
+
+// the face's geometry for the first-order fluxes: n (cell 0 -> cell 1) and,
+// in n[3], the distance |d1| + |d2| (interior) or 2 |d1| (boundary)
+__device__ __forceinline__ void face_normal(const double* g, bool bnd, double* n) {
+  n[0] = g[G_N]; n[1] = g[G_N + 1]; n[2] = g[G_N + 2];
+  const double d1 = sqrt(g[G_D1] * g[G_D1] + g[G_D1 + 1] * g[G_D1 + 1] + g[G_D1 + 2] * g[G_D1 + 2]);
+  const double d2 = sqrt(g[G_D2] * g[G_D2] + g[G_D2 + 1] * g[G_D2 + 1] + g[G_D2 + 2] * g[G_D2 + 2]);
+  n[3] = bnd ? 2.0 * d1 : d1 + d2;
+}
+
+// P_A: diagonal block of cell c and one block per face slot, from forward
+// differences of each face's first-order flux (with the case's flux scheme,
+// inviscid unless visc) in each of the ten states it depends on; at a
+// boundary face the ghost is re-derived from the perturbed cell state
+// (update_boundaries, boundary.c:188-320).  Each face is differentiated by
+// both of its cells (no face buffer).
+template <int MCF>
+__global__ void __launch_bounds__(128) k_cpl_build_pa(KArgs<double> a, const double* __restrict__ dtl,
+                                                      float* __restrict__ PAd, float* __restrict__ PAo, int visc) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.nc) return;
+  const size_t nc = a.nc;
+  Phys<double> ph;
+  ph.load(a.pc);
+  double qc[10];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) qc[j] = a.U[(size_t)j * nc + c];
+  cons_to_prims(qc, ph);
+  const double iv = 1.0 / a.vol[c];
+  double D[25];
+#pragma unroll
+  for (int e = 0; e < 25; ++e) D[e] = 0.0;
+  const double idt = 1.0 / dtl[c];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) D[j * 5 + j] = idt;
+  for (int k = 0; k < MCF; ++k) {
+    float* Ok = PAo + (size_t)k * 25 * nc + c;
+    const int e = a.cface[(size_t)c * MCF + k];
+    if (e < 0) { zero_block(Ok, nc); continue; }
+    const int f = e >> 1, side = e & 1;
+    const double* g = a.geo + (size_t)f * GEO;
+    const bool bnd = f >= a.nf_int;
+    double n[4];
+    face_normal(g, bnd, n);
+    const double w = (side ? -1.0 : 1.0) * g[G_A] * iv;  // -dR_c/dF_f
+    const int region = bnd ? a.fregion[f - a.nf_int] : 0;
+    double qo[10];
+    if (bnd) {
+      ghost_state(qc, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qo);
+    } else {
+      const int o = side ? a.fc0[f] : a.fc1[f];
+#pragma unroll
+      for (int j = 0; j < 5; ++j) qo[j] = a.U[(size_t)j * nc + o];
+    }
+    double F0[5];
+    if (side) fo_flux(qo, qc, n, a.pc, F0, visc != 0);
+    else fo_flux(qc, qo, n, a.pc, F0, visc != 0);
+    // the cell's own state
+    for (int v = 0; v < 5; ++v) {
+      const double h = 1e-7 * fmax(fabs(qc[v]), 1e-3);
+      double qp[10], F[5];
+#pragma unroll
+      for (int j = 0; j < 5; ++j) qp[j] = qc[j];
+      qp[v] += h;
+      if (bnd) {
+        double qg[10];
+        cons_to_prims(qp, ph);
+        ghost_state(qp, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qg);
+        fo_flux(qp, qg, n, a.pc, F, visc != 0);
+      } else if (side) {
+        fo_flux(qo, qp, n, a.pc, F, visc != 0);
+      } else {
+        fo_flux(qp, qo, n, a.pc, F, visc != 0);
+      }
+      const double s = w / h;
+#pragma unroll
+      for (int i = 0; i < 5; ++i) D[i * 5 + v] += (F[i] - F0[i]) * s;
+    }
+    if (bnd) { zero_block(Ok, nc); continue; }
+    // the neighbour's state
+    for (int v = 0; v < 5; ++v) {
+      const double h = 1e-7 * fmax(fabs(qo[v]), 1e-3);
+      double qp[5], F[5];
+#pragma unroll
+      for (int j = 0; j < 5; ++j) qp[j] = qo[j];
+      qp[v] += h;
+      if (side) fo_flux(qp, qc, n, a.pc, F, visc != 0);
+      else fo_flux(qc, qp, n, a.pc, F, visc != 0);
+      const double s = w / h;
+#pragma unroll
+      for (int i = 0; i < 5; ++i) Ok[(size_t)(i * 5 + v) * nc] = (float)((F[i] - F0[i]) * s);
+    }
+  }
+  store_block(PAd + c, nc, D);
+}
+
+// 5x5 inverse (row-major, FP64 Gauss-Jordan with partial pivoting); false
+// when singular
+__device__ bool invert5(const double* B, double* X) {
+  double M[5][10];
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 5; ++j) {
+      M[i][j] = B[i * 5 + j];
+      M[i][5 + j] = (i == j) ? 1.0 : 0.0;
+    }
+  for (int col = 0; col < 5; ++col) {
+    int piv = col;
+    for (int i = col + 1; i < 5; ++i)
+      if (fabs(M[i][col]) > fabs(M[piv][col])) piv = i;
+    if (!(fabs(M[piv][col]) > 1e-300)) return false;
+    if (piv != col)
+      for (int j = 0; j < 10; ++j) { const double t = M[col][j]; M[col][j] = M[piv][j]; M[piv][j] = t; }
+    const double ip = 1.0 / M[col][col];
+    for (int j = 0; j < 10; ++j) M[col][j] *= ip;
+    for (int i = 0; i < 5; ++i) {
+      if (i == col) continue;
+      const double fct = M[i][col];
+      for (int j = 0; j < 10; ++j) M[i][j] -= fct * M[col][j];
+    }
+  }
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 5; ++j) X[i * 5 + j] = M[i][5 + j];
+  return true;
+}
+
+// P_R: the Rusanov Jacobian's slot blocks and its inverted diagonal blocks
+template <int MCF>
+__global__ void __launch_bounds__(128) k_cpl_build_pr(KArgs<double> a, const double* __restrict__ dtl,
+                                                      float* __restrict__ PRi, float* __restrict__ PRo) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.nc) return;
+  const size_t nc = a.nc;
+  Phys<double> ph;
+  ph.load(a.pc);
+  const double kappa = a.pc.kappa, mu = a.pc.mu;
+  double qc[10];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) qc[j] = a.U[(size_t)j * nc + c];
+  cons_to_prims(qc, ph);
+  const double iv = 1.0 / a.vol[c];
+  double D[25];
+#pragma unroll
+  for (int e = 0; e < 25; ++e) D[e] = 0.0;
+  const double idt = 1.0 / dtl[c];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) D[j * 5 + j] = idt;
+  for (int k = 0; k < MCF; ++k) {
+    float* Ok = PRo + (size_t)k * 25 * nc + c;
+    const int e = a.cface[(size_t)c * MCF + k];
+    if (e < 0) { zero_block(Ok, nc); continue; }
+    const int f = e >> 1, side = e & 1;
+    const double* g = a.geo + (size_t)f * GEO;
+    const bool bnd = f >= a.nf_int;
+    double n[4];
+    face_normal(g, bnd, n);
+    const double w = (side ? -1.0 : 1.0) * g[G_A] * iv;
+    double Ac[25], lc;
+    euler_jacobian(qc, n, kappa, Ac, &lc);
+    if (!bnd) {
+      const int o = side ? a.fc0[f] : a.fc1[f];
+      double qo[5];
+#pragma unroll
+      for (int j = 0; j < 5; ++j) qo[j] = a.U[(size_t)j * nc + o];
+      double Ao[25], lo;
+      euler_jacobian(qo, n, kappa, Ao, &lo);
+      const double lam = fmax(lc, lo) + 2.0 * mu / (0.5 * (qc[0] + qo[0]) * n[3]);
+      // own: cell 0 -> (A + lam I) / 2, cell 1 -> (A - lam I) / 2; the other the opposite
+      const double so = side ? -lam : lam;
+#pragma unroll
+      for (int e2 = 0; e2 < 25; ++e2) {
+        const double id = (e2 % 6 == 0) ? 1.0 : 0.0;
+        D[e2] += w * 0.5 * (Ac[e2] + so * id);
+        Ok[(size_t)e2 * nc] = (float)(w * 0.5 * (Ao[e2] - so * id));
+      }
+    } else {
+      const int region = a.fregion[f - a.nf_int];
+      double qg[10], Ag[25], lg;
+      ghost_state(qc, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qg);
+      euler_jacobian(qg, n, kappa, Ag, &lg);
+      const double lam = fmax(lc, lg) + 2.0 * mu / (qc[0] * n[3]);
+      // d ghost / d U_c by forward differences
+      double G[25];
+      for (int v = 0; v < 5; ++v) {
+        const double h = 1e-7 * fmax(fabs(qc[v]), 1e-3);
+        double qp[10], qh[10];
+#pragma unroll
+        for (int j = 0; j < 5; ++j) qp[j] = qc[j];
+        qp[v] += h;
+        cons_to_prims(qp, ph);
+        ghost_state(qp, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qh);
+#pragma unroll
+        for (int i = 0; i < 5; ++i) G[i * 5 + v] = (qh[i] - qg[i]) / h;
+      }
+#pragma unroll
+      for (int i = 0; i < 5; ++i) {
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+          double s = 0.5 * (Ac[i * 5 + j] + (i == j ? lam : 0.0));
+#pragma unroll
+          for (int l = 0; l < 5; ++l) s += 0.5 * (Ag[i * 5 + l] - (i == l ? lam : 0.0)) * G[l * 5 + j];
+          D[i * 5 + j] += w * s;
+        }
+      }
+      zero_block(Ok, nc);
+    }
+  }
+  double X[25];
+  if (!invert5(D, X)) {
+#pragma unroll
+    for (int e = 0; e < 25; ++e) X[e] = (e % 6 == 0) ? 1.0 / D[e] : 0.0;
+  }
+  store_block(PRi + c, nc, X);
+}
+
+__device__ __forceinline__ void ld5(const float* __restrict__ x, size_t nc, int c, float* v) {
+#pragma unroll
+  for (int j = 0; j < 5; ++j) v[j] = __ldg(x + (size_t)j * nc + c);
+}
+
+__device__ __forceinline__ void block_mul_add(const float* __restrict__ B, size_t nc, const float* x, float* y) {
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    float s = y[i];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) s = fmaf(__ldg(B + (size_t)(i * 5 + j) * nc), x[j], s);
+    y[i] = s;
+  }
+}
+
+// y = P x: the diagonal block times x_c plus each slot block times the
+// neighbour's x
+template <int MCF>
+__global__ void __launch_bounds__(256) k_cpl_product(int nc, const float* __restrict__ Dg,
+                                                     const float* __restrict__ O, const int* __restrict__ nbr,
+                                                     const float* __restrict__ x, float* __restrict__ y) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  float xc[5], acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  ld5(x, nc, c, xc);
+  block_mul_add(Dg + c, nc, xc, acc);
+#pragma unroll
+  for (int k = 0; k < MCF; ++k) {
+    const int o = __ldg(nbr + (size_t)k * nc + c);
+    if (o < 0) continue;
+    float xo[5];
+    ld5(x, nc, o, xo);
+    block_mul_add(O + (size_t)k * 25 * nc + c, nc, xo, acc);
+  }
+#pragma unroll
+  for (int j = 0; j < 5; ++j) y[(size_t)j * nc + c] = acc[j];
+}
+
+// one block-Jacobi sweep y = Dinv (b - O x) (x null: y = Dinv b)
+template <int MCF, class TO>
+__global__ void __launch_bounds__(256) k_cpl_sweep(int nc, const float* __restrict__ Di, const float* __restrict__ O,
+                                                   const int* __restrict__ nbr, const float* __restrict__ b,
+                                                   const float* __restrict__ x, TO* __restrict__ y) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  float t[5], r[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  ld5(b, nc, c, t);
+  if (x != nullptr) {
+    float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < MCF; ++k) {
+      const int o = __ldg(nbr + (size_t)k * nc + c);
+      if (o < 0) continue;
+      float xo[5];
+      ld5(x, nc, o, xo);
+      block_mul_add(O + (size_t)k * 25 * nc + c, nc, xo, s);
+    }
+#pragma unroll
+    for (int j = 0; j < 5; ++j) t[j] -= s[j];
+  }
+  block_mul_add(Di + c, nc, t, r);
+#pragma unroll
+  for (int j = 0; j < 5; ++j) y[(size_t)j * nc + c] = (TO)r[j];
+}
+
+// V_0 = v / |v| (the inverse norm from a device slot), stored FP32
+template <class T>
+__global__ void k_cpl_start(size_t n, const T* __restrict__ v, const double* __restrict__ inv, float* __restrict__ V0) {
+  const double s = *inv;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    V0[i] = (float)((double)v[i] * s);
+}
+
+// the inner least-squares problem min |beta e_1 - H y| by Givens rotations
+// (FP64, one thread): H from the Gram-Schmidt passes' columns, y [m] into
+// hin + m * kHcol + 8; the columns past a breakdown (a zero subdiagonal or a
+// zero or non-finite rotation) get y = 0
+__global__ void k_cpl_lsq(int m, double* __restrict__ hin) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double H[30][31];
+  double cs[30], sn[30], g[31], y[30];
+  const double beta = hin[(size_t)m * kHcol];  // |v| from the norm pass
+  for (int i = 0; i <= m; ++i) g[i] = 0.0;
+  g[0] = beta;
+  int kk = 0;
+  for (int j = 0; j < m; ++j) {
+    const double* hc = hin + (size_t)j * kHcol;
+    for (int i = 0; i <= j; ++i) H[j][i] = hc[i] + hc[32 + i];
+    const double hn = hc[64];
+    H[j][j + 1] = hn;
+    for (int i = 0; i < j; ++i) {
+      const double a0 = H[j][i], b0 = H[j][i + 1];
+      H[j][i] = cs[i] * a0 + sn[i] * b0;
+      H[j][i + 1] = -sn[i] * a0 + cs[i] * b0;
+    }
+    const double a0 = H[j][j], b0 = H[j][j + 1];
+    const double r = sqrt(a0 * a0 + b0 * b0);
+    if (!(r > 0.0) || !isfinite(r)) break;
+    cs[j] = a0 / r;
+    sn[j] = b0 / r;
+    H[j][j] = r;
+    g[j + 1] = -sn[j] * g[j];
+    g[j] = cs[j] * g[j];
+    kk = j + 1;
+    if (!(hn > 0.0)) break;  // the Krylov space is invariant: exact solution
+  }
+  for (int i = kk - 1; i >= 0; --i) {
+    double s = g[i];
+    for (int j = i + 1; j < kk; ++j) s -= H[j][i] * y[j];
+    y[i] = s / H[i][i];
+  }
+  double* out = hin + (size_t)m * kHcol + 8;
+  for (int i = 0; i < m; ++i) out[i] = (i < kk) ? y[i] : 0.0;
+}
+
+// u = sum_j y_j V_j (FP32 basis, ldb apart)
+__global__ void k_cpl_combine(size_t n, size_t ldb, const float* __restrict__ V, const double* __restrict__ y, int m,
+                              float* __restrict__ u) {
+  __shared__ float ys[32];
+  if (threadIdx.x < 32) ys[threadIdx.x] = (threadIdx.x < (unsigned)m) ? (float)y[threadIdx.x] : 0.f;
+  __syncthreads();
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    float s = 0.f;
+    for (int j = 0; j < m; ++j) s = fmaf(ys[j], __ldg(V + (size_t)j * ldb + i), s);
+    u[i] = s;
+  }
+}
+
+}  // namespace
+
+#define CCK(expr)                                               \
+  do {                                                          \
+    fv3d_status st__ = ctx.cuda((expr), #expr);                 \
+    if (st__ != FV3D_OK) return st__;                           \
+  } while (0)
+
+fv3d_status Coupled::setup(Ctx& ctx, Implicit& im, int m_inner, int n_sweeps) {
+  // captured Arnoldi steps hold the buffers and the inner iteration counts
+  if (m_inner != m_in || n_sweeps != sweep_count) im.release_graphs();
+  m_in = m_inner;
+  sweep_count = n_sweeps;
+  if (nc == ctx.nc && mcf == ctx.mcf && ldb == im.ldb && m_cap >= m_inner) return FV3D_OK;
+  im.release_graphs();
+  nc = ctx.nc;
+  mcf = ctx.mcf;
+  n = im.n;
+  ldb = im.ldb;
+  m_cap = m_inner;
+  if (mcf != 4 && mcf != 6 && mcf != 8) return ctx.fail(FV3D_ERR_UNSUPPORTED, "coupled preconditioner: %d face slots", mcf);
+  cudaError_t e = nbr.alloc((size_t)mcf * nc);
+  if (e == cudaSuccess) e = PAd.alloc(25 * (size_t)nc);
+  if (e == cudaSuccess) e = PAo.alloc((size_t)mcf * 25 * nc);
+  if (e == cudaSuccess) e = PRi.alloc(25 * (size_t)nc);
+  if (e == cudaSuccess) e = PRo.alloc((size_t)mcf * 25 * nc);
+  if (e == cudaSuccess) e = Vi.alloc((size_t)(m_cap + 1) * ldb);
+  if (e == cudaSuccess) e = wi.alloc(ldb);
+  if (e == cudaSuccess) e = ti.alloc(ldb);
+  if (e == cudaSuccess) e = ui.alloc(ldb);
+  if (e == cudaSuccess) e = hin.alloc((size_t)(m_cap + 1) * kHcol);
+  CCK(e);
+  // the tails past n of the FP32 vectors are never written: zero them once
+  CCK(cudaMemsetAsync(Vi.p, 0, sizeof(float) * Vi.n, ctx.stream));
+  CCK(cudaMemsetAsync(hin.p, 0, sizeof(double) * hin.n, ctx.stream));
+  KArgs<double> a = ctx.args<double>();
+  k_cpl_nbr<<<nblk(nc), 256, 0, ctx.stream>>>(nc, mcf, a.cface, a.fc0, a.fc1, nbr.p);
+  CCK(cudaGetLastError());
+  return FV3D_OK;
+}
+
+fv3d_status Coupled::build(Ctx& ctx, Implicit& im) {
+  KArgs<double> a = ctx.args<double>();
+  const int g = nblk(nc, 128);
+#define CPL_BUILD(M)                                                                           \
+  k_cpl_build_pa<M><<<g, 128, 0, ctx.stream>>>(a, im.dtl.p, PAd.p, PAo.p, 0);                 \
+  k_cpl_build_pr<M><<<g, 128, 0, ctx.stream>>>(a, im.dtl.p, PRi.p, PRo.p)
+  if (mcf == 4) { CPL_BUILD(4); }
+  else if (mcf == 6) { CPL_BUILD(6); }
+  else { CPL_BUILD(8); }
+#undef CPL_BUILD
+  CCK(cudaGetLastError());
+  return FV3D_OK;
+}
+
+// out = M_R b: `count` block-Jacobi sweeps of P_R from zero
+template <class TO>
+fv3d_status Coupled::sweeps(Ctx& ctx, int count, const float* b, TO* out) {
+  const int g = nblk(nc);
+  // sweeps alternate between ti and ui... the last one writes out; b is never overwritten
+  const float* x = nullptr;
+  for (int s = 0; s < count; ++s) {
+    const bool last = (s == count - 1);
+    float* tmp = (s % 2 == 0) ? ti.p : wi.p;
+#define CPL_SWEEP(M)                                                                                     \
+  if (last) k_cpl_sweep<M, TO><<<g, 256, 0, ctx.stream>>>(nc, PRi.p, PRo.p, nbr.p, b, x, out);            \
+  else k_cpl_sweep<M, float><<<g, 256, 0, ctx.stream>>>(nc, PRi.p, PRo.p, nbr.p, b, x, tmp)
+    if (mcf == 4) { CPL_SWEEP(4); }
+    else if (mcf == 6) { CPL_SWEEP(6); }
+    else { CPL_SWEEP(8); }
+#undef CPL_SWEEP
+    x = tmp;
+  }
+  CCK(cudaGetLastError());
+  return FV3D_OK;
+}
+
+template <class T>
+fv3d_status Coupled::apply(Ctx& ctx, Implicit& im, const T* v, T* z) {
+  const int m = m_in, sw = sweep_count;
+  double* hb = hin.p + (size_t)m * kHcol;  // |v| and its inverse, then y at +8
+  // |v| (FP64 for a FP64 input, FP32 otherwise) and V_0 = v / |v|
+  fv3d_status st = im.gs_pass<T>(ctx, 0, const_cast<T*>(v), v, 1, nullptr, hb, 1.0, nullptr);
+  if (st != FV3D_OK) return st;
+  k_cpl_start<T><<<std::min(4096, nblk(n)), 256, 0, ctx.stream>>>(n, v, hb + 1, Vi.p);
+  CCK(cudaGetLastError());
+  const int g = nblk(nc);
+  for (int j = 0; j < m; ++j) {
+    float* vj = Vi.p + (size_t)j * ldb;
+    double* hc = hin.p + (size_t)j * kHcol;
+    // t = M_R v_j (into ui), w = P_A t
+    if ((st = sweeps<float>(ctx, sw, vj, ui.p)) != FV3D_OK) return st;
+    if (mcf == 4) k_cpl_product<4><<<g, 256, 0, ctx.stream>>>(nc, PAd.p, PAo.p, nbr.p, ui.p, wi.p);
+    else if (mcf == 6) k_cpl_product<6><<<g, 256, 0, ctx.stream>>>(nc, PAd.p, PAo.p, nbr.p, ui.p, wi.p);
+    else k_cpl_product<8><<<g, 256, 0, ctx.stream>>>(nc, PAd.p, PAo.p, nbr.p, ui.p, wi.p);
+    CCK(cudaGetLastError());
+    // classical Gram-Schmidt twice, v_{j+1} = w / |w| (the outer solve's passes, FP32)
+    if ((st = im.gs_pass<float>(ctx, 1, wi.p, Vi.p, j + 1, nullptr, hc, 0.0, nullptr)) != FV3D_OK) return st;
+    if ((st = im.gs_pass<float>(ctx, 2, wi.p, Vi.p, j + 1, hc, hc + 32, 0.0, nullptr, nullptr, hc + 64)) != FV3D_OK)
+      return st;
+    if ((st = im.gs_pass<float>(ctx, 3, wi.p, Vi.p, j + 1, hc + 32, nullptr, 0.0, nullptr, nullptr, nullptr,
+                                Vi.p + (size_t)(j + 1) * ldb, hc + 65)) != FV3D_OK)
+      return st;
+  }
+  k_cpl_lsq<<<1, 32, 0, ctx.stream>>>(m, hin.p);
+  k_cpl_combine<<<std::min(4096, nblk(n)), 256, 0, ctx.stream>>>(n, ldb, Vi.p, hb + 8, m, ui.p);
+  CCK(cudaGetLastError());
+  // z = M_R u
+  return sweeps<T>(ctx, sw, ui.p, z);
+}
+
+template fv3d_status Coupled::apply<float>(Ctx&, Implicit&, const float*, float*);
+template fv3d_status Coupled::apply<double>(Ctx&, Implicit&, const double*, double*);
+
+}  // namespace fv3d
+
+// ---------------------------------------------------------------------------
+// export of the last build's blocks (reference cell order)
+// ---------------------------------------------------------------------------
+using namespace fv3d;
+
+extern "C" fv3d_status fv3d_get_coupled_blocks(fv3d_ctx* handle, int which, double* diag, double* slots,
+                                               int* neighbour, int* max_slots) {
+  if (handle == nullptr || max_slots == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  const Coupled* cp = ctx->implicit ? ctx->implicit->coupled : nullptr;
+  if (cp == nullptr || cp->nc != ctx->nc) return ctx->fail(FV3D_ERR_STATE, "no coupled preconditioner built");
+  if (which != 0 && which != 1) return ctx->fail(FV3D_ERR_INVALID_ARG, "which must be 0 (P_A) or 1 (P_R)");
+  *max_slots = cp->mcf;
+  if (diag == nullptr && slots == nullptr && neighbour == nullptr) return FV3D_OK;
+  if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "cudaSetDevice");
+  const size_t nc = cp->nc, mcf = cp->mcf;
+  std::vector<float> d(25 * nc), o(mcf * 25 * nc);
+  std::vector<int> nb(mcf * nc);
+  const float* src_d = which ? cp->PRi.p : cp->PAd.p;
+  const float* src_o = which ? cp->PRo.p : cp->PAo.p;
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess ||
+      cudaMemcpy(d.data(), src_d, sizeof(float) * d.size(), cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(o.data(), src_o, sizeof(float) * o.size(), cudaMemcpyDeviceToHost) != cudaSuccess ||
+      cudaMemcpy(nb.data(), cp->nbr.p, sizeof(int) * nb.size(), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return ctx->fail(FV3D_ERR_DEVICE, "copy coupled blocks");
+  for (size_t c = 0; c < nc; ++c) {
+    const size_t r = (size_t)ctx->perm[c];
+    for (int e = 0; e < 25; ++e) {
+      if (diag) diag[r * 25 + e] = d[(size_t)e * nc + c];
+      for (size_t k = 0; k < mcf; ++k)
+        if (slots) slots[(r * mcf + k) * 25 + e] = o[(k * 25 + e) * nc + c];
+    }
+    if (neighbour)
+      for (size_t k = 0; k < mcf; ++k) {
+        const int x = nb[k * nc + c];
+        neighbour[r * mcf + k] = (x < 0) ? -1 : ctx->perm[x];
+      }
+  }
+  return FV3D_OK;
+}

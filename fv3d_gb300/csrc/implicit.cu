@@ -30,6 +30,7 @@
 
 #include "context.h"
 #include "implicit.h"
+#include "fo_flux.cuh"
 
 namespace fv3d {
 
@@ -504,54 +505,6 @@ __global__ void k_make_record(int nc, const double* __restrict__ W, float* __res
 }
 
 // ---- first-order FD diagonal blocks ---------------------------------------
-// global-frame convective flux . n (FP64): AUSM or Rusanov
-__device__ void fo_flux(const double* l, const double* r, const double* n, const PhysConst& pc,
-                        double* F) {
-  const double km1 = pc.km1, kappa = pc.kappa;
-  const double irl = 1.0 / l[0], irr = 1.0 / r[0];
-  const double ul = l[1] * irl, vl = l[2] * irl, wl = l[3] * irl;
-  const double ur = r[1] * irr, vr = r[2] * irr, wr = r[3] * irr;
-  const double pl = fmax(1.00E-10, km1 * (l[4] - 0.5 * (l[1] * ul + l[2] * vl + l[3] * wl)));
-  const double pr = fmax(1.00E-10, km1 * (r[4] - 0.5 * (r[1] * ur + r[2] * vr + r[3] * wr)));
-  const double unl = ul * n[0] + vl * n[1] + wl * n[2];
-  const double unr = ur * n[0] + vr * n[1] + wr * n[2];
-  const double cl = sqrt(kappa * pl * irl), cr = sqrt(kappa * pr * irr);
-  if (pc.flux == 1) {
-    const double lam = fmax(fabs(unl) + cl, fabs(unr) + cr);
-    F[0] = 0.5 * (l[0] * unl + r[0] * unr) - 0.5 * lam * (r[0] - l[0]);
-    for (int d = 0; d < 3; ++d)
-      F[1 + d] = 0.5 * (l[1 + d] * unl + pl * n[d] + r[1 + d] * unr + pr * n[d]) - 0.5 * lam * (r[1 + d] - l[1 + d]);
-    F[4] = 0.5 * ((l[4] + pl) * unl + (r[4] + pr) * unr) - 0.5 * lam * (r[4] - l[4]);
-  } else {
-    const double Ml = unl / cl, Mr = unr / cr;
-    double mp, pp, mm, pm;
-    if (Ml <= -1.0) { mp = 0.0; pp = 0.0; }
-    else if (Ml < 1.0) { mp = 0.25 * (Ml + 1.0) * (Ml + 1.0); pp = 0.25 * pl * (1.0 + Ml) * (1.0 + Ml) * (2.0 - Ml); }
-    else { mp = Ml; pp = pl; }
-    if (Mr <= -1.0) { mm = Mr; pm = pr; }
-    else if (Mr < 1.0) { mm = -0.25 * (Mr - 1.0) * (Mr - 1.0); pm = 0.25 * pr * (1.0 - Mr) * (1.0 - Mr) * (2.0 + Mr); }
-    else { mm = 0.0; pm = 0.0; }
-    const double mdl = fmax(0.0, mp + mm) * cl * l[0];
-    const double mdr = fmin(0.0, mp + mm) * cr * r[0];
-    F[0] = mdl + mdr;
-    F[1] = mdl * ul + mdr * ur + (pp + pm) * n[0];
-    F[2] = mdl * vl + mdr * vr + (pp + pm) * n[1];
-    F[3] = mdl * wl + mdr * wr + (pp + pm) * n[2];
-    F[4] = mdl * (l[4] + pl) * irl + mdr * (r[4] + pr) * irr;
-  }
-  // two-point viscous flux across the face: -mu du/dn, -(mu u.du/dn + k dT/dn)
-  if (pc.mu != 0.0) {
-    const double id = 1.0 / n[3];  // n[3] carries the centre distance
-    const double mu = pc.mu, k = pc.heat_lambda;
-    const double Tl = pl * irl / pc.R_mix, Tr = pr * irr / pc.R_mix;
-    const double du = ur - ul, dv = vr - vl, dw = wr - wl;
-    F[1] -= mu * du * id;
-    F[2] -= mu * dv * id;
-    F[3] -= mu * dw * id;
-    F[4] -= (mu * (0.5 * (ul + ur) * du + 0.5 * (vl + vr) * dv + 0.5 * (wl + wr) * dw) + k * (Tr - Tl)) * id;
-  }
-}
-
 // D_c = I/dt_c + (1/V_c) sum_f d(F_f . n_out A_f)/dU_c  (column-major 5x5)
 __global__ void k_fo_blocks(KArgs<double> a, const double* __restrict__ dtl,
                             const double* __restrict__ fdist, double* __restrict__ D) {
@@ -919,9 +872,18 @@ fv3d_status Implicit::norm(Ctx& ctx, const double* v, double* out) {
   return FV3D_OK;
 }
 
+// the cell-coupling preconditioner (coupled.cu) runs its inner Gram-Schmidt
+// passes in FP32 and the norm of its input in the input's type
+template fv3d_status Implicit::gs_pass<float>(Ctx&, int, float*, const float*, int, const double*, double*, double,
+                                              const double*, const float*, double*, float*, const double*);
+template fv3d_status Implicit::gs_pass<double>(Ctx&, int, double*, const double*, int, const double*, double*,
+                                               double, const double*, const double*, double*, double*,
+                                               const double*);
+
 template <class T>
 fv3d_status Implicit::precondition(Ctx& ctx, const T* v, T* z) {
   if (opts.preconditioner == FV3D_PC_LEARNED && !use_block_jacobi) return ctx.mlp->apply(ctx, v, z);
+  if (opts.preconditioner == FV3D_PC_COUPLED) return coupled->apply<T>(ctx, *this, v, z);
   if (opts.preconditioner == FV3D_PC_NONE) {
     if (z != v) ICK(cudaMemcpyAsync(z, v, sizeof(T) * n, cudaMemcpyDeviceToDevice, ctx.stream));
     return FV3D_OK;
@@ -973,6 +935,12 @@ fv3d_status Implicit::build_blocks(Ctx& ctx) {
   // no preconditioner: no blocks, unless a harvest wants them as features
   const bool harvesting = ctx.mlp && ctx.mlp->ready && ctx.mlp->harvest_per_step > 0;
   if (opts.preconditioner == FV3D_PC_NONE && !harvesting) return FV3D_OK;
+  if (opts.preconditioner == FV3D_PC_COUPLED) {
+    if (coupled == nullptr) coupled = new Coupled();
+    fv3d_status st = coupled->setup(ctx, *this, opts.inner_dim, opts.inner_sweeps);
+    if (st == FV3D_OK) st = coupled->build(ctx, *this);
+    return st;
+  }
   if (opts.preconditioner == FV3D_PC_LUMPED) {
     // every cell perturbed at once by +-eps/2, eps = 1e-4 ||U_v||_2 (implicit.c:65-117)
     std::vector<double> slice(ctx.nc);
@@ -1152,6 +1120,12 @@ fv3d_status Implicit::fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res
 fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit_stats* stats) {
   opts = o;
   if (opts.krylov_dim < 1 || opts.krylov_dim > 31) return ctx.fail(FV3D_ERR_INVALID_ARG, "krylov_dim must be 1..31");
+  if (opts.preconditioner == FV3D_PC_COUPLED) {
+    if (opts.inner_dim == 0) opts.inner_dim = 10;
+    if (opts.inner_sweeps == 0) opts.inner_sweeps = 2;
+    if (opts.inner_dim < 1 || opts.inner_dim > 30 || opts.inner_sweeps < 1 || opts.inner_sweeps > 8)
+      return ctx.fail(FV3D_ERR_INVALID_ARG, "inner_dim must be 1..30 and inner_sweeps 1..8");
+  }
   if (opts.preconditioner == FV3D_PC_LEARNED && !(ctx.mlp && ctx.mlp->ready))
     return ctx.fail(FV3D_ERR_STATE, "learned preconditioner requested but no MLP initialised");
   fv3d_status st = ensure_fp64_path(ctx);
@@ -1423,6 +1397,8 @@ extern "C" fv3d_status fv3d_implicit_default_opts(fv3d_implicit_opts* o) {
   o->pc_refresh = 1;
   o->max_restarts = 0;
   o->sync_every = 10;
+  o->inner_dim = 10;
+  o->inner_sweeps = 2;
   return FV3D_OK;
 }
 
@@ -1434,7 +1410,7 @@ extern "C" fv3d_status fv3d_solve_implicit(fv3d_ctx* handle, const fv3d_implicit
   for (int b = 0; b < ctx->nb; ++b)
     if (!(ctx->region_set & (1u << ctx->h_fregion[b])))
       return ctx->fail(FV3D_ERR_STATE, "boundary region %d has no condition", ctx->h_fregion[b]);
-  if (opts->preconditioner < 0 || opts->preconditioner > FV3D_PC_NONE || opts->jv_precision < 0 ||
+  if (opts->preconditioner < 0 || opts->preconditioner > FV3D_PC_COUPLED || opts->jv_precision < 0 ||
       opts->jv_precision > 1 || !(opts->tol_rel > 0.0) || !(opts->cfl_start > 0.0) || opts->max_newton < 0)
     return ctx->fail(FV3D_ERR_INVALID_ARG, "bad implicit options");
   if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "cudaSetDevice");

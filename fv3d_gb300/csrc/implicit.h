@@ -33,6 +33,26 @@ struct Mlp {
   fv3d_status harvest(Ctx& ctx, const Implicit& im);
 };
 
+// cell-coupling preconditioner (coupled.cu): z = M v, M an inner GMRES on
+// P_A = I/dt - dR1/dU right-preconditioned by block-Jacobi sweeps of the
+// first-order Rusanov Jacobian P_R
+struct Coupled {
+  int nc = 0, mcf = 0, m_cap = 0;  // sizes the buffers are allocated for
+  int m_in = 0, sweep_count = 0;   // inner GMRES iterations and sweeps of the current solve
+  size_t n = 0, ldb = 0;
+  DevBuf<int> nbr;                 // [mcf][nc] neighbour of each face slot, -1 ghost or none
+  DevBuf<float> PAd, PAo;          // P_A: diagonal blocks [25][nc], slot blocks [mcf][25][nc]
+  DevBuf<float> PRi, PRo;          // P_R: inverted diagonal blocks [25][nc], slot blocks [mcf][25][nc]
+  DevBuf<float> Vi, wi, ti, ui;    // inner basis [(m_in + 1)][ldb], work vectors [ldb]
+  DevBuf<double> hin;              // inner Hessenberg columns [m_in + 1][72] and y
+  fv3d_status setup(Ctx& ctx, Implicit& im, int m_inner, int n_sweeps);
+  fv3d_status build(Ctx& ctx, Implicit& im);
+  template <class T>
+  fv3d_status apply(Ctx& ctx, Implicit& im, const T* v, T* z);
+  template <class TO>
+  fv3d_status sweeps(Ctx& ctx, int count, const float* b, TO* out);
+};
+
 struct Implicit {
   fv3d_implicit_opts opts;
   size_t n = 0;   // 5 * cells
@@ -50,9 +70,11 @@ struct Implicit {
   double* hcols = nullptr;        // pinned: each Arnoldi step's coefficients, [32][kHostCoefs]
 
   std::map<long long, cudaGraphExec_t> arnoldi_graphs;  // captured Arnoldi steps
+  Coupled* coupled = nullptr;     // FV3D_PC_COUPLED work space, created on first use
 
   ~Implicit() {
     release_graphs();
+    delete coupled;
     if (hpin) cudaFreeHost(hpin);
     if (hcols) cudaFreeHost(hcols);
   }

@@ -201,7 +201,12 @@ enum {
     FV3D_PC_BLOCK_JACOBI = 0,  /* first-order diagonal blocks (FD, FP64 build, FP32 apply) */
     FV3D_PC_LUMPED = 1,        /* the reference's lumped blocks (implicit.c:61-119) */
     FV3D_PC_LEARNED = 2,       /* per-cell MLP, block-Jacobi fallback on stagnation */
-    FV3D_PC_NONE = 3
+    FV3D_PC_NONE = 3,
+    FV3D_PC_COUPLED = 4        /* couples cells: inner GMRES(inner_dim) on I/dt - dR1/dU, R1 the
+                                  first-order inviscid residual with the case's flux (its blocks
+                                  by finite differences per face), right-preconditioned by
+                                  inner_sweeps block-Jacobi sweeps of the first-order Rusanov
+                                  Jacobian (analytic, wave speed frozen) */
 };
 typedef struct fv3d_implicit_opts {
     double cfl_start;      /* initial CFL (100) */
@@ -218,6 +223,9 @@ typedef struct fv3d_implicit_opts {
     int sync_every;        /* Arnoldi steps launched between host synchronisations (10; 0 takes
                               10): the Givens rotations of a chunk run after it, so a cycle that
                               meets eta inside a chunk computes up to sync_every - 1 unused steps */
+    int inner_dim;         /* FV3D_PC_COUPLED: inner GMRES iterations per application, 1..30 (10) */
+    int inner_sweeps;      /* FV3D_PC_COUPLED: Rusanov block-Jacobi sweeps per inner
+                              preconditioning, 1..8 (2) */
 } fv3d_implicit_opts;
 typedef struct fv3d_implicit_stats {
     int newton_steps;
@@ -238,6 +246,16 @@ fv3d_status fv3d_implicit_history(const fv3d_ctx *ctx, double *res, int max, int
 /* 5x5 blocks of the last preconditioner build, [n_cells][25] column-major,
  * reference cell order (lumped blocks: compare with calc_jacobian_numerical) */
 fv3d_status fv3d_get_blocks(fv3d_ctx *ctx, double *blocks);
+/* Blocks of the last FV3D_PC_COUPLED build (no reference counterpart: the
+ * reference's preconditioner is its lumped diagonal, implicit.c:61-119), in
+ * reference cell order, row-major 5x5: which 0 gives P_A = I/dt - dR1/dU
+ * (diagonal blocks and one block per face slot), which 1 the Rusanov matrix
+ * P_R (its inverted diagonal blocks and its slot blocks).  diag [n_cells*25],
+ * slots [n_cells*max_slots*25], neighbour [n_cells*max_slots] (the slot's
+ * other cell, -1 for a boundary face or an unused slot); *max_slots is set
+ * first, and NULL arrays are skipped. */
+fv3d_status fv3d_get_coupled_blocks(fv3d_ctx *ctx, int which, double *diag, double *slots,
+                                    int *neighbour, int *max_slots);
 /* The implicit solve's matrix-free Jacobian-vector product at the current
  * state, J z = (R(U + eps z) - R(U)) / eps (the product the reference forms
  * from its lumped blocks in matrix_vector_numerical, implicit.c:362-384,

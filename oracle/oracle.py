@@ -25,7 +25,23 @@ LIBS = {
     # load only in a process started with libasan preloaded
     "restated_san": os.path.join(HERE, "_san", "liboracle_san.so"),
 }
-REFERENCE_TREE = os.environ.get("FV3D_REFERENCE_TREE", "/root/reference")
+
+
+def reference_tree() -> str:
+    """The reference source tree: FV3D_REFERENCE_TREE when set, else the
+    default of the build recipe oracle/Makefile.ref (the one file that names
+    where the tree lies on the build machine)."""
+    env = os.environ.get("FV3D_REFERENCE_TREE")
+    if env:
+        return env
+    p = subprocess.run(["make", "-s", "-f", os.path.join(HERE, "Makefile.ref"), "print-ref"],
+                       capture_output=True, text=True)
+    return p.stdout.strip() if p.returncode == 0 else ""
+
+
+def reference_tree_present() -> bool:
+    return os.path.isdir(os.path.join(reference_tree(), "src", "Solver"))
+
 
 _f8p = C.POINTER(C.c_double)
 _i4p = C.POINTER(C.c_int)
@@ -53,8 +69,8 @@ def build(which: str = "restated", quiet: bool = True) -> str:
     """Compile the oracle library (gcc).  "reference" needs the reference tree."""
     mk = "Makefile.ref" if which == "reference" else "Makefile"
     args = ["make", "-s", "-f", os.path.join(HERE, mk)]
-    if which == "reference":
-        args.append(f"REF={REFERENCE_TREE}")
+    if which == "reference" and os.environ.get("FV3D_REFERENCE_TREE"):
+        args.append(f"REF={os.environ['FV3D_REFERENCE_TREE']}")
     elif which == "restated_san":
         args.append("sanitize")
     subprocess.run(args, check=True, capture_output=quiet)

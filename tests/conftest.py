@@ -7,7 +7,11 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE = os.environ.get("FV3D_REFERENCE_TREE", "/root/reference")
+from oracle.oracle import reference_tree  # noqa: E402
+
+# the reference source tree (FV3D_REFERENCE_TREE, else the oracle build
+# recipe's default); tests that read it skip where it is absent
+REFERENCE = reference_tree()
 
 
 def pytest_configure(config):

@@ -1,7 +1,9 @@
-"""The Python examples in README.md and INTEGRATION.md call what exists:
-every module function and Solver method they name is there and accepts
-the arguments they pass (parsed, not run: running them needs a GPU)."""
+"""The Python examples (fv3d_gb300/examples/*.py) call what exists: every
+module function and Solver method they name is there and accepts the
+arguments they pass (parsed, not run: running them needs a GPU); and the
+code that README.md and INTEGRATION.md show is quoted from them verbatim."""
 import ast
+import glob
 import inspect
 import os
 import re
@@ -12,15 +14,20 @@ from fv3d_gb300 import api, cases, gmsh, params
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 MODULES = {"api": api, "cases": cases, "params": params, "gmsh": gmsh}
+EXAMPLES = sorted(glob.glob(os.path.join(ROOT, "fv3d_gb300", "examples", "*.py")))
 
 
 def examples():
-    out = []
-    for doc in ("README.md", "INTEGRATION.md"):
-        text = open(os.path.join(ROOT, doc)).read()
-        for k, block in enumerate(re.findall(r"```python\n(.*?)```", text, flags=re.S)):
-            out.append(pytest.param(block, id=f"{doc}:{k}"))
-    return out
+    return [pytest.param(open(p).read(), id=os.path.basename(p)) for p in EXAMPLES]
+
+
+@pytest.mark.parametrize("doc", ["README.md", "INTEGRATION.md"])
+def test_documented_code_is_quoted_from_the_examples(doc):
+    sources = [open(p).read() for p in EXAMPLES]
+    blocks = re.findall(r"```python\n(.*?)```", open(os.path.join(ROOT, doc)).read(), flags=re.S)
+    assert blocks
+    for b in blocks:
+        assert any(b in s for s in sources), f"{doc}: a python block is not in fv3d_gb300/examples/"
 
 
 def _target(call, solver_names):

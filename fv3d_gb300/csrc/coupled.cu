@@ -23,10 +23,11 @@
 // next without changing the answer.
 //
 // Storage: FP32 blocks, row-major within a block, element-major over cells
-// ([e][nc]: a warp's loads of element e are contiguous); slot blocks
-// [slot][e][nc].  Blocks are built per Newton step in FP64: P_A's by forward
-// finite differences of each face flux (h = 1e-7 max(|U_v|, 1e-3)), P_R's
-// analytically.  Every product and sweep is a cell gather: no atomics, no
+// ([e][nc]: a warp's loads of element e are contiguous); P_A's slot blocks
+// [slot][e][nc].  P_R's slot blocks are a A(U_o) + b I, applied without being
+// stored (per slot the normal and a, b; per cell (u, v, w, H)).  Built per
+// Newton step in FP64: P_A's blocks by forward finite differences of each
+// face flux (h = 1e-7 max(|U_v|, 1e-3)), P_R's analytically.  Every product and sweep is a cell gather: no atomics, no
 // face buffers.  The inner Krylov basis, its Gram-Schmidt passes and the
 // sweeps run in FP32; the inner least-squares problem in FP64 on the device,
 // so an application needs no host synchronisation and is captured in the
@@ -223,10 +224,36 @@ __device__ bool invert5(const double* B, double* X) {
   return true;
 }
 
-// P_R: the Rusanov Jacobian's slot blocks and its inverted diagonal blocks
+// P_R's slot blocks are applied without being stored: the block of slot k
+// is a_k A(U_o) + b_k I (the Euler flux Jacobian of the neighbour's state
+// along the face normal, a and b from the face's area, volume, wave speed and
+// side), so a sweep reads per slot the normal and two scalars plus the
+// neighbour's (u, v, w, H) instead of 25 entries.
+// A(U; n) x in FP32 from the state's (u, v, w, H):
+//   dp = phi x0 - (g-1) u.x_m + (g-1) x4,  phi = (g-1) |u|^2 / 2,
+//   (A x)_0 = n.x_m,  (A x)_m = n dp + u (n.x_m - un x0) + un x_m,
+//   (A x)_4 = H (n.x_m - un x0) + un (dp + x4)
+__device__ __forceinline__ void rus_jx(const float4 st, float gm1, const float4 n, const float* x, float* y) {
+  const float un = st.x * n.x + st.y * n.y + st.z * n.z;
+  const float nm = n.x * x[1] + n.y * x[2] + n.z * x[3];
+  const float um = st.x * x[1] + st.y * x[2] + st.z * x[3];
+  const float phi = 0.5f * gm1 * (st.x * st.x + st.y * st.y + st.z * st.z);
+  const float dp = phi * x[0] - gm1 * um + gm1 * x[4];
+  const float q = nm - un * x[0];
+  y[0] = nm;
+  y[1] = n.x * dp + st.x * q + un * x[1];
+  y[2] = n.y * dp + st.y * q + un * x[2];
+  y[3] = n.z * dp + st.z * q + un * x[3];
+  y[4] = st.w * q + un * (dp + x[4]);
+}
+
+// P_R: the inverted diagonal blocks (FP64 Gauss-Jordan, stored FP32), the
+// slot coefficients of the matrix-free off-diagonal blocks and the cell's
+// (u, v, w, H)
 template <int MCF>
 __global__ void __launch_bounds__(128) k_cpl_build_pr(KArgs<double> a, const double* __restrict__ dtl,
-                                                      float* __restrict__ PRi, float* __restrict__ PRo) {
+                                                      float* __restrict__ PRi, float4* __restrict__ rna,
+                                                      float* __restrict__ rb, float4* __restrict__ st4) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.nc) return;
   const size_t nc = a.nc;
@@ -237,6 +264,11 @@ __global__ void __launch_bounds__(128) k_cpl_build_pr(KArgs<double> a, const dou
 #pragma unroll
   for (int j = 0; j < 5; ++j) qc[j] = a.U[(size_t)j * nc + c];
   cons_to_prims(qc, ph);
+  {
+    const double ir = 1.0 / qc[0];
+    st4[c] = make_float4((float)(qc[1] * ir), (float)(qc[2] * ir), (float)(qc[3] * ir),
+                         (float)((qc[4] + qc[PR]) * ir));
+  }
   const double iv = 1.0 / a.vol[c];
   double D[25];
 #pragma unroll
@@ -245,9 +277,9 @@ __global__ void __launch_bounds__(128) k_cpl_build_pr(KArgs<double> a, const dou
 #pragma unroll
   for (int j = 0; j < 5; ++j) D[j * 5 + j] = idt;
   for (int k = 0; k < MCF; ++k) {
-    float* Ok = PRo + (size_t)k * 25 * nc + c;
+    const size_t sk = (size_t)k * nc + c;
     const int e = a.cface[(size_t)c * MCF + k];
-    if (e < 0) { zero_block(Ok, nc); continue; }
+    if (e < 0) { rna[sk] = make_float4(0.f, 0.f, 0.f, 0.f); rb[sk] = 0.f; continue; }
     const int f = e >> 1, side = e & 1;
     const double* g = a.geo + (size_t)f * GEO;
     const bool bnd = f >= a.nf_int;
@@ -267,11 +299,9 @@ __global__ void __launch_bounds__(128) k_cpl_build_pr(KArgs<double> a, const dou
       // own: cell 0 -> (A + lam I) / 2, cell 1 -> (A - lam I) / 2; the other the opposite
       const double so = side ? -lam : lam;
 #pragma unroll
-      for (int e2 = 0; e2 < 25; ++e2) {
-        const double id = (e2 % 6 == 0) ? 1.0 : 0.0;
-        D[e2] += w * 0.5 * (Ac[e2] + so * id);
-        Ok[(size_t)e2 * nc] = (float)(w * 0.5 * (Ao[e2] - so * id));
-      }
+      for (int e2 = 0; e2 < 25; ++e2) D[e2] += w * 0.5 * (Ac[e2] + ((e2 % 6 == 0) ? so : 0.0));
+      rna[sk] = make_float4((float)n[0], (float)n[1], (float)n[2], (float)(0.5 * w));
+      rb[sk] = (float)(-0.5 * w * so);
     } else {
       const int region = a.fregion[f - a.nf_int];
       double qg[10], Ag[25], lg;
@@ -301,7 +331,8 @@ __global__ void __launch_bounds__(128) k_cpl_build_pr(KArgs<double> a, const dou
           D[i * 5 + j] += w * s;
         }
       }
-      zero_block(Ok, nc);
+      rna[sk] = make_float4(0.f, 0.f, 0.f, 0.f);
+      rb[sk] = 0.f;
     }
   }
   double X[25];
@@ -310,6 +341,32 @@ __global__ void __launch_bounds__(128) k_cpl_build_pr(KArgs<double> a, const dou
     for (int e = 0; e < 25; ++e) X[e] = (e % 6 == 0) ? 1.0 / D[e] : 0.0;
   }
   store_block(PRi + c, nc, X);
+}
+
+// P_R's slot blocks written out (for the block export): column j of slot k
+// is a A(U_o) e_j + b e_j, by the sweep's own arithmetic
+template <int MCF>
+__global__ void k_cpl_expand_pr(int nc, const int* __restrict__ nbr, const float4* __restrict__ rna,
+                                const float* __restrict__ rb, const float4* __restrict__ st4, float gm1,
+                                float* __restrict__ O) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  for (int k = 0; k < MCF; ++k) {
+    const size_t sk = (size_t)k * nc + c;
+    float* Ok = O + (size_t)k * 25 * nc + c;
+    const int o = nbr[sk];
+    for (int j = 0; j < 5; ++j) {
+      float x[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, y[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      x[j] = 1.f;
+      if (o >= 0) {
+        rus_jx(st4[o], gm1, rna[sk], x, y);
+#pragma unroll
+        for (int i = 0; i < 5; ++i) y[i] = rna[sk].w * y[i] + rb[sk] * x[i];
+      }
+#pragma unroll
+      for (int i = 0; i < 5; ++i) Ok[(size_t)(i * 5 + j) * nc] = y[i];
+    }
+  }
 }
 
 __device__ __forceinline__ void ld5(const float* __restrict__ x, size_t nc, int c, float* v) {
@@ -350,27 +407,32 @@ __global__ void __launch_bounds__(256) k_cpl_product(int nc, const float* __rest
   for (int j = 0; j < 5; ++j) y[(size_t)j * nc + c] = acc[j];
 }
 
-// one block-Jacobi sweep y = Dinv (b - O x) (x null: y = Dinv b)
+// one block-Jacobi sweep of P_R, y = Dinv (b - O x) (x null: y = Dinv b),
+// the slot blocks O applied matrix-free
 template <int MCF, class TO>
-__global__ void __launch_bounds__(256) k_cpl_sweep(int nc, const float* __restrict__ Di, const float* __restrict__ O,
-                                                   const int* __restrict__ nbr, const float* __restrict__ b,
-                                                   const float* __restrict__ x, TO* __restrict__ y) {
+__global__ void __launch_bounds__(256) k_cpl_sweep(int nc, const float* __restrict__ Di, const int* __restrict__ nbr,
+                                                   const float4* __restrict__ rna, const float* __restrict__ rb,
+                                                   const float4* __restrict__ st4, float gm1,
+                                                   const float* __restrict__ b, const float* __restrict__ x,
+                                                   TO* __restrict__ y) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
   float t[5], r[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
   ld5(b, nc, c, t);
   if (x != nullptr) {
-    float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int k = 0; k < MCF; ++k) {
-      const int o = __ldg(nbr + (size_t)k * nc + c);
+      const size_t sk = (size_t)k * nc + c;
+      const int o = __ldg(nbr + sk);
       if (o < 0) continue;
-      float xo[5];
+      float xo[5], jx[5];
       ld5(x, nc, o, xo);
-      block_mul_add(O + (size_t)k * 25 * nc + c, nc, xo, s);
-    }
+      const float4 na = __ldg(rna + sk);
+      const float bk = __ldg(rb + sk);
+      rus_jx(__ldg(st4 + o), gm1, na, xo, jx);
 #pragma unroll
-    for (int j = 0; j < 5; ++j) t[j] -= s[j];
+      for (int j = 0; j < 5; ++j) t[j] -= na.w * jx[j] + bk * xo[j];
+    }
   }
   block_mul_add(Di + c, nc, t, r);
 #pragma unroll
@@ -465,7 +527,9 @@ fv3d_status Coupled::setup(Ctx& ctx, Implicit& im, int m_inner, int n_sweeps) {
   if (e == cudaSuccess) e = PAd.alloc(25 * (size_t)nc);
   if (e == cudaSuccess) e = PAo.alloc((size_t)mcf * 25 * nc);
   if (e == cudaSuccess) e = PRi.alloc(25 * (size_t)nc);
-  if (e == cudaSuccess) e = PRo.alloc((size_t)mcf * 25 * nc);
+  if (e == cudaSuccess) e = rna.alloc((size_t)mcf * nc);
+  if (e == cudaSuccess) e = rb.alloc((size_t)mcf * nc);
+  if (e == cudaSuccess) e = st4.alloc(nc);
   if (e == cudaSuccess) e = Vi.alloc((size_t)(m_cap + 1) * ldb);
   if (e == cudaSuccess) e = wi.alloc(ldb);
   if (e == cudaSuccess) e = ti.alloc(ldb);
@@ -486,7 +550,7 @@ fv3d_status Coupled::build(Ctx& ctx, Implicit& im) {
   const int g = nblk(nc, 128);
 #define CPL_BUILD(M)                                                                           \
   k_cpl_build_pa<M><<<g, 128, 0, ctx.stream>>>(a, im.dtl.p, PAd.p, PAo.p, 0);                 \
-  k_cpl_build_pr<M><<<g, 128, 0, ctx.stream>>>(a, im.dtl.p, PRi.p, PRo.p)
+  k_cpl_build_pr<M><<<g, 128, 0, ctx.stream>>>(a, im.dtl.p, PRi.p, rna.p, rb.p, st4.p)
   if (mcf == 4) { CPL_BUILD(4); }
   else if (mcf == 6) { CPL_BUILD(6); }
   else { CPL_BUILD(8); }
@@ -499,14 +563,15 @@ fv3d_status Coupled::build(Ctx& ctx, Implicit& im) {
 template <class TO>
 fv3d_status Coupled::sweeps(Ctx& ctx, int count, const float* b, TO* out) {
   const int g = nblk(nc);
-  // sweeps alternate between ti and ui... the last one writes out; b is never overwritten
+  const float gm1 = (float)ctx.phys.km1;
+  // the sweeps alternate between ti and wi, the last one writes out; b is never overwritten
   const float* x = nullptr;
   for (int s = 0; s < count; ++s) {
     const bool last = (s == count - 1);
     float* tmp = (s % 2 == 0) ? ti.p : wi.p;
 #define CPL_SWEEP(M)                                                                                     \
-  if (last) k_cpl_sweep<M, TO><<<g, 256, 0, ctx.stream>>>(nc, PRi.p, PRo.p, nbr.p, b, x, out);            \
-  else k_cpl_sweep<M, float><<<g, 256, 0, ctx.stream>>>(nc, PRi.p, PRo.p, nbr.p, b, x, tmp)
+  if (last) k_cpl_sweep<M, TO><<<g, 256, 0, ctx.stream>>>(nc, PRi.p, nbr.p, rna.p, rb.p, st4.p, gm1, b, x, out); \
+  else k_cpl_sweep<M, float><<<g, 256, 0, ctx.stream>>>(nc, PRi.p, nbr.p, rna.p, rb.p, st4.p, gm1, b, x, tmp)
     if (mcf == 4) { CPL_SWEEP(4); }
     else if (mcf == 6) { CPL_SWEEP(6); }
     else { CPL_SWEEP(8); }
@@ -575,7 +640,17 @@ extern "C" fv3d_status fv3d_get_coupled_blocks(fv3d_ctx* handle, int which, doub
   std::vector<float> d(25 * nc), o(mcf * 25 * nc);
   std::vector<int> nb(mcf * nc);
   const float* src_d = which ? cp->PRi.p : cp->PAd.p;
-  const float* src_o = which ? cp->PRo.p : cp->PAo.p;
+  DevBuf<float> expanded;  // P_R's slot blocks, written out by the sweep's arithmetic
+  if (which) {
+    if (expanded.alloc(mcf * 25 * nc) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "allocation");
+    const int g = (int)((nc + 255) / 256);
+    const float gm1 = (float)ctx->phys.km1;
+    if (mcf == 4) k_cpl_expand_pr<4><<<g, 256, 0, ctx->stream>>>((int)nc, cp->nbr.p, cp->rna.p, cp->rb.p, cp->st4.p, gm1, expanded.p);
+    else if (mcf == 6) k_cpl_expand_pr<6><<<g, 256, 0, ctx->stream>>>((int)nc, cp->nbr.p, cp->rna.p, cp->rb.p, cp->st4.p, gm1, expanded.p);
+    else k_cpl_expand_pr<8><<<g, 256, 0, ctx->stream>>>((int)nc, cp->nbr.p, cp->rna.p, cp->rb.p, cp->st4.p, gm1, expanded.p);
+    if (cudaGetLastError() != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "expand P_R blocks");
+  }
+  const float* src_o = which ? expanded.p : cp->PAo.p;
   if (cudaStreamSynchronize(ctx->stream) != cudaSuccess ||
       cudaMemcpy(d.data(), src_d, sizeof(float) * d.size(), cudaMemcpyDeviceToHost) != cudaSuccess ||
       cudaMemcpy(o.data(), src_o, sizeof(float) * o.size(), cudaMemcpyDeviceToHost) != cudaSuccess ||

@@ -42,7 +42,9 @@ struct Coupled {
   size_t n = 0, ldb = 0;
   DevBuf<int> nbr;                 // [mcf][nc] neighbour of each face slot, -1 ghost or none
   DevBuf<float> PAd, PAo;          // P_A: diagonal blocks [25][nc], slot blocks [mcf][25][nc]
-  DevBuf<float> PRi, PRo;          // P_R: inverted diagonal blocks [25][nc], slot blocks [mcf][25][nc]
+  DevBuf<float> PRi;               // P_R: inverted diagonal blocks [25][nc]; its slot blocks are applied
+  DevBuf<float4> rna, st4;         // matrix-free: per slot (normal, a) [mcf][nc], per cell (u, v, w, H)
+  DevBuf<float> rb;                // per slot b [mcf][nc]
   DevBuf<float> Vi, wi, ti, ui;    // inner basis [(m_in + 1)][ldb], work vectors [ldb]
   DevBuf<double> hin;              // inner Hessenberg columns [m_in + 1][72] and y
   fv3d_status setup(Ctx& ctx, Implicit& im, int m_inner, int n_sweeps);

@@ -14,6 +14,10 @@ roofline: the dominant kernel's algorithmic bytes (the fixed byte model in
          byte_model below) / its average CUDA-event duration, against the
          measured HBM copy bandwidth
 cpu_baseline: the FP64 CPU oracle on the host cores, bounded sample
+error_vs_fp64: the mixed path against the FP64 GPU path over the first steps
+implicit: the implicit steady channel (96 x 48 x 48): seconds to a 1e-8
+         relative residual with each preconditioner, end to end through the
+         C ABI, the reference's implicit step on the GPU and on the host
 
 --impl reference times the CPU implementation of the path (the reference's
 own sources when they were built here, else the C restatement) on the host
@@ -55,6 +59,10 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--max-newton", type=int, default=400,
                    help="channel: Newton step limit per solve (a small value for profiling runs)")
+    p.add_argument("--no-implicit", action="store_true",
+                   help="skip the implicit channel solve the default run adds to its line")
+    p.add_argument("--fp64-check-steps", type=int, default=200,
+                   help="explicit steps of the mixed-vs-FP64 error check the default run adds")
     return p.parse_args()
 
 
@@ -218,23 +226,75 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def run_channel(args):
+CHANNEL_KEYS = ("converged", "newton_steps", "gmres_iterations", "jv_evaluations", "rel_res", "wall_ms",
+                "fallbacks")
+
+
+def implicit_cpu_baseline(c, steps=2):
+    """The reference's implicit time step (timestep_newton, implicit.c:224-351:
+    one Newton iteration with the lumped Jacobian of calc_jacobian_numerical,
+    ten residuals, and the block-diagonal solve; steady, so the step ends
+    after its first iteration, within max_iter_inner = 2) on the host:
+    seconds per step over `steps` steps after one warm-up step, one core."""
+    from oracle import oracle as orc
+    which = "reference" if orc.available("reference") else "restated"
+    o = orc.Oracle(which)
+    o.init(c.mesh, c.params, c.region_type, c.region_prim)
+    o.set_conserved(c.u0)
+    dt = o.timestep_convective(1.0)
+    o.step_newton(0, 0.0, dt, scheme=0, solver=1, max_iter_inner=2, is_transient=False)
+    t0 = time.perf_counter()
+    for k in range(steps):
+        o.step_newton(k + 1, 0.0, dt, scheme=0, solver=1, max_iter_inner=2, is_transient=False)
+    secs = time.perf_counter() - t0
+    return {"value": round(secs / steps, 4), "unit": "s per Newton step (timestep_newton)", "cores": 1,
+            "kind": "reference" if which == "reference" else "port",
+            "sample": f"{steps} steady backward-Euler steps of timestep_newton on the full channel (one Newton "
+                      f"iteration each: 10 FP64 residuals for the lumped Jacobian + the block-diagonal solve) "
+                      f"after 1 warm-up step, 1 core, {secs:.1f} s"}
+
+
+def implicit_channel(args, with_cpu=True):
     """Implicit steady channel (96 x 48 x 48 stretched hexes, AUSM, second
-    order): wall time of the pseudo-transient Newton-Krylov solve to a 1e-8
-    relative FP64 residual, with FGMRES(30) unpreconditioned (the fastest
-    here), with block Jacobi, and optionally with the learned preconditioner
-    trained on pairs harvested from the block-Jacobi solve."""
+    order, Re=1000): wall time of the pseudo-transient Newton-Krylov solve to
+    a 1e-8 relative FP64 residual through the C ABI, with each
+    preconditioner: the cell-coupling one (the fastest), none (FGMRES(30),
+    3 restarts), block Jacobi (FGMRES(30), the configuration as written),
+    and optionally the learned one.  Also the reference's own implicit step
+    (timestep_newton) on the GPU and on the host cores."""
     from fv3d_gb300 import api, cases
     c = cases.channel()
-    keys = ("converged", "newton_steps", "gmres_iterations", "jv_evaluations", "rel_res", "wall_ms",
-            "fallbacks")
     runs = {}
+    plans = [("coupled", dict(inner_dim=10, inner_sweeps=6, sync_every=3, max_newton=args.max_newton)),
+             ("none", dict(max_restarts=3, max_newton=args.max_newton)),
+             ("block_jacobi", dict(max_newton=min(args.max_newton, 100)))]
     with api.Solver(c.mesh, c.params, c.region_type, c.region_prim, "fp64", "morton") as s:
-        plans = [("none", dict(max_restarts=3)), ("block_jacobi", {})]
         for pc, kw in plans:
             s.set_state(c.u0)
-            st = s.solve_implicit(preconditioner=pc, max_newton=args.max_newton, check=False, **kw)
-            runs[pc] = {k: st[k] for k in keys}
+            st = s.solve_implicit(preconditioner=pc, check=False, **kw)
+            runs[pc] = {k: st[k] for k in CHANNEL_KEYS}
+            runs[pc]["settings"] = kw
+        # end to end through the C ABI: the initial state from pinned host
+        # rows, the solve, the converged state back into them
+        try:
+            import torch
+            hb = torch.empty((c.mesh.n_cells, 5), dtype=torch.float64, pin_memory=True).numpy()
+        except Exception:
+            hb = np.empty((c.mesh.n_cells, 5))
+        hb[:] = c.u0
+        t0 = time.perf_counter()
+        s.set_state(hb)
+        s.solve_implicit(preconditioner="coupled", check=False, **plans[0][1])
+        s.get_conserved(out=hb)
+        e2e_s = time.perf_counter() - t0
+        # the reference's own implicit step (lumped blocks) on the GPU, per step
+        s.set_state(c.u0)
+        dt = s.timestep(1.0)
+        s.step_newton(0, 0.0, dt, "euler", max_iter_inner=2, is_transient=False, check=False)
+        t1 = time.perf_counter()
+        for k in range(5):
+            s.step_newton(k + 1, 0.0, dt, "euler", max_iter_inner=2, is_transient=False, check=False)
+        gpu_step = (time.perf_counter() - t1) / 5
         if args.learned:
             # training pairs from plain Newton-Krylov steps (a separate,
             # untimed solve harvesting 100,000 cells per Newton step, up to
@@ -248,17 +308,34 @@ def run_channel(args):
             tr["harvest_newton_steps"] = hv["newton_steps"]
             s.set_state(c.u0)
             st = s.solve_implicit(preconditioner="learned", max_newton=args.max_newton, check=False)
-            runs["learned"] = {k: st[k] for k in keys}
+            runs["learned"] = {k: st[k] for k in CHANNEL_KEYS}
             runs["learned"]["train"] = tr
-    best = runs["none"]
-    line = {"metric": "seconds to 1e-8 relative steady residual", "value": round(best["wall_ms"] / 1e3, 3),
-            "unit": "s", "n_gpus": 1, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64 (Jv f32)", "data": "synthetic",
-            "config": {"workload": f"channel 96x48x48: {c.mesh.n_cells} cells, {c.mesh.n_faces} faces, AUSM, "
-                                   "Green-Gauss linear, no limiter, Re=1000, pseudo-transient Newton, "
-                                   "SER CFL 100 -> 1e4, FGMRES(30), FD Jv in FP32",
-                       "preconditioner": "none (3 restarts)"},
-            "runs": runs}
+    conv = {k: v for k, v in runs.items() if v["converged"]}
+    best = min(conv, key=lambda k: conv[k]["wall_ms"]) if conv else "coupled"
+    out = {"metric": "seconds to 1e-8 relative steady residual", "value": round(runs[best]["wall_ms"] / 1e3, 4),
+           "unit": "s", "higher_is_better": False, "preconditioner": best,
+           "workload": f"channel 96x48x48: {c.mesh.n_cells} cells, {c.mesh.n_faces} faces, AUSM, Green-Gauss "
+                       "linear, no limiter, Re=1000, adiabatic walls, inflow, pressure outlet, periodic z; "
+                       "pseudo-transient Newton, SER CFL 100 -> 1e4, FGMRES(30) to eta 0.01, FD Jv in FP32, "
+                       "FP64 residual and update",
+           "e2e": {"value": round(e2e_s, 4), "unit": "s",
+                   "h2d_bytes_per_step": int(hb.nbytes), "d2h_bytes_per_step": int(hb.nbytes),
+                   "note": "wall clock around fv3d_set_state (pinned host rows) + fv3d_solve_implicit "
+                           "(coupled) + fv3d_get_conserved (pinned host rows); one 'step' = one solve"},
+           "reference_step_on_gpu_s": round(gpu_step, 5),
+           "runs": runs}
+    if with_cpu:
+        out["cpu_baseline"] = implicit_cpu_baseline(c)
+    return out
+
+
+def run_channel(args):
+    """The implicit channel alone, as its own JSON line."""
+    imp = implicit_channel(args, with_cpu=not args.no_cpu_baseline)
+    line = {"metric": imp["metric"], "value": imp["value"], "unit": "s", "n_gpus": 1, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64 (Jv f32)", "data": "synthetic",
+            "config": {"workload": imp["workload"], "preconditioner": imp["preconditioner"]},
+            "implicit": imp}
     print(json.dumps(line))
 
 
@@ -366,18 +443,40 @@ def main():
            "note": "wall clock around fv3d_step_explicit_io: pinned host state in (H2D), 1 graph step, "
                    "host state out (D2H), every step"}
     s.close()
+    # error of the mixed path against the FP64 GPU path over the first
+    # fp64_check_steps steps of the same run (from the initial state)
+    err64 = None
+    if args.precision == "mixed" and args.fp64_check_steps > 0:
+        outs = {}
+        for prec in ("mixed", "fp64"):
+            with api.Solver(case.mesh, case.params, case.region_type, case.region_prim, prec, "morton",
+                            device=local) as s2:
+                s2.set_state(case.u0)
+                s2.step_explicit(scheme, args.fp64_check_steps, cfl=0.5)
+                outs[prec] = s2.get_conserved()
+        d = np.linalg.norm(outs["mixed"] - outs["fp64"], axis=0)
+        ref = np.linalg.norm(outs["fp64"], axis=0)
+        err64 = {"steps": args.fp64_check_steps,
+                 "rel_l2": [float(x) for x in d / np.maximum(ref, ref[0])],
+                 "note": "mixed FP32/FP64 against the FP64 GPU path (itself within 1e-15 of the reference's "
+                         "own CPU solution after 500 steps, tests/test_gpu_fullrun.py), relative L2 per "
+                         "conserved variable"}
     if rank != 0:
         return
     cb = None
     if not args.no_cpu_baseline and world == 1:
         cb = cpu_baseline(args, 1)
+    imp = None
+    if world == 1 and not args.no_implicit:
+        imp = implicit_channel(args, with_cpu=not args.no_cpu_baseline)
     line = {"metric": "Mcell-updates/s per RK stage", "value": round(value, 2),
             "unit": "Mcell-updates/s per RK stage", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms / args.steps, 5),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32+f64" if args.precision == "mixed" else "f64", "data": "synthetic",
             "config": workload_config(args, case), "roofline": roofline, "cpu_baseline": cb,
-            "e2e": e2e, "gpu_launches": args.steps * ((2 if args.precision == "mixed" else 3) * nst + 1), "clocks": clk.summary()}
+            "e2e": e2e, "gpu_launches": args.steps * ((2 if args.precision == "mixed" else 3) * nst + 1),
+            "clocks": clk.summary(), "error_vs_fp64": err64, "implicit": imp}
     print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

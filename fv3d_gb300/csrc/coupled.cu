@@ -22,16 +22,19 @@
 // flexible GMRES, so the inner solve may differ from one application to the
 // next without changing the answer.
 //
-// Storage: FP32 blocks, row-major within a block, element-major over cells
-// ([e][nc]: a warp's loads of element e are contiguous); P_A's slot blocks
-// [slot][e][nc].  P_R's slot blocks are a A(U_o) + b I, applied without being
-// stored (per slot the normal and a, b; per cell (u, v, w, H)).  Built per
-// Newton step in FP64: P_A's blocks by forward finite differences of each
-// face flux (h = 1e-7 max(|U_v|, 1e-3)), P_R's analytically.  Every product and sweep is a cell gather: no atomics, no
-// face buffers.  The inner Krylov basis, its Gram-Schmidt passes and the
-// sweeps run in FP32; the inner least-squares problem in FP64 on the device,
-// so an application needs no host synchronisation and is captured in the
-// outer Arnoldi step's CUDA graph.
+// Both operators are applied matrix-free.  P_A x is the exact derivative of
+// each face's first-order flux along (x_c, x_o), evaluated in FP32 by
+// hand-written forward-mode arithmetic from per-cell FP32 state records and
+// per-slot (normal, s A / V); at a boundary face the ghost's tangent is
+// G x_c, G = d ghost / d U_c by forward differences of update_boundaries in
+// FP64.  P_R's slot blocks are a A(U_o) + b I (per slot the normal and a, b;
+// per cell (u, v, w, H)); its diagonal blocks are built in FP64, inverted and
+// stored FP32, row-major within a block, element-major over cells ([e][nc]: a
+// warp's loads of element e are contiguous).  Every product and sweep is a
+// cell gather: no atomics, no face buffers.  The inner Krylov basis, its
+// Gram-Schmidt passes, the sweeps and the inner least-squares problem run in
+// FP32 on the device, so an application needs no host synchronisation and is
+// captured in the outer Arnoldi step's CUDA graph.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -47,9 +50,9 @@ namespace {
 inline int nblk(size_t n, int t = 256) { return (int)((n + t - 1) / t); }
 constexpr int kHcol = 72;  // per inner column: h [0, 32), h' [32, 64), |w| and 1/|w| at 64, 65
 
-// neighbour of each face slot: the other cell, -1 for a boundary face or an
-// unused slot
-__global__ void k_cpl_nbr(int nc, int mcf, const int* __restrict__ cface, const int* __restrict__ fc0,
+// neighbour of each face slot: the other cell (>= 0), -2 - b for boundary
+// face b (nf_int + b), -1 for an unused slot
+__global__ void k_cpl_nbr(int nc, int mcf, int nf_int, const int* __restrict__ cface, const int* __restrict__ fc0,
                           const int* __restrict__ fc1, int* __restrict__ nbr) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
@@ -58,8 +61,7 @@ __global__ void k_cpl_nbr(int nc, int mcf, const int* __restrict__ cface, const 
     int o = -1;
     if (e >= 0) {
       const int f = e >> 1;
-      o = (e & 1) ? fc0[f] : fc1[f];
-      if (o >= nc) o = -1;  // ghost index of a boundary face
+      o = (f >= nf_int) ? -2 - (f - nf_int) : ((e & 1) ? fc0[f] : fc1[f]);
     }
     nbr[(size_t)k * nc + c] = o;
   }
@@ -95,11 +97,6 @@ __device__ __forceinline__ void store_block(float* __restrict__ dst, size_t nc, 
   for (int e = 0; e < 25; ++e) dst[(size_t)e * nc] = (float)B[e];
 }
 
-__device__ __forceinline__ void zero_block(float* __restrict__ dst, size_t nc) {
-#pragma unroll
-  for (int e = 0; e < 25; ++e) dst[(size_t)e * nc] = 0.f;
-}
-
 // the face's geometry for the first-order fluxes: n (cell 0 -> cell 1) and,
 // in n[3], the distance |d1| + |d2| (interior) or 2 |d1| (boundary)
 __device__ __forceinline__ void face_normal(const double* g, bool bnd, double* n) {
@@ -109,15 +106,25 @@ __device__ __forceinline__ void face_normal(const double* g, bool bnd, double* n
   n[3] = bnd ? 2.0 * d1 : d1 + d2;
 }
 
-// P_A: diagonal block of cell c and one block per face slot, from forward
-// differences of each face's first-order flux (with the case's flux scheme,
-// inviscid unless visc) in each of the ten states it depends on; at a
-// boundary face the ghost is re-derived from the perturbed cell state
-// (update_boundaries, boundary.c:188-320).  Each face is differentiated by
-// both of its cells (no face buffer).
+// FP32 state record of a conserved FP64 state: rho, m, E, p, 1/c, 1/rho
+// (reciprocals, so that the product's derivatives divide nowhere)
+__device__ __forceinline__ void put_state(float* __restrict__ rec, const double* q, double kappa, double km1) {
+  const double ir = 1.0 / q[0];
+  const double p = fmax(1.00E-10, km1 * (q[4] - 0.5 * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]) * ir));
+  float4* d = reinterpret_cast<float4*>(rec);
+  d[0] = make_float4((float)q[0], (float)q[1], (float)q[2], (float)q[3]);
+  d[1] = make_float4((float)q[4], (float)p, (float)(1.0 / sqrt(kappa * p * ir)), (float)ir);
+}
+
+// What P_A's matrix-free product reads, per Newton step: each cell's FP32
+// state record and 1/dt, each slot's (normal, s A / V), and at each boundary
+// face the ghost's record and d ghost / d U_cell (forward differences of
+// update_boundaries, boundary.c:188-320, in FP64)
 template <int MCF>
-__global__ void __launch_bounds__(128) k_cpl_build_pa(KArgs<double> a, const double* __restrict__ dtl,
-                                                      float* __restrict__ PAd, float* __restrict__ PAo, int visc) {
+__global__ void __launch_bounds__(128) k_cpl_build_state(KArgs<double> a, const double* __restrict__ dtl,
+                                                         float* __restrict__ cst, float* __restrict__ idt,
+                                                         float4* __restrict__ pna, float* __restrict__ gst,
+                                                         float* __restrict__ gjac) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.nc) return;
   const size_t nc = a.nc;
@@ -126,73 +133,162 @@ __global__ void __launch_bounds__(128) k_cpl_build_pa(KArgs<double> a, const dou
   double qc[10];
 #pragma unroll
   for (int j = 0; j < 5; ++j) qc[j] = a.U[(size_t)j * nc + c];
+  put_state(cst + 8 * (size_t)c, qc, a.pc.kappa, a.pc.km1);
   cons_to_prims(qc, ph);
+  idt[c] = (float)(1.0 / dtl[c]);
   const double iv = 1.0 / a.vol[c];
-  double D[25];
-#pragma unroll
-  for (int e = 0; e < 25; ++e) D[e] = 0.0;
-  const double idt = 1.0 / dtl[c];
-#pragma unroll
-  for (int j = 0; j < 5; ++j) D[j * 5 + j] = idt;
   for (int k = 0; k < MCF; ++k) {
-    float* Ok = PAo + (size_t)k * 25 * nc + c;
+    const size_t sk = (size_t)k * nc + c;
     const int e = a.cface[(size_t)c * MCF + k];
-    if (e < 0) { zero_block(Ok, nc); continue; }
+    if (e < 0) { pna[sk] = make_float4(0.f, 0.f, 0.f, 0.f); continue; }
     const int f = e >> 1, side = e & 1;
     const double* g = a.geo + (size_t)f * GEO;
-    const bool bnd = f >= a.nf_int;
-    double n[4];
-    face_normal(g, bnd, n);
-    const double w = (side ? -1.0 : 1.0) * g[G_A] * iv;  // -dR_c/dF_f
-    const int region = bnd ? a.fregion[f - a.nf_int] : 0;
-    double qo[10];
-    if (bnd) {
-      ghost_state(qc, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qo);
-    } else {
-      const int o = side ? a.fc0[f] : a.fc1[f];
-#pragma unroll
-      for (int j = 0; j < 5; ++j) qo[j] = a.U[(size_t)j * nc + o];
-    }
-    double F0[5];
-    if (side) fo_flux(qo, qc, n, a.pc, F0, visc != 0);
-    else fo_flux(qc, qo, n, a.pc, F0, visc != 0);
-    // the cell's own state
+    // the sign of s A / V carries the side (A / V > 0)
+    pna[sk] = make_float4((float)g[G_N], (float)g[G_N + 1], (float)g[G_N + 2],
+                          (float)((side ? -1.0 : 1.0) * g[G_A] * iv));
+    if (f < a.nf_int) continue;
+    const int b = f - a.nf_int, region = a.fregion[b];
+    double qg[10];
+    ghost_state(qc, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qg);
+    put_state(gst + 8 * (size_t)b, qg, a.pc.kappa, a.pc.km1);
     for (int v = 0; v < 5; ++v) {
       const double h = 1e-7 * fmax(fabs(qc[v]), 1e-3);
-      double qp[10], F[5];
+      double qp[10], qh[10];
 #pragma unroll
       for (int j = 0; j < 5; ++j) qp[j] = qc[j];
       qp[v] += h;
-      if (bnd) {
-        double qg[10];
-        cons_to_prims(qp, ph);
-        ghost_state(qp, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qg);
-        fo_flux(qp, qg, n, a.pc, F, visc != 0);
-      } else if (side) {
-        fo_flux(qo, qp, n, a.pc, F, visc != 0);
-      } else {
-        fo_flux(qp, qo, n, a.pc, F, visc != 0);
-      }
-      const double s = w / h;
+      cons_to_prims(qp, ph);
+      ghost_state(qp, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qh);
 #pragma unroll
-      for (int i = 0; i < 5; ++i) D[i * 5 + v] += (F[i] - F0[i]) * s;
-    }
-    if (bnd) { zero_block(Ok, nc); continue; }
-    // the neighbour's state
-    for (int v = 0; v < 5; ++v) {
-      const double h = 1e-7 * fmax(fabs(qo[v]), 1e-3);
-      double qp[5], F[5];
-#pragma unroll
-      for (int j = 0; j < 5; ++j) qp[j] = qo[j];
-      qp[v] += h;
-      if (side) fo_flux(qp, qc, n, a.pc, F, visc != 0);
-      else fo_flux(qc, qp, n, a.pc, F, visc != 0);
-      const double s = w / h;
-#pragma unroll
-      for (int i = 0; i < 5; ++i) Ok[(size_t)(i * 5 + v) * nc] = (float)((F[i] - F0[i]) * s);
+      for (int i = 0; i < 5; ++i) gjac[25 * (size_t)b + i * 5 + v] = (float)((qh[i] - qg[i]) / h);
     }
   }
-  store_block(PAd + c, nc, D);
+}
+
+// ---- forward-mode derivative of the first-order inviscid face flux ---------
+// A side's state (from its record) and the derivative of its primitives
+// along a tangent x of its conserved state.
+struct SideTan {
+  float rho, u[3], E, p, c, ic, ir, un, H;
+  float dun, dp, dc, dH, du[3];
+};
+
+__device__ __forceinline__ void side_tangent(const float4 r0, const float4 r1, const float* x, const float4 n,
+                                             float gam, float gm1, SideTan& s) {
+  s.rho = r0.x; s.E = r1.x; s.p = r1.y; s.ic = r1.z; s.ir = r1.w;
+  s.c = gam * s.p * s.ir * s.ic;  // c^2 / c
+  s.u[0] = r0.y * s.ir; s.u[1] = r0.z * s.ir; s.u[2] = r0.w * s.ir;
+  s.un = s.u[0] * n.x + s.u[1] * n.y + s.u[2] * n.z;
+  s.H = (s.E + s.p) * s.ir;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) s.du[i] = (x[1 + i] - s.u[i] * x[0]) * s.ir;
+  s.dun = s.du[0] * n.x + s.du[1] * n.y + s.du[2] * n.z;
+  const float q2 = s.u[0] * s.u[0] + s.u[1] * s.u[1] + s.u[2] * s.u[2];
+  const float um = s.u[0] * x[1] + s.u[1] * x[2] + s.u[2] * x[3];
+  s.dp = (s.p > 1.00E-10f) ? gm1 * (x[4] - um + 0.5f * q2 * x[0]) : 0.f;
+  s.dc = 0.5f * gam * s.ir * s.ic * (s.dp - s.p * s.ir * x[0]);
+  s.dH = (x[4] + s.dp - s.H * x[0]) * s.ir;
+}
+
+// dF = (dF/dU_L) dl + (dF/dU_R) dr for the first-order flux F(U_L, U_R; n)
+// of fo_flux (Rusanov: flux.c:320-336, AUSM: flux.c:344-406), the branch of
+// each max / min and of the Mach-number splitting taken at the state (at a
+// tie the one a forward difference along the tangent would see)
+__device__ void flux_jvp(const float4 l0, const float4 l1, const float4 r0, const float4 r1, const float* dl,
+                         const float* dr, const float4 n, int rusanov, float gam, float gm1, float* dF) {
+  SideTan L, R;
+  side_tangent(l0, l1, dl, n, gam, gm1, L);
+  side_tangent(r0, r1, dr, n, gam, gm1, R);
+  const float nn[3] = {n.x, n.y, n.z};
+  if (rusanov) {
+    const float aL = fabsf(L.un) + L.c, aR = fabsf(R.un) + R.c;
+    const float sL = (L.un >= 0.f) ? 1.f : -1.f, sR = (R.un >= 0.f) ? 1.f : -1.f;
+    const float daL = sL * L.dun + L.dc, daR = sR * R.dun + R.dc;
+    const bool left = (aL > aR) || (aL == aR && daL >= daR);
+    const float lam = left ? aL : aR, dlam = left ? daL : daR;
+    const float uL[5] = {l0.x, l0.y, l0.z, l0.w, l1.x}, uR[5] = {r0.x, r0.y, r0.z, r0.w, r1.x};
+    float dfL[5], dfR[5];
+    dfL[0] = dl[0] * L.un + L.rho * L.dun;
+    dfR[0] = dr[0] * R.un + R.rho * R.dun;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      dfL[1 + i] = dl[1 + i] * L.un + uL[1 + i] * L.dun + L.dp * nn[i];
+      dfR[1 + i] = dr[1 + i] * R.un + uR[1 + i] * R.dun + R.dp * nn[i];
+    }
+    dfL[4] = (dl[4] + L.dp) * L.un + (L.E + L.p) * L.dun;
+    dfR[4] = (dr[4] + R.dp) * R.un + (R.E + R.p) * R.dun;
+#pragma unroll
+    for (int j = 0; j < 5; ++j)
+      dF[j] = 0.5f * (dfL[j] + dfR[j]) - 0.5f * dlam * (uR[j] - uL[j]) - 0.5f * lam * (dr[j] - dl[j]);
+    return;
+  }
+  const float ML = L.un * L.ic, MR = R.un * R.ic;
+  const float dML = (L.dun - ML * L.dc) * L.ic, dMR = (R.dun - MR * R.dc) * R.ic;
+  // split Mach numbers and pressures (their values enter only through the
+  // mass flux: the pressure flux is linear in them)
+  float mp, dmp, dpp, mm, dmm, dpm;
+  if (ML <= -1.f) { mp = dmp = dpp = 0.f; }
+  else if (ML < 1.f) {
+    mp = 0.25f * (ML + 1.f) * (ML + 1.f);
+    dmp = 0.5f * (ML + 1.f) * dML;
+    dpp = 0.25f * (L.dp * (1.f + ML) * (1.f + ML) * (2.f - ML) + 3.f * L.p * (1.f - ML * ML) * dML);
+  } else { mp = ML; dmp = dML; dpp = L.dp; }
+  if (MR <= -1.f) { mm = MR; dmm = dMR; dpm = R.dp; }
+  else if (MR < 1.f) {
+    mm = -0.25f * (MR - 1.f) * (MR - 1.f);
+    dmm = -0.5f * (MR - 1.f) * dMR;
+    dpm = 0.25f * (R.dp * (1.f - MR) * (1.f - MR) * (2.f + MR) - 3.f * R.p * (1.f - MR * MR) * dMR);
+  } else { mm = dmm = dpm = 0.f; }
+  const float sm = mp + mm, ds = dmp + dmm;
+  float mdl = 0.f, dmdl = 0.f, mdr = 0.f, dmdr = 0.f;
+  if (sm > 0.f || (sm == 0.f && ds > 0.f)) {
+    mdl = sm * L.c * L.rho;
+    dmdl = ds * L.c * L.rho + sm * (L.dc * L.rho + L.c * dl[0]);
+  } else {
+    mdr = sm * R.c * R.rho;
+    dmdr = ds * R.c * R.rho + sm * (R.dc * R.rho + R.c * dr[0]);
+  }
+  const float dP = dpp + dpm;
+  dF[0] = dmdl + dmdr;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) dF[1 + i] = dmdl * L.u[i] + mdl * L.du[i] + dmdr * R.u[i] + mdr * R.du[i] + dP * nn[i];
+  dF[4] = dmdl * L.H + mdl * L.dH + dmdr * R.H + mdr * R.dH;
+}
+
+__device__ __forceinline__ void ld_state(const float* __restrict__ rec, float4& r0, float4& r1) {
+  r0 = __ldg(reinterpret_cast<const float4*>(rec));
+  r1 = __ldg(reinterpret_cast<const float4*>(rec) + 1);
+}
+
+// one slot's contribution s A / V dF to (P_A x)_c: xo is the neighbour's x
+// (interior) or unused (boundary: the ghost's tangent is G x_c)
+__device__ __forceinline__ void slot_jvp(const float4 c0, const float4 c1, const float* xc, int o,
+                                         const float* __restrict__ cst, const float* __restrict__ gst,
+                                         const float* __restrict__ gjac, const float* xo, const float4 na,
+                                         int rusanov, float gam, float gm1, float* acc) {
+  float dF[5];
+  if (o >= 0) {
+    float4 o0, o1;
+    ld_state(cst + 8 * (size_t)o, o0, o1);
+    if (na.w >= 0.f) flux_jvp(c0, c1, o0, o1, xc, xo, na, rusanov, gam, gm1, dF);
+    else flux_jvp(o0, o1, c0, c1, xo, xc, na, rusanov, gam, gm1, dF);
+  } else {
+    const int b = -2 - o;
+    float4 g0, g1;
+    ld_state(gst + 8 * (size_t)b, g0, g1);
+    float xg[5];
+    const float* G = gjac + 25 * (size_t)b;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      float t = 0.f;
+#pragma unroll
+      for (int j = 0; j < 5; ++j) t = fmaf(__ldg(G + i * 5 + j), xc[j], t);
+      xg[i] = t;
+    }
+    flux_jvp(c0, c1, g0, g1, xc, xg, na, rusanov, gam, gm1, dF);
+  }
+#pragma unroll
+  for (int j = 0; j < 5; ++j) acc[j] = fmaf(na.w, dF[j], acc[j]);
 }
 
 // 5x5 inverse (row-major, FP64 Gauss-Jordan with partial pivoting); false
@@ -384,27 +480,66 @@ __device__ __forceinline__ void block_mul_add(const float* __restrict__ B, size_
   }
 }
 
-// y = P x: the diagonal block times x_c plus each slot block times the
-// neighbour's x
+// y = P_A x = x / dt - dR1/dU x, matrix-free: per slot the exact
+// derivative of the face's first-order flux along (x_c, x_o) in FP32
 template <int MCF>
-__global__ void __launch_bounds__(256) k_cpl_product(int nc, const float* __restrict__ Dg,
-                                                     const float* __restrict__ O, const int* __restrict__ nbr,
-                                                     const float* __restrict__ x, float* __restrict__ y) {
+__global__ void __launch_bounds__(256) k_cpl_product(int nc, const float* __restrict__ cst,
+                                                     const float* __restrict__ idt, const float4* __restrict__ pna,
+                                                     const int* __restrict__ nbr, const float* __restrict__ gst,
+                                                     const float* __restrict__ gjac, int rusanov, float gam,
+                                                     float gm1, const float* __restrict__ x, float* __restrict__ y) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
-  float xc[5], acc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  float xc[5], acc[5];
   ld5(x, nc, c, xc);
-  block_mul_add(Dg + c, nc, xc, acc);
+  const float id = __ldg(idt + c);
+#pragma unroll
+  for (int j = 0; j < 5; ++j) acc[j] = id * xc[j];
+  float4 c0, c1;
+  ld_state(cst + 8 * (size_t)c, c0, c1);
 #pragma unroll
   for (int k = 0; k < MCF; ++k) {
-    const int o = __ldg(nbr + (size_t)k * nc + c);
-    if (o < 0) continue;
-    float xo[5];
-    ld5(x, nc, o, xo);
-    block_mul_add(O + (size_t)k * 25 * nc + c, nc, xo, acc);
+    const size_t sk = (size_t)k * nc + c;
+    const int o = __ldg(nbr + sk);
+    if (o == -1) continue;
+    float xo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    if (o >= 0) ld5(x, nc, o, xo);
+    slot_jvp(c0, c1, xc, o, cst, gst, gjac, xo, __ldg(pna + sk), rusanov, gam, gm1, acc);
   }
 #pragma unroll
   for (int j = 0; j < 5; ++j) y[(size_t)j * nc + c] = acc[j];
+}
+
+// P_A written out as blocks (for the block export), by the product's own
+// arithmetic: column j of the diagonal block is the response to x_c = e_j,
+// of slot k's block the response of that slot to x_o = e_j
+template <int MCF>
+__global__ void k_cpl_expand_pa(int nc, const float* __restrict__ cst, const float* __restrict__ idt,
+                                const float4* __restrict__ pna, const int* __restrict__ nbr,
+                                const float* __restrict__ gst, const float* __restrict__ gjac, int rusanov, float gam,
+                                float gm1, float* __restrict__ Dg, float* __restrict__ O) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  float4 c0, c1;
+  ld_state(cst + 8 * (size_t)c, c0, c1);
+  for (int j = 0; j < 5; ++j) {
+    float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, zero[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    e[j] = 1.f;
+    float d[5];
+    for (int i = 0; i < 5; ++i) d[i] = idt[c] * e[i];
+    for (int k = 0; k < MCF; ++k) {
+      const size_t sk = (size_t)k * nc + c;
+      const int o = nbr[sk];
+      float* Ok = O + (size_t)k * 25 * nc + c;
+      float col[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+      if (o != -1) {
+        slot_jvp(c0, c1, e, o, cst, gst, gjac, zero, pna[sk], rusanov, gam, gm1, d);
+        if (o >= 0) slot_jvp(c0, c1, zero, o, cst, gst, gjac, e, pna[sk], rusanov, gam, gm1, col);
+      }
+      for (int i = 0; i < 5; ++i) Ok[(size_t)(i * 5 + j) * nc] = col[i];
+    }
+    for (int i = 0; i < 5; ++i) Dg[(size_t)(i * 5 + j) * nc + c] = d[i];
+  }
 }
 
 // one block-Jacobi sweep of P_R, y = Dinv (b - O x) (x null: y = Dinv b),
@@ -448,45 +583,49 @@ __global__ void k_cpl_start(size_t n, const T* __restrict__ v, const double* __r
 }
 
 // the inner least-squares problem min |beta e_1 - H y| by Givens rotations
-// (FP64, one thread): H from the Gram-Schmidt passes' columns, y [m] into
-// hin + m * kHcol + 8; the columns past a breakdown (a zero subdiagonal or a
-// zero or non-finite rotation) get y = 0
+// (FP32, one thread, H in shared memory): H from the Gram-Schmidt passes'
+// columns, y [m] into hin + m * kHcol + 8; the columns past a breakdown (a
+// zero subdiagonal or a zero or non-finite rotation) get y = 0
 __global__ void k_cpl_lsq(int m, double* __restrict__ hin) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double H[30][31];
-  double cs[30], sn[30], g[31], y[30];
-  const double beta = hin[(size_t)m * kHcol];  // |v| from the norm pass
-  for (int i = 0; i <= m; ++i) g[i] = 0.0;
-  g[0] = beta;
+  __shared__ float H[30][31];
+  __shared__ float cs[30], sn[30], g[31], y[30];
+  const int t = threadIdx.x;
+  // the columns, loaded by the block
+  for (int q = t; q < m * 31; q += blockDim.x) {
+    const int j = q / 31, i = q % 31;
+    const double* hc = hin + (size_t)j * kHcol;
+    H[j][i] = (i <= j) ? (float)(hc[i] + hc[32 + i]) : (i == j + 1 ? (float)hc[64] : 0.f);
+  }
+  __syncthreads();
+  if (t != 0) return;
+  for (int i = 0; i <= m; ++i) g[i] = 0.f;
+  g[0] = (float)hin[(size_t)m * kHcol];  // |v| from the norm pass
   int kk = 0;
   for (int j = 0; j < m; ++j) {
-    const double* hc = hin + (size_t)j * kHcol;
-    for (int i = 0; i <= j; ++i) H[j][i] = hc[i] + hc[32 + i];
-    const double hn = hc[64];
-    H[j][j + 1] = hn;
+    const float hn = H[j][j + 1];
     for (int i = 0; i < j; ++i) {
-      const double a0 = H[j][i], b0 = H[j][i + 1];
+      const float a0 = H[j][i], b0 = H[j][i + 1];
       H[j][i] = cs[i] * a0 + sn[i] * b0;
       H[j][i + 1] = -sn[i] * a0 + cs[i] * b0;
     }
-    const double a0 = H[j][j], b0 = H[j][j + 1];
-    const double r = sqrt(a0 * a0 + b0 * b0);
-    if (!(r > 0.0) || !isfinite(r)) break;
+    const float a0 = H[j][j], b0 = H[j][j + 1];
+    const float r = sqrtf(a0 * a0 + b0 * b0);
+    if (!(r > 0.f) || !isfinite(r)) break;
     cs[j] = a0 / r;
     sn[j] = b0 / r;
     H[j][j] = r;
     g[j + 1] = -sn[j] * g[j];
     g[j] = cs[j] * g[j];
     kk = j + 1;
-    if (!(hn > 0.0)) break;  // the Krylov space is invariant: exact solution
+    if (!(hn > 0.f)) break;  // the Krylov space is invariant: exact solution
   }
   for (int i = kk - 1; i >= 0; --i) {
-    double s = g[i];
+    float s = g[i];
     for (int j = i + 1; j < kk; ++j) s -= H[j][i] * y[j];
     y[i] = s / H[i][i];
   }
   double* out = hin + (size_t)m * kHcol + 8;
-  for (int i = 0; i < m; ++i) out[i] = (i < kk) ? y[i] : 0.0;
+  for (int i = 0; i < m; ++i) out[i] = (i < kk) ? (double)y[i] : 0.0;
 }
 
 // u = sum_j y_j V_j (FP32 basis, ldb apart)
@@ -515,7 +654,7 @@ fv3d_status Coupled::setup(Ctx& ctx, Implicit& im, int m_inner, int n_sweeps) {
   if (m_inner != m_in || n_sweeps != sweep_count) im.release_graphs();
   m_in = m_inner;
   sweep_count = n_sweeps;
-  if (nc == ctx.nc && mcf == ctx.mcf && ldb == im.ldb && m_cap >= m_inner) return FV3D_OK;
+  if (nc == ctx.nc && mcf == ctx.mcf && nb == ctx.nb && ldb == im.ldb && m_cap >= m_inner) return FV3D_OK;
   im.release_graphs();
   nc = ctx.nc;
   mcf = ctx.mcf;
@@ -523,9 +662,13 @@ fv3d_status Coupled::setup(Ctx& ctx, Implicit& im, int m_inner, int n_sweeps) {
   ldb = im.ldb;
   m_cap = m_inner;
   if (mcf != 4 && mcf != 6 && mcf != 8) return ctx.fail(FV3D_ERR_UNSUPPORTED, "coupled preconditioner: %d face slots", mcf);
+  nb = ctx.nb;
   cudaError_t e = nbr.alloc((size_t)mcf * nc);
-  if (e == cudaSuccess) e = PAd.alloc(25 * (size_t)nc);
-  if (e == cudaSuccess) e = PAo.alloc((size_t)mcf * 25 * nc);
+  if (e == cudaSuccess) e = cst.alloc(8 * (size_t)nc);
+  if (e == cudaSuccess) e = idt.alloc(nc);
+  if (e == cudaSuccess) e = pna.alloc((size_t)mcf * nc);
+  if (e == cudaSuccess) e = gst.alloc(8 * (size_t)nb);
+  if (e == cudaSuccess) e = gjac.alloc(25 * (size_t)nb);
   if (e == cudaSuccess) e = PRi.alloc(25 * (size_t)nc);
   if (e == cudaSuccess) e = rna.alloc((size_t)mcf * nc);
   if (e == cudaSuccess) e = rb.alloc((size_t)mcf * nc);
@@ -540,7 +683,7 @@ fv3d_status Coupled::setup(Ctx& ctx, Implicit& im, int m_inner, int n_sweeps) {
   CCK(cudaMemsetAsync(Vi.p, 0, sizeof(float) * Vi.n, ctx.stream));
   CCK(cudaMemsetAsync(hin.p, 0, sizeof(double) * hin.n, ctx.stream));
   KArgs<double> a = ctx.args<double>();
-  k_cpl_nbr<<<nblk(nc), 256, 0, ctx.stream>>>(nc, mcf, a.cface, a.fc0, a.fc1, nbr.p);
+  k_cpl_nbr<<<nblk(nc), 256, 0, ctx.stream>>>(nc, mcf, ctx.nf_int, a.cface, a.fc0, a.fc1, nbr.p);
   CCK(cudaGetLastError());
   return FV3D_OK;
 }
@@ -549,7 +692,7 @@ fv3d_status Coupled::build(Ctx& ctx, Implicit& im) {
   KArgs<double> a = ctx.args<double>();
   const int g = nblk(nc, 128);
 #define CPL_BUILD(M)                                                                           \
-  k_cpl_build_pa<M><<<g, 128, 0, ctx.stream>>>(a, im.dtl.p, PAd.p, PAo.p, 0);                 \
+  k_cpl_build_state<M><<<g, 128, 0, ctx.stream>>>(a, im.dtl.p, cst.p, idt.p, pna.p, gst.p, gjac.p); \
   k_cpl_build_pr<M><<<g, 128, 0, ctx.stream>>>(a, im.dtl.p, PRi.p, rna.p, rb.p, st4.p)
   if (mcf == 4) { CPL_BUILD(4); }
   else if (mcf == 6) { CPL_BUILD(6); }
@@ -585,6 +728,8 @@ fv3d_status Coupled::sweeps(Ctx& ctx, int count, const float* b, TO* out) {
 template <class T>
 fv3d_status Coupled::apply(Ctx& ctx, Implicit& im, const T* v, T* z) {
   const int m = m_in, sw = sweep_count;
+  const int rusanov = ctx.phys.flux == 1 ? 1 : 0;
+  const float gam = (float)ctx.phys.kappa, gm1 = (float)ctx.phys.km1;
   double* hb = hin.p + (size_t)m * kHcol;  // |v| and its inverse, then y at +8
   // |v| (FP64 for a FP64 input, FP32 otherwise) and V_0 = v / |v|
   fv3d_status st = im.gs_pass<T>(ctx, 0, const_cast<T*>(v), v, 1, nullptr, hb, 1.0, nullptr);
@@ -597,9 +742,13 @@ fv3d_status Coupled::apply(Ctx& ctx, Implicit& im, const T* v, T* z) {
     double* hc = hin.p + (size_t)j * kHcol;
     // t = M_R v_j (into ui), w = P_A t
     if ((st = sweeps<float>(ctx, sw, vj, ui.p)) != FV3D_OK) return st;
-    if (mcf == 4) k_cpl_product<4><<<g, 256, 0, ctx.stream>>>(nc, PAd.p, PAo.p, nbr.p, ui.p, wi.p);
-    else if (mcf == 6) k_cpl_product<6><<<g, 256, 0, ctx.stream>>>(nc, PAd.p, PAo.p, nbr.p, ui.p, wi.p);
-    else k_cpl_product<8><<<g, 256, 0, ctx.stream>>>(nc, PAd.p, PAo.p, nbr.p, ui.p, wi.p);
+#define CPL_PRODUCT(M)                                                                                      \
+  k_cpl_product<M><<<g, 256, 0, ctx.stream>>>(nc, cst.p, idt.p, pna.p, nbr.p, gst.p, gjac.p, rusanov, gam, gm1, \
+                                              ui.p, wi.p)
+    if (mcf == 4) CPL_PRODUCT(4);
+    else if (mcf == 6) CPL_PRODUCT(6);
+    else CPL_PRODUCT(8);
+#undef CPL_PRODUCT
     CCK(cudaGetLastError());
     // classical Gram-Schmidt twice, v_{j+1} = w / |w| (the outer solve's passes, FP32)
     if ((st = im.gs_pass<float>(ctx, 1, wi.p, Vi.p, j + 1, nullptr, hc, 0.0, nullptr)) != FV3D_OK) return st;
@@ -639,18 +788,26 @@ extern "C" fv3d_status fv3d_get_coupled_blocks(fv3d_ctx* handle, int which, doub
   const size_t nc = cp->nc, mcf = cp->mcf;
   std::vector<float> d(25 * nc), o(mcf * 25 * nc);
   std::vector<int> nb(mcf * nc);
-  const float* src_d = which ? cp->PRi.p : cp->PAd.p;
-  DevBuf<float> expanded;  // P_R's slot blocks, written out by the sweep's arithmetic
-  if (which) {
-    if (expanded.alloc(mcf * 25 * nc) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "allocation");
-    const int g = (int)((nc + 255) / 256);
-    const float gm1 = (float)ctx->phys.km1;
-    if (mcf == 4) k_cpl_expand_pr<4><<<g, 256, 0, ctx->stream>>>((int)nc, cp->nbr.p, cp->rna.p, cp->rb.p, cp->st4.p, gm1, expanded.p);
-    else if (mcf == 6) k_cpl_expand_pr<6><<<g, 256, 0, ctx->stream>>>((int)nc, cp->nbr.p, cp->rna.p, cp->rb.p, cp->st4.p, gm1, expanded.p);
-    else k_cpl_expand_pr<8><<<g, 256, 0, ctx->stream>>>((int)nc, cp->nbr.p, cp->rna.p, cp->rb.p, cp->st4.p, gm1, expanded.p);
-    if (cudaGetLastError() != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "expand P_R blocks");
-  }
-  const float* src_o = which ? expanded.p : cp->PAo.p;
+  // the slot blocks (and P_A's diagonal blocks) written out by the
+  // matrix-free operators' own arithmetic
+  DevBuf<float> ex_d, ex_o;
+  if (ex_o.alloc(mcf * 25 * nc) != cudaSuccess || (which == 0 && ex_d.alloc(25 * nc) != cudaSuccess))
+    return ctx->fail(FV3D_ERR_DEVICE, "allocation");
+  const int g = (int)((nc + 255) / 256);
+  const float gam = (float)ctx->phys.kappa, gm1 = (float)ctx->phys.km1;
+  const int rus = ctx->phys.flux == 1 ? 1 : 0;
+  const Coupled& q = *cp;
+#define CPL_EXPAND(M)                                                                                          \
+  if (which) k_cpl_expand_pr<M><<<g, 256, 0, ctx->stream>>>((int)nc, q.nbr.p, q.rna.p, q.rb.p, q.st4.p, gm1, ex_o.p); \
+  else k_cpl_expand_pa<M><<<g, 256, 0, ctx->stream>>>((int)nc, q.cst.p, q.idt.p, q.pna.p, q.nbr.p, q.gst.p, q.gjac.p, \
+                                                      rus, gam, gm1, ex_d.p, ex_o.p)
+  if (mcf == 4) { CPL_EXPAND(4); }
+  else if (mcf == 6) { CPL_EXPAND(6); }
+  else { CPL_EXPAND(8); }
+#undef CPL_EXPAND
+  if (cudaGetLastError() != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "expand blocks");
+  const float* src_d = which ? cp->PRi.p : ex_d.p;
+  const float* src_o = ex_o.p;
   if (cudaStreamSynchronize(ctx->stream) != cudaSuccess ||
       cudaMemcpy(d.data(), src_d, sizeof(float) * d.size(), cudaMemcpyDeviceToHost) != cudaSuccess ||
       cudaMemcpy(o.data(), src_o, sizeof(float) * o.size(), cudaMemcpyDeviceToHost) != cudaSuccess ||

@@ -40,8 +40,12 @@ struct Coupled {
   int nc = 0, mcf = 0, m_cap = 0;  // sizes the buffers are allocated for
   int m_in = 0, sweep_count = 0;   // inner GMRES iterations and sweeps of the current solve
   size_t n = 0, ldb = 0;
-  DevBuf<int> nbr;                 // [mcf][nc] neighbour of each face slot, -1 ghost or none
-  DevBuf<float> PAd, PAo;          // P_A: diagonal blocks [25][nc], slot blocks [mcf][25][nc]
+  DevBuf<int> nbr;                 // [mcf][nc] neighbour of each face slot, -2 - b boundary face b, -1 none
+  int nb = 0;
+  // P_A, matrix-free: FP32 state records [nc][8] (rho, m, E, p, 1/c, 1/rho), 1/dt [nc], per slot
+  // (normal, s A / V) [mcf][nc], per boundary face the ghost's record [nb][8] and d ghost / d U [nb][25]
+  DevBuf<float> cst, idt, gst, gjac;
+  DevBuf<float4> pna;
   DevBuf<float> PRi;               // P_R: inverted diagonal blocks [25][nc]; its slot blocks are applied
   DevBuf<float4> rna, st4;         // matrix-free: per slot (normal, a) [mcf][nc], per cell (u, v, w, H)
   DevBuf<float> rb;                // per slot b [mcf][nc]

@@ -246,11 +246,13 @@ fv3d_status fv3d_implicit_history(const fv3d_ctx *ctx, double *res, int max, int
 /* 5x5 blocks of the last preconditioner build, [n_cells][25] column-major,
  * reference cell order (lumped blocks: compare with calc_jacobian_numerical) */
 fv3d_status fv3d_get_blocks(fv3d_ctx *ctx, double *blocks);
-/* Blocks of the last FV3D_PC_COUPLED build (no reference counterpart: the
- * reference's preconditioner is its lumped diagonal, implicit.c:61-119), in
- * reference cell order, row-major 5x5: which 0 gives P_A = I/dt - dR1/dU
- * (diagonal blocks and one block per face slot), which 1 the Rusanov matrix
- * P_R (its inverted diagonal blocks and its slot blocks).  diag [n_cells*25],
+/* Blocks of the operators of the last FV3D_PC_COUPLED build (no reference
+ * counterpart: the reference's preconditioner is its lumped diagonal,
+ * implicit.c:61-119).  The solve applies them matrix-free; this call writes
+ * them out by the same arithmetic, in reference cell order, row-major 5x5:
+ * which 0 gives P_A = I/dt - dR1/dU (diagonal blocks and one block per face
+ * slot), which 1 the Rusanov matrix P_R (its inverted diagonal blocks and
+ * its slot blocks).  diag [n_cells*25],
  * slots [n_cells*max_slots*25], neighbour [n_cells*max_slots] (the slot's
  * other cell, -1 for a boundary face or an unused slot); *max_slots is set
  * first, and NULL arrays are skipped. */

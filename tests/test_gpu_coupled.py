@@ -1,11 +1,13 @@
 """The cell-coupling preconditioner of the implicit solve (FV3D_PC_COUPLED)
 against its CPU definition in oracle/coupling.py, through the C ABI.
 
-  * the blocks the GPU builds (P_A = I/dt - dR1/dU of the first-order
-    inviscid residual with the case's flux, by finite differences per face;
-    P_R the first-order Rusanov Jacobian, analytic, wave speed frozen) equal
-    the CPU's (coloured finite differences of the oracle's residual; the
-    analytic Rusanov assembly) to FP32 storage precision;
+  * the operators the GPU applies (P_A = I/dt - dR1/dU of the first-order
+    inviscid residual with the case's flux, matrix-free by the exact FP32
+    derivative of each face flux; P_R the first-order Rusanov Jacobian,
+    analytic, wave speed frozen, its slot blocks matrix-free), written out as
+    blocks by their own arithmetic, equal the CPU's (coloured finite
+    differences of the oracle's residual; the analytic Rusanov assembly) to
+    FP32 precision;
   * the nested solve (inner GMRES(10) on P_A right-preconditioned by two
     Rusanov block-Jacobi sweeps, FGMRES(30) outside, FP64 Jacobian-vector
     products) takes the CPU solve's Newton and Krylov counts on the 12x8x4
@@ -85,8 +87,10 @@ def test_coupled_blocks_match_the_cpu_definition():
     ed, eo = block_errors(PA, da, oa, nba)
     print("P_A blocks: diag median %.2e max %.2e, slots median %.2e max %.2e"
           % (np.median(ed), ed.max(), np.median(eo), eo.max()))
-    assert np.median(ed) < 1e-6 and ed.max() < 1e-4, (np.median(ed), ed.max())
-    assert np.median(eo) < 1e-6 and eo.max() < 1e-4, (np.median(eo), eo.max())
+    # FP32 forward-mode derivatives against FP64 forward differences: measured
+    # median 3e-7, largest 4e-6 (a block of small entries)
+    assert np.median(ed) < 1e-6 and ed.max() < 2e-5, (np.median(ed), ed.max())
+    assert np.median(eo) < 1e-6 and eo.max() < 2e-5, (np.median(eo), eo.max())
     PR = cp.coupling_matrix(c.mesh, U, c.params["kappa"], c.params["mu_mix"], dt, cp.ghost_derivative(o, c.mesh, U))
     ed, eo = block_errors(PR, dr, orr, nbr, inverse_diag=True)
     print("P_R blocks: inverse diag median %.2e max %.2e, slots median %.2e max %.2e"

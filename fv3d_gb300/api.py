@@ -67,7 +67,7 @@ class ImplicitOpts(C.Structure):
                 ("max_newton", C.c_int), ("krylov_dim", C.c_int), ("eta", C.c_double),
                 ("fd_eps", C.c_double), ("jv_precision", C.c_int), ("preconditioner", C.c_int),
                 ("pc_refresh", C.c_int), ("max_restarts", C.c_int), ("sync_every", C.c_int),
-                ("inner_dim", C.c_int), ("inner_sweeps", C.c_int)]
+                ("inner_dim", C.c_int), ("inner_sweeps", C.c_int), ("inner_omega", C.c_double)]
 
 
 class ImplicitStats(C.Structure):

@@ -937,7 +937,7 @@ fv3d_status Implicit::build_blocks(Ctx& ctx) {
   if (opts.preconditioner == FV3D_PC_NONE && !harvesting) return FV3D_OK;
   if (opts.preconditioner == FV3D_PC_COUPLED) {
     if (coupled == nullptr) coupled = new Coupled();
-    fv3d_status st = coupled->setup(ctx, *this, opts.inner_dim, opts.inner_sweeps);
+    fv3d_status st = coupled->setup(ctx, *this, opts.inner_dim, opts.inner_sweeps, (float)opts.inner_omega);
     if (st == FV3D_OK) st = coupled->build(ctx, *this);
     return st;
   }
@@ -1122,9 +1122,11 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
   if (opts.krylov_dim < 1 || opts.krylov_dim > 31) return ctx.fail(FV3D_ERR_INVALID_ARG, "krylov_dim must be 1..31");
   if (opts.preconditioner == FV3D_PC_COUPLED) {
     if (opts.inner_dim == 0) opts.inner_dim = 10;
-    if (opts.inner_sweeps == 0) opts.inner_sweeps = 2;
-    if (opts.inner_dim < 1 || opts.inner_dim > 30 || opts.inner_sweeps < 1 || opts.inner_sweeps > 8)
-      return ctx.fail(FV3D_ERR_INVALID_ARG, "inner_dim must be 1..30 and inner_sweeps 1..8");
+    if (opts.inner_sweeps == 0) opts.inner_sweeps = 4;
+    if (opts.inner_omega == 0.0) opts.inner_omega = 0.7;
+    if (opts.inner_dim < 1 || opts.inner_dim > 30 || opts.inner_sweeps < 1 || opts.inner_sweeps > 8 ||
+        !(opts.inner_omega > 0.0 && opts.inner_omega <= 2.0))
+      return ctx.fail(FV3D_ERR_INVALID_ARG, "inner_dim must be 1..30, inner_sweeps 1..8, inner_omega in (0, 2]");
   }
   if (opts.preconditioner == FV3D_PC_LEARNED && !(ctx.mlp && ctx.mlp->ready))
     return ctx.fail(FV3D_ERR_STATE, "learned preconditioner requested but no MLP initialised");
@@ -1398,7 +1400,8 @@ extern "C" fv3d_status fv3d_implicit_default_opts(fv3d_implicit_opts* o) {
   o->max_restarts = 0;
   o->sync_every = 10;
   o->inner_dim = 10;
-  o->inner_sweeps = 2;
+  o->inner_sweeps = 4;
+  o->inner_omega = 0.7;
   return FV3D_OK;
 }
 

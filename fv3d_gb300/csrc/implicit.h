@@ -39,6 +39,7 @@ struct Mlp {
 struct Coupled {
   int nc = 0, mcf = 0, m_cap = 0;  // sizes the buffers are allocated for
   int m_in = 0, sweep_count = 0;   // inner GMRES iterations and sweeps of the current solve
+  float omega = 0.f;               // damping of the sweeps
   size_t n = 0, ldb = 0;
   DevBuf<int> nbr;                 // [mcf][nc] neighbour of each face slot, -2 - b boundary face b, -1 none
   int nb = 0;
@@ -49,9 +50,9 @@ struct Coupled {
   DevBuf<float> PRi;               // P_R: inverted diagonal blocks [25][nc]; its slot blocks are applied
   DevBuf<float4> rna, st4;         // matrix-free: per slot (normal, a) [mcf][nc], per cell (u, v, w, H)
   DevBuf<float> rb;                // per slot b [mcf][nc]
-  DevBuf<float> Vi, wi, ti, ui;    // inner basis [(m_in + 1)][ldb], work vectors [ldb]
+  DevBuf<float> Vi, Ti, wi, ti;    // inner basis [(m_in + 1)][ldb], directions [m_in][ldb], work [ldb]
   DevBuf<double> hin;              // inner Hessenberg columns [m_in + 1][72] and y
-  fv3d_status setup(Ctx& ctx, Implicit& im, int m_inner, int n_sweeps);
+  fv3d_status setup(Ctx& ctx, Implicit& im, int m_inner, int n_sweeps, float damping);
   fv3d_status build(Ctx& ctx, Implicit& im);
   template <class T>
   fv3d_status apply(Ctx& ctx, Implicit& im, const T* v, T* z);

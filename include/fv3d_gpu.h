@@ -225,7 +225,8 @@ typedef struct fv3d_implicit_opts {
                               meets eta inside a chunk computes up to sync_every - 1 unused steps */
     int inner_dim;         /* FV3D_PC_COUPLED: inner GMRES iterations per application, 1..30 (10) */
     int inner_sweeps;      /* FV3D_PC_COUPLED: Rusanov block-Jacobi sweeps per inner
-                              preconditioning, 1..8 (2) */
+                              preconditioning, 1..8 (4) */
+    double inner_omega;    /* FV3D_PC_COUPLED: damping of those sweeps, (0, 2] (0.7) */
 } fv3d_implicit_opts;
 typedef struct fv3d_implicit_stats {
     int newton_steps;

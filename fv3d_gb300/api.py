@@ -163,6 +163,7 @@ EXPORTS = {
     "fv3d_mlp_harvest": ([C.c_void_p, C.c_int, C.c_int], C.c_int),
     "fv3d_mlp_dataset": ([C.c_void_p, C.POINTER(C.c_int)], C.c_int),
     "fv3d_mlp_train": ([C.c_void_p, C.POINTER(MlpTrainOpts), C.POINTER(MlpTrainStats)], C.c_int),
+    "fv3d_mlp_adam_step": ([C.c_void_p, _f4p, C.c_double], C.c_int),
 }
 
 _lib = None
@@ -497,6 +498,11 @@ class Solver:
         self._check(self.lib.fv3d_mlp_train(self.h, C.byref(MlpTrainOpts(epochs, batch, lr, seed)),
                                             C.byref(st)))
         return {f: getattr(st, f) for f, _ in MlpTrainStats._fields_}
+
+    def mlp_adam_step(self, grad, lr=1e-3):
+        """One Adam step of the parameters with the given gradient."""
+        g = np.ascontiguousarray(grad, dtype=np.float32)
+        self._check(self.lib.fv3d_mlp_adam_step(self.h, _p(g, _f4p), lr))
 
     def selftest_bounded_wait(self, limit_us: int = 2000):
         """(timed_out, elapsed_ms) of a bounded wait on a phase nothing completes."""

@@ -888,12 +888,12 @@ double* g_noalloc_ptr[kNoAllocMaxDevices] = {};  // resolved by the first call o
 extern "C" fv3d_status fv3d_global_residual_noalloc(fv3d_ctx* handle, double dt, double res[5]) {
   if (handle == nullptr || res == nullptr) return FV3D_ERR_INVALID_ARG;
   Ctx* ctx = reinterpret_cast<Ctx*>(handle);
-  if (!ctx->residual_valid) return ctx->fail(FV3D_ERR_STATE, "no residual evaluated (call fv3d_time_derivative)");
-  if (ctx->nc > FV3D_NOALLOC_MAX_CELLS)
+  if (ctx->mesh_ready && ctx->nc > FV3D_NOALLOC_MAX_CELLS)
     return ctx->fail(FV3D_ERR_UNSUPPORTED,
                      "fv3d_global_residual_noalloc: %d cells exceed its static scratch (at most %d cells); "
                      "use fv3d_global_residual",
                      ctx->nc, FV3D_NOALLOC_MAX_CELLS);
+  if (!ctx->residual_valid) return ctx->fail(FV3D_ERR_STATE, "no residual evaluated (call fv3d_time_derivative)");
   const int dev = ctx->cfg.device;
   if (dev < 0 || dev >= kNoAllocMaxDevices)
     return ctx->fail(FV3D_ERR_UNSUPPORTED, "fv3d_global_residual_noalloc: device %d beyond %d", dev,

@@ -27,6 +27,7 @@ struct Mlp {
   fv3d_status forward_host(Ctx& ctx, const float* X, int n, float* Y);
   fv3d_status grad_host(Ctx& ctx, const float* X, const float* T, int n, double* loss, float* g);
   fv3d_status train(Ctx& ctx, const fv3d_mlp_train_opts& o, fv3d_mlp_train_stats* stats);
+  fv3d_status adam_step(Ctx& ctx, float lr);
   fv3d_status build_features(Ctx& ctx, const Implicit& im);
   fv3d_status apply(Ctx& ctx, const double* v, double* z);
   fv3d_status apply(Ctx& ctx, const float* v, float* z);

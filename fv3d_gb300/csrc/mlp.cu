@@ -619,6 +619,17 @@ fv3d_status Mlp::grad_host(Ctx& ctx, const float* X, const float* T, int n, doub
   return FV3D_OK;
 }
 
+// one Adam step of the master parameters with the gradient in grad
+// (beta1 0.9, beta2 0.999, eps 1e-8; bias corrections from the step count)
+fv3d_status Mlp::adam_step(Ctx& ctx, float lr) {
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+  adam_t += 1;
+  const float c1 = 1.f - powf(b1, (float)adam_t), c2 = 1.f - powf(b2, (float)adam_t);
+  k_adam<<<(MLP_NPARAM + 255) / 256, 256, 0, ctx.stream>>>(P.p, grad.p, m.p, v.p, lr, b1, b2, eps, c1, c2);
+  MCK(cudaGetLastError());
+  return FV3D_OK;
+}
+
 fv3d_status Mlp::train(Ctx& ctx, const fv3d_mlp_train_opts& o, fv3d_mlp_train_stats* stats) {
   if (n_samples <= 0) return ctx.fail(FV3D_ERR_STATE, "no training samples harvested");
   const int B = std::max(MLP_TILE, (o.batch / MLP_TILE) * MLP_TILE);
@@ -631,7 +642,6 @@ fv3d_status Mlp::train(Ctx& ctx, const fv3d_mlp_train_opts& o, fv3d_mlp_train_st
   const auto t0 = std::chrono::steady_clock::now();
   const int nparts = B / MLP_TILE;
   double first = -1.0, last = 0.0;
-  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   for (int ep = 0; ep < o.epochs; ++ep) {
     std::iota(h.begin(), h.end(), 0);
     std::shuffle(h.begin(), h.end(), rng);
@@ -643,11 +653,7 @@ fv3d_status Mlp::train(Ctx& ctx, const fv3d_mlp_train_opts& o, fv3d_mlp_train_st
       k_mlp_train<<<nparts, 128, train_smem(), ctx.stream>>>(P.p, X.p, T.p, Wt.p, perm.p + b0, B, 1.f / B,
                                                              part.p, loss_part.p);
       k_mlp_reduce<<<(MLP_NPARAM + 255) / 256, 256, 0, ctx.stream>>>(nparts, part.p, grad.p);
-      adam_t += 1;
-      const float c1 = 1.f - powf(b1, (float)adam_t), c2 = 1.f - powf(b2, (float)adam_t);
-      k_adam<<<(MLP_NPARAM + 255) / 256, 256, 0, ctx.stream>>>(P.p, grad.p, m.p, v.p, (float)o.lr, b1, b2, eps,
-                                                             c1, c2);
-      MCK(cudaGetLastError());
+      if ((st = adam_step(ctx, (float)o.lr)) != FV3D_OK) return st;
       if (b0 == 0 || b0 + 2 * B > n_samples) {  // loss of the first and last batch of the epoch
         MCK(cudaMemcpyAsync(lp.data(), loss_part.p, sizeof(float) * nparts, cudaMemcpyDeviceToHost, ctx.stream));
         MCK(cudaStreamSynchronize(ctx.stream));
@@ -756,6 +762,21 @@ extern "C" fv3d_status fv3d_mlp_set_params(fv3d_ctx* handle, const float* params
 }
 
 extern "C" int fv3d_mlp_num_params(void) { return MLP_NPARAM; }
+
+extern "C" fv3d_status fv3d_mlp_adam_step(fv3d_ctx* handle, const float* grad, double lr) {
+  if (handle == nullptr || grad == nullptr) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (!ctx->mlp || !ctx->mlp->ready) return ctx->fail(FV3D_ERR_STATE, "MLP not initialised");
+  if (!(lr > 0.0)) return ctx->fail(FV3D_ERR_INVALID_ARG, "learning rate must be positive");
+  if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "cudaSetDevice");
+  Mlp& net = *ctx->mlp;
+  if (cudaMemcpy(net.grad.p, grad, sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice) != cudaSuccess)
+    return ctx->fail(FV3D_ERR_DEVICE, "copy gradient");
+  fv3d_status st = net.adam_step(*ctx, (float)lr);
+  if (st != FV3D_OK) return st;
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "Adam step");
+  return FV3D_OK;
+}
 
 extern "C" fv3d_status fv3d_mlp_forward(fv3d_ctx* handle, const float* X, int n, float* Y) {
   if (handle == nullptr || X == nullptr || Y == nullptr || n <= 0) return FV3D_ERR_INVALID_ARG;

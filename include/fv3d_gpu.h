@@ -185,9 +185,13 @@ fv3d_status fv3d_global_residual(fv3d_ctx *ctx, double dt, double res[5]);
  * larger meshes get FV3D_ERR_UNSUPPORTED.  Results are bitwise those of
  * fv3d_global_residual.  The first call on a device looks up the array's
  * address (cudaGetSymbolAddress); make that first call before any stream
- * capture begins.  Nothing in the array needs to start at zero.  Calls that
- * overlap on one device (other threads, other contexts) race on the one
- * array: serialise them. */
+ * capture begins.  The address is kept for the rest of the process: after a
+ * cudaDeviceReset of that device (which also ends every context of this
+ * library on it) do not call this function on the device again.  Each call
+ * waits for the context's stream before it returns, as the result is
+ * copied into res on the host.  Nothing in the array needs to start at zero.
+ * Calls that overlap on one device (other threads, other contexts) race on
+ * the one array: serialise them. */
 #define FV3D_NOALLOC_MAX_CELLS 2097152
 fv3d_status fv3d_global_residual_noalloc(fv3d_ctx *ctx, double dt, double res[5]);
 
@@ -382,6 +386,11 @@ fv3d_status fv3d_mlp_dataset(const fv3d_ctx *ctx, int *n_samples);
 /* Adam training on the harvested pairs (forward/backward/Adam kernels) */
 fv3d_status fv3d_mlp_train(fv3d_ctx *ctx, const fv3d_mlp_train_opts *opts,
                            fv3d_mlp_train_stats *stats);
+/* one Adam step (beta1 0.9, beta2 0.999, eps 1e-8) of the parameters with a
+ * caller-given gradient [fv3d_mlp_num_params()], the device step each batch
+ * of fv3d_mlp_train takes; moments and step count carry over between calls
+ * and training (fv3d_mlp_init resets them) */
+fv3d_status fv3d_mlp_adam_step(fv3d_ctx *ctx, const float *grad, double lr);
 
 /* ---- measurement helpers ------------------------------------------------------ */
 /* average device time (ms) per launch of each kernel of one explicit stage

@@ -318,3 +318,44 @@ def test_profile_step_runs_the_step(precision):
         ms = s.profile_step("rk33", 3, 0.5)
         assert np.all(ms > 0)
         assert np.array_equal(s.get_conserved(), u_graph)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_mesh_from_gmsh_41_file(oracle, tmp_path, precision):
+    """A walled channel written as a Gmsh MSH 4.1 file (the reference
+    preprocessor's format) and read back: the GPU residual on that mesh
+    against the oracle's (tests/test_gmsh.py shows the file's mesh equals
+    the generator's)."""
+    import os
+    from fv3d_gb300 import gmsh
+    nx, ny, nz = 6, 4, 4
+    xs = np.linspace(0, 2, nx + 1)
+    ys = mg.stretched_coords(ny, 1.0, 1.1)
+    zs = np.linspace(0, 1, nz + 1)
+    nodes, cn, sh = mg._structured(nx, ny, nz, xs, ys, zs, (False, False, False), 0.0, 0, (2.0, 1.0, 1.0))
+
+    def tag(x):
+        return 1 if abs(x[0]) < 1e-12 else (2 if abs(x[0] - 2.0) < 1e-12 else 3)
+
+    count, first = {}, {}
+    for c in range(cn.shape[0]):
+        for lf in mg.HEX_FACES:
+            key = tuple(sorted(cn[c, lf]))
+            count[key] = count.get(key, 0) + 1
+            first.setdefault(key, cn[c, lf])
+    bnd = [(tag(nodes[list(k)].mean(axis=0)), list(first[k])) for k, n in count.items() if n == 1]
+    p = os.path.join(tmp_path, "channel41.msh")
+    gmsh.write_msh(p, nodes, cn, "hex", bnd, {(2, 1): "inflow", (2, 2): "outlet", (2, 3): "wall", (3, 4): "fluid"},
+                   version="4.1")
+    mesh = gmsh.read_msh(p)
+    assert mesh.region_names == ["flow", "inflow", "outlet", "wall"]
+    c = cases.channel(nx, ny, nz)          # physics, region conditions and state (walls also at z here)
+    c.params["mu_mix"] = 0.01
+    u = perturbed(c)
+    oracle.init(mesh, c.params, c.region_type, c.region_prim)
+    oracle.set_conserved(u)
+    r_ref = oracle.time_derivative(0.0)
+    with api.Solver(mesh, c.params, c.region_type, c.region_prim, precision) as s:
+        s.set_state(u)
+        err = rel_max(s.time_derivative(0.0), r_ref)
+    assert err < (FP64_RESIDUAL_TOL if precision == "fp64" else MIXED_RESIDUAL_TOL), err

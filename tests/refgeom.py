@@ -18,10 +18,15 @@ def load():
     pkg.__path__ = [util]
     sys.modules["refgeom_pkg"] = pkg
     mods = {}
-    for name in ("element", "math", "geometry"):
-        spec = importlib.util.spec_from_file_location(f"refgeom_pkg.{name}", os.path.join(util, f"{name}.py"))
-        mod = importlib.util.module_from_spec(spec)
-        sys.modules[f"refgeom_pkg.{name}"] = mod
-        spec.loader.exec_module(mod)
-        mods[name] = mod
+    # the reference tree is read only: no bytecode caches written into it
+    saved, sys.dont_write_bytecode = sys.dont_write_bytecode, True
+    try:
+        for name in ("element", "math", "geometry"):
+            spec = importlib.util.spec_from_file_location(f"refgeom_pkg.{name}", os.path.join(util, f"{name}.py"))
+            mod = importlib.util.module_from_spec(spec)
+            sys.modules[f"refgeom_pkg.{name}"] = mod
+            spec.loader.exec_module(mod)
+            mods[name] = mod
+    finally:
+        sys.dont_write_bytecode = saved
     return mods["element"], mods["geometry"]

@@ -50,8 +50,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--case", default="tgv_tet", choices=["tgv_tet", "tgv_hex", "tgv_mixed", "euler16", "channel"])
-    p.add_argument("--learned", action="store_true",
-                   help="channel: also harvest, train and evaluate the learned preconditioner")
+    p.add_argument("--no-learned", action="store_true",
+                   help="implicit channel: skip harvesting, training and evaluating the learned preconditioner")
     p.add_argument("--n", type=int, default=64)
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--e2e-steps", type=int, default=20)
@@ -260,7 +260,8 @@ def implicit_channel(args, with_cpu=True):
     a 1e-8 relative FP64 residual through the C ABI, with each
     preconditioner: the cell-coupling one (the fastest), none (FGMRES(30),
     3 restarts), block Jacobi (FGMRES(30), the configuration as written),
-    and optionally the learned one.  Also the reference's own implicit step
+    and the learned one (falling back to the coupled one).  Also the
+    reference's own implicit step
     (timestep_newton) on the GPU and on the host cores."""
     from fv3d_gb300 import api, cases
     c = cases.channel()
@@ -296,10 +297,11 @@ def implicit_channel(args, with_cpu=True):
         for k in range(5):
             s.step_newton(k + 1, 0.0, dt, "euler", max_iter_inner=2, is_transient=False, check=False)
         gpu_step = (time.perf_counter() - t1) / 5
-        if args.learned:
+        if not args.no_learned:
             # training pairs from plain Newton-Krylov steps (a separate,
             # untimed solve harvesting 100,000 cells per Newton step, up to
-            # 2e7 pairs), a few epochs of Adam, then the learned solve
+            # 2e7 pairs), a few epochs of Adam, then the learned solve, whose
+            # stagnating cycles are redone with the coupled preconditioner
             s.mlp_init(5)
             s.mlp_harvest(100000, 20000000)
             s.set_state(c.u0)
@@ -308,8 +310,10 @@ def implicit_channel(args, with_cpu=True):
             tr = s.mlp_train(epochs=4, batch=16384, lr=2e-3)
             tr["harvest_newton_steps"] = hv["newton_steps"]
             s.set_state(c.u0)
-            st = s.solve_implicit(preconditioner="learned", max_newton=args.max_newton, check=False)
+            kw = dict(plans[0][1])
+            st = s.solve_implicit(preconditioner="learned", fallback="coupled", check=False, **kw)
             runs["learned"] = {k: st[k] for k in CHANNEL_KEYS}
+            runs["learned"]["settings"] = dict(kw, fallback="coupled")
             runs["learned"]["train"] = tr
     conv = {k: v for k, v in runs.items() if v["converged"]}
     best = min(conv, key=lambda k: conv[k]["wall_ms"]) if conv else "coupled"

@@ -67,7 +67,8 @@ class ImplicitOpts(C.Structure):
                 ("max_newton", C.c_int), ("krylov_dim", C.c_int), ("eta", C.c_double),
                 ("fd_eps", C.c_double), ("jv_precision", C.c_int), ("preconditioner", C.c_int),
                 ("pc_refresh", C.c_int), ("max_restarts", C.c_int), ("sync_every", C.c_int),
-                ("inner_dim", C.c_int), ("inner_sweeps", C.c_int), ("inner_omega", C.c_double)]
+                ("inner_dim", C.c_int), ("inner_sweeps", C.c_int), ("inner_omega", C.c_double),
+                ("fallback", C.c_int)]
 
 
 class ImplicitStats(C.Structure):
@@ -348,7 +349,7 @@ class Solver:
         o = ImplicitOpts()
         self._check(self.lib.fv3d_implicit_default_opts(C.byref(o)))
         for k, v in kw.items():
-            if k == "preconditioner" and isinstance(v, str):
+            if k in ("preconditioner", "fallback") and isinstance(v, str):
                 v = PRECONDITIONERS[v]
             if k == "jv_precision" and isinstance(v, str):
                 v = {"fp64": 0, "fp32": 1}[v]

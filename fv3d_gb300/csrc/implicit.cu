@@ -882,8 +882,10 @@ template fv3d_status Implicit::gs_pass<double>(Ctx&, int, double*, const double*
 
 template <class T>
 fv3d_status Implicit::precondition(Ctx& ctx, const T* v, T* z) {
-  if (opts.preconditioner == FV3D_PC_LEARNED && !use_block_jacobi) return ctx.mlp->apply(ctx, v, z);
-  if (opts.preconditioner == FV3D_PC_COUPLED) return coupled->apply<T>(ctx, *this, v, z);
+  if (opts.preconditioner == FV3D_PC_LEARNED && !use_fallback) return ctx.mlp->apply(ctx, v, z);
+  if (opts.preconditioner == FV3D_PC_COUPLED || (opts.preconditioner == FV3D_PC_LEARNED &&
+                                                 opts.fallback == FV3D_PC_COUPLED))
+    return coupled->apply<T>(ctx, *this, v, z);
   if (opts.preconditioner == FV3D_PC_NONE) {
     if (z != v) ICK(cudaMemcpyAsync(z, v, sizeof(T) * n, cudaMemcpyDeviceToDevice, ctx.stream));
     return FV3D_OK;
@@ -935,11 +937,12 @@ fv3d_status Implicit::build_blocks(Ctx& ctx) {
   // no preconditioner: no blocks, unless a harvest wants them as features
   const bool harvesting = ctx.mlp && ctx.mlp->ready && ctx.mlp->harvest_per_step > 0;
   if (opts.preconditioner == FV3D_PC_NONE && !harvesting) return FV3D_OK;
-  if (opts.preconditioner == FV3D_PC_COUPLED) {
+  if (opts.preconditioner == FV3D_PC_COUPLED ||
+      (opts.preconditioner == FV3D_PC_LEARNED && opts.fallback == FV3D_PC_COUPLED)) {
     if (coupled == nullptr) coupled = new Coupled();
     fv3d_status st = coupled->setup(ctx, *this, opts.inner_dim, opts.inner_sweeps, (float)opts.inner_omega);
     if (st == FV3D_OK) st = coupled->build(ctx, *this);
-    return st;
+    if (st != FV3D_OK || opts.preconditioner == FV3D_PC_COUPLED) return st;
   }
   if (opts.preconditioner == FV3D_PC_LUMPED) {
     // every cell perturbed at once by +-eps/2, eps = 1e-4 ||U_v||_2 (implicit.c:65-117)
@@ -999,8 +1002,7 @@ fv3d_status Implicit::enqueue_arnoldi(Ctx& ctx, T* Vt, T* Zt, T* wt, int k) {
 
 template <class T>
 fv3d_status Implicit::arnoldi_step(Ctx& ctx, T* Vt, T* Zt, T* wt, int k) {
-  const int pc = (opts.preconditioner == FV3D_PC_LEARNED && use_block_jacobi) ? (int)FV3D_PC_BLOCK_JACOBI
-                                                                             : opts.preconditioner;
+  const int pc = (opts.preconditioner == FV3D_PC_LEARNED && use_fallback) ? opts.fallback : opts.preconditioner;
   const long long key = (((long long)k * 8 + pc) * 2 + (sizeof(T) == 4 ? 1 : 0)) * 2 + opts.jv_precision;
   auto it = arnoldi_graphs.find(key);
   if (it == arnoldi_graphs.end()) {
@@ -1120,7 +1122,10 @@ fv3d_status Implicit::fgmres(Ctx& ctx, double rnorm, int* iters, double* rel_res
 fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit_stats* stats) {
   opts = o;
   if (opts.krylov_dim < 1 || opts.krylov_dim > 31) return ctx.fail(FV3D_ERR_INVALID_ARG, "krylov_dim must be 1..31");
-  if (opts.preconditioner == FV3D_PC_COUPLED) {
+  if (opts.preconditioner == FV3D_PC_LEARNED && opts.fallback != FV3D_PC_COUPLED)
+    opts.fallback = FV3D_PC_BLOCK_JACOBI;
+  if (opts.preconditioner == FV3D_PC_COUPLED ||
+      (opts.preconditioner == FV3D_PC_LEARNED && opts.fallback == FV3D_PC_COUPLED)) {
     if (opts.inner_dim == 0) opts.inner_dim = 10;
     if (opts.inner_sweeps == 0) opts.inner_sweeps = 4;
     if (opts.inner_omega == 0.0) opts.inner_omega = 0.7;
@@ -1188,12 +1193,12 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
       if (st != FV3D_OK) return st;
       int it = 0;
       double rr = 0.0;
-      use_block_jacobi = false;
+      use_fallback = false;
       if ((st = fgmres(ctx, res, &it, &rr)) != FV3D_OK) return st;
       gmres_total += it;
       if (opts.preconditioner == FV3D_PC_LEARNED && !(rr <= 0.5)) {
         // stagnation with the learned preconditioner: redo with block Jacobi
-        use_block_jacobi = true;
+        use_fallback = true;
         fallbacks += 1;
         if ((st = fgmres(ctx, res, &it, &rr)) != FV3D_OK) return st;
         gmres_total += it;
@@ -1402,6 +1407,7 @@ extern "C" fv3d_status fv3d_implicit_default_opts(fv3d_implicit_opts* o) {
   o->inner_dim = 10;
   o->inner_sweeps = 4;
   o->inner_omega = 0.7;
+  o->fallback = FV3D_PC_BLOCK_JACOBI;
   return FV3D_OK;
 }
 

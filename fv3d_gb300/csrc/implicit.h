@@ -73,7 +73,7 @@ struct Implicit {
   std::vector<double> history;  // ||R||_2 per Newton step
   int jv_count = 0;
   double unorm = 0.0;
-  bool use_block_jacobi = false;  // learned preconditioner fell back this step
+  bool use_fallback = false;      // learned preconditioner fell back this step
   double* hpin = nullptr;         // pinned host scalars (kHostCoefs doubles)
   double* hcols = nullptr;        // pinned: each Arnoldi step's coefficients, [32][kHostCoefs]
 

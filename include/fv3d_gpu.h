@@ -204,7 +204,7 @@ fv3d_status fv3d_global_residual_noalloc(fv3d_ctx *ctx, double dt, double res[5]
 enum {
     FV3D_PC_BLOCK_JACOBI = 0,  /* first-order diagonal blocks (FD, FP64 build, FP32 apply) */
     FV3D_PC_LUMPED = 1,        /* the reference's lumped blocks (implicit.c:61-119) */
-    FV3D_PC_LEARNED = 2,       /* per-cell MLP, block-Jacobi fallback on stagnation */
+    FV3D_PC_LEARNED = 2,       /* per-cell MLP; a stagnating cycle is redone with `fallback` */
     FV3D_PC_NONE = 3,
     FV3D_PC_COUPLED = 4        /* couples cells: inner GMRES(inner_dim) on I/dt - dR1/dU, R1 the
                                   first-order inviscid residual with the case's flux (its blocks
@@ -231,6 +231,8 @@ typedef struct fv3d_implicit_opts {
     int inner_sweeps;      /* FV3D_PC_COUPLED: Rusanov block-Jacobi sweeps per inner
                               preconditioning, 1..8 (4) */
     double inner_omega;    /* FV3D_PC_COUPLED: damping of those sweeps, (0, 2] (0.7) */
+    int fallback;          /* FV3D_PC_LEARNED: the preconditioner a stagnating cycle is redone
+                              with, FV3D_PC_BLOCK_JACOBI (default) or FV3D_PC_COUPLED */
 } fv3d_implicit_opts;
 typedef struct fv3d_implicit_stats {
     int newton_steps;

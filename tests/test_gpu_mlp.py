@@ -196,3 +196,30 @@ def test_stagnating_network_falls_back_to_block_jacobi():
         st = s.solve_implicit(preconditioner="learned", tol_rel=1e-6, max_newton=200)
     assert st["converged"] == 1
     assert st["fallbacks"] == st["newton_steps"]
+
+
+def test_learned_with_coupled_fallback_reaches_the_oracle_tolerance():
+    """The learned preconditioner with the coupled one as its fallback:
+    converges to the same steady state (the oracle's residual drops by
+    1e-8); the fallback count says how often the network's cycle stagnated."""
+    c = cases.channel(12, 8, 4)
+    o = orc.Oracle("restated")
+    with api.from_case(c, "fp64") as s:
+        s.mlp_init(5)
+        s.mlp_harvest(256, 400000)
+        s.solve_implicit(preconditioner="none", tol_rel=1e-8, max_restarts=3)
+        s.mlp_harvest(0, 400000)
+        s.mlp_train(epochs=20, batch=1024, lr=2e-3)
+        s.set_state(c.u0)
+        st = s.solve_implicit(preconditioner="learned", fallback="coupled", tol_rel=1e-8)
+        u = s.get_conserved()
+        s.set_state(c.u0)
+        cp_st = s.solve_implicit(preconditioner="coupled", tol_rel=1e-8)
+    print("learned + coupled fallback", st["newton_steps"], st["gmres_iterations"], st["fallbacks"],
+          "coupled", cp_st["newton_steps"], cp_st["gmres_iterations"])
+    assert st["converged"] == 1
+    o.init(c.mesh, c.params, c.region_type, c.region_prim)
+    o.set_conserved(c.u0)
+    r0 = np.linalg.norm(o.time_derivative(0.0))
+    o.set_conserved(u)
+    assert np.linalg.norm(o.time_derivative(0.0)) / r0 <= 1e-7

@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--case", default="tgv_tet", choices=["tgv_tet", "tgv_hex", "tgv_mixed", "euler16", "channel"])
+    p.add_argument("--pcs", default="coupled,none,block_jacobi",
+                   help="implicit channel: the preconditioners to time (comma-separated; coupled first)")
     p.add_argument("--no-learned", action="store_true",
                    help="implicit channel: skip harvesting, training and evaluating the learned preconditioner")
     p.add_argument("--n", type=int, default=64)
@@ -270,6 +272,8 @@ def implicit_channel(args, with_cpu=True):
                               max_newton=args.max_newton)),
              ("none", dict(max_restarts=3, max_newton=args.max_newton)),
              ("block_jacobi", dict(max_newton=min(args.max_newton, 100)))]
+    wanted = args.pcs.split(",")
+    plans = [p_ for p_ in plans if p_[0] in wanted or p_[0] == "coupled"]
     with api.Solver(c.mesh, c.params, c.region_type, c.region_prim, "fp64", "morton") as s:
         for pc, kw in plans:
             s.set_state(c.u0)

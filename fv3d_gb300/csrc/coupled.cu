@@ -49,7 +49,7 @@ namespace fv3d {
 namespace {
 
 inline int nblk(size_t n, int t = 256) { return (int)((n + t - 1) / t); }
-constexpr int kHcol = 72;  // per inner column: h [0, 32), h' [32, 64), |w| and 1/|w| at 64, 65
+constexpr int kHcol = 72;  // per inner column: h [0, 32), |w - V h| and its inverse at 64, 65
 
 // neighbour of each face slot: the other cell (>= 0), -2 - b for boundary
 // face b (nf_int + b), -1 for an unused slot
@@ -484,7 +484,7 @@ __device__ __forceinline__ void block_mul_add(const float* __restrict__ B, size_
 // y = P_A x = x / dt - dR1/dU x, matrix-free: per slot the exact
 // derivative of the face's first-order flux along (x_c, x_o) in FP32
 template <int MCF>
-__global__ void __launch_bounds__(256) k_cpl_product(int nc, const float* __restrict__ cst,
+__global__ void __launch_bounds__(256, 4) k_cpl_product(int nc, const float* __restrict__ cst,
                                                      const float* __restrict__ idt, const float4* __restrict__ pna,
                                                      const int* __restrict__ nbr, const float* __restrict__ gst,
                                                      const float* __restrict__ gjac, int rusanov, float gam,
@@ -595,11 +595,11 @@ __global__ void k_cpl_lsq(int m, double* __restrict__ hin) {
   __shared__ float H[30][31];
   __shared__ float cs[30], sn[30], g[31], y[30];
   const int t = threadIdx.x;
-  // the columns, loaded by the block
+  // the columns, loaded by the block (one Gram-Schmidt pass: h at [0, 32))
   for (int q = t; q < m * 31; q += blockDim.x) {
     const int j = q / 31, i = q % 31;
     const double* hc = hin + (size_t)j * kHcol;
-    H[j][i] = (i <= j) ? (float)(hc[i] + hc[32 + i]) : (i == j + 1 ? (float)hc[64] : 0.f);
+    H[j][i] = (i <= j) ? (float)hc[i] : (i == j + 1 ? (float)hc[64] : 0.f);
   }
   __syncthreads();
   if (t != 0) return;
@@ -759,11 +759,12 @@ fv3d_status Coupled::apply(Ctx& ctx, Implicit& im, const T* v, T* z) {
     else CPL_PRODUCT(8);
 #undef CPL_PRODUCT
     CCK(cudaGetLastError());
-    // classical Gram-Schmidt twice, v_{j+1} = w / |w| (the outer solve's passes, FP32)
-    if ((st = im.gs_pass<float>(ctx, 1, wi.p, Vi.p, j + 1, nullptr, hc, 0.0, nullptr)) != FV3D_OK) return st;
-    if ((st = im.gs_pass<float>(ctx, 2, wi.p, Vi.p, j + 1, hc, hc + 32, 0.0, nullptr, nullptr, hc + 64)) != FV3D_OK)
+    // classical Gram-Schmidt once (dots and |w|^2 in one pass, the norm of
+    // the projected w by Pythagoras), v_{j+1} = w / |w|, FP32: a short
+    // inner solve that only preconditions needs no re-orthogonalisation
+    if ((st = im.gs_pass<float>(ctx, 4, wi.p, Vi.p, j + 1, nullptr, hc, 0.0, nullptr, nullptr, hc + 64)) != FV3D_OK)
       return st;
-    if ((st = im.gs_pass<float>(ctx, 3, wi.p, Vi.p, j + 1, hc + 32, nullptr, 0.0, nullptr, nullptr, nullptr,
+    if ((st = im.gs_pass<float>(ctx, 3, wi.p, Vi.p, j + 1, hc, nullptr, 0.0, nullptr, nullptr, nullptr,
                                 Vi.p + (size_t)(j + 1) * ldb, hc + 65)) != FV3D_OK)
       return st;
   }

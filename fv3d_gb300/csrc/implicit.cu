@@ -182,6 +182,9 @@ __device__ __forceinline__ void st_group(T* p, const T* x) {
 //           sqrt(|w|^2 - sum_j h'_j^2) (V orthonormal) and its inverse
 //   PASS 3  v_{k+1} = (w - sum_j h'_j V_j) / that norm, no sums
 //   PASS 0  |w| alone
+//   PASS 4  h_j = w . V_j and |w|^2 (one Gram-Schmidt pass, for the inner
+//           solves of the coupled preconditioner): the last block forms
+//           |w - sum_j h_j V_j| by Pythagoras; PASS 3 follows with h
 // Products and sums in T (FP32 basis: FP32 pipe), the final sums and the
 // coefficients in FP64.
 template <class T>
@@ -282,7 +285,7 @@ __device__ __forceinline__ void gs_group(T* __restrict__ w, const T* __restrict_
   if (PASS == 0) {
 #pragma unroll
     for (int l = 0; l < G; ++l) acc[0] = fmadd(wi[l], wi[l], acc[0]);
-  } else if (PASS == 1) {
+  } else if (PASS == 1 || PASS == 4) {
 #pragma unroll
     for (int j = 0; j < KMAX; ++j)
       if (j < k) {
@@ -291,6 +294,10 @@ __device__ __forceinline__ void gs_group(T* __restrict__ w, const T* __restrict_
 #pragma unroll
         for (int l = 0; l < G; ++l) acc[j] = fmadd(wi[l], v[l], acc[j]);
       }
+    if (PASS == 4) {
+#pragma unroll
+      for (int l = 0; l < G; ++l) acc[KMAX] = fmadd(wi[l], wi[l], acc[KMAX]);
+    }
   } else {
     T sum[G];
 #pragma unroll
@@ -341,7 +348,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : FV3D_GS_MINBLOCKS)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (PASS >= 2 && threadIdx.x < 32) hs[threadIdx.x] = (threadIdx.x < (unsigned)k) ? (T)h_in[threadIdx.x] : T(0);
   __syncthreads();
-  constexpr int NA = (PASS == 0 || PASS == 3) ? 1 : (PASS == 2 ? KMAX + 1 : KMAX);
+  constexpr int NA = (PASS == 0 || PASS == 3) ? 1 : ((PASS == 2 || PASS == 4) ? KMAX + 1 : KMAX);
   constexpr int L = 16 / sizeof(T);
   T acc[NA];
 #pragma unroll
@@ -357,21 +364,21 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : FV3D_GS_MINBLOCKS)
   // PASS 2: |w|^2 goes to column 31 (k <= 31 vectors use columns 0 .. 30)
 #pragma unroll
   for (int j = 0; j < NA; ++j) {
-    const bool take = (PASS == 2 && j == KMAX) || j < kk;
+    const bool take = ((PASS == 2 || PASS == 4) && j == KMAX) || j < kk;
     if (!take) continue;
     T v = acc[j];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) sh[warp][(PASS == 2 && j == KMAX) ? 31 : j] = v;
+    if (lane == 0) sh[warp][((PASS == 2 || PASS == 4) && j == KMAX) ? 31 : j] = v;
   }
   __syncthreads();
-  if (threadIdx.x < 32 && ((int)threadIdx.x < kk || (PASS == 2 && threadIdx.x == 31))) {
+  if (threadIdx.x < 32 && ((int)threadIdx.x < kk || ((PASS == 2 || PASS == 4) && threadIdx.x == 31))) {
     T s = T(0);
 #pragma unroll
     for (int wv = 0; wv < 8; ++wv) s += sh[wv][threadIdx.x];
     partial[(size_t)blockIdx.x * 32 + threadIdx.x] = s;
   }
-  gs_finalize<T>(partial, gridDim.x, kk, out, PASS == 0, c, counter, PASS == 2 ? out2 : nullptr);
+  gs_finalize<T>(partial, gridDim.x, kk, out, PASS == 0, c, counter, (PASS == 2 || PASS == 4) ? out2 : nullptr);
 }
 
 
@@ -842,7 +849,8 @@ template <class T>
 fv3d_status Implicit::gs_pass(Ctx& ctx, int pass, T* wv, const T* Vb, int k, const double* h_in, double* dst,
                               double c, const double* c_dev, const T* jv_z, double* dst2, T* vout,
                               const double* scale) {
-  if (pass == 2 && k > 31) return ctx.fail(FV3D_ERR_INVALID_ARG, "Gram-Schmidt pass over %d > 31 vectors", k);
+  if ((pass == 2 || pass == 4) && k > 31)
+    return ctx.fail(FV3D_ERR_INVALID_ARG, "Gram-Schmidt pass over %d > 31 vectors", k);
   JvArgs<T> jv;
   if (jv_z != nullptr) {
     jv.z = jv_z; jv.Rp = Rp.p; jv.Rb = Rb.p; jv.idt = idtl.p; jv.ieps = jv_ieps; jv.nc = (size_t)ctx.nc;
@@ -856,6 +864,7 @@ fv3d_status Implicit::gs_pass(Ctx& ctx, int pass, T* wv, const T* Vb, int k, con
   if (pass == 0) GS_LAUNCH(1, 0);
   else if (pass == 3) { if (k <= 8) GS_LAUNCH(8, 3); else if (k <= 16) GS_LAUNCH(16, 3); else GS_LAUNCH(32, 3); }
   else if (pass == 1) { if (k <= 8) GS_LAUNCH(8, 1); else if (k <= 16) GS_LAUNCH(16, 1); else GS_LAUNCH(32, 1); }
+  else if (pass == 4) { if (k <= 8) GS_LAUNCH(8, 4); else if (k <= 16) GS_LAUNCH(16, 4); else GS_LAUNCH(32, 4); }
   else { if (k <= 8) GS_LAUNCH(8, 2); else if (k <= 16) GS_LAUNCH(16, 2); else GS_LAUNCH(32, 2); }
 #undef GS_LAUNCH
   ICK(cudaGetLastError());

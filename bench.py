@@ -52,6 +52,8 @@ def parse():
     p.add_argument("--case", default="tgv_tet", choices=["tgv_tet", "tgv_hex", "tgv_mixed", "euler16", "channel"])
     p.add_argument("--pcs", default="coupled,none,block_jacobi",
                    help="implicit channel: the preconditioners to time (comma-separated; coupled first)")
+    p.add_argument("--harvest-newton", type=int, default=200,
+                   help="implicit channel: Newton steps of the harvesting solve (200: the configuration's)")
     p.add_argument("--no-learned", action="store_true",
                    help="implicit channel: skip harvesting, training and evaluating the learned preconditioner")
     p.add_argument("--n", type=int, default=64)
@@ -309,7 +311,8 @@ def implicit_channel(args, with_cpu=True):
             s.mlp_init(5)
             s.mlp_harvest(100000, 20000000)
             s.set_state(c.u0)
-            hv = s.solve_implicit(preconditioner="none", max_newton=200, max_restarts=3, check=False)
+            hv = s.solve_implicit(preconditioner="none", max_newton=args.harvest_newton, max_restarts=3,
+                                  check=False)
             s.mlp_harvest(0, 20000000)
             tr = s.mlp_train(epochs=4, batch=16384, lr=2e-3)
             tr["harvest_newton_steps"] = hv["newton_steps"]
@@ -319,6 +322,24 @@ def implicit_channel(args, with_cpu=True):
             runs["learned"] = {k: st[k] for k in CHANNEL_KEYS}
             runs["learned"]["settings"] = dict(kw, fallback="coupled")
             runs["learned"]["train"] = tr
+            # one application of the network to a field on the mesh: the
+            # tcgen05 kernels (used) and the warp-level mma.sync ones
+            peaks = {}
+            pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+            if os.path.exists(pk):
+                with open(pk) as f:
+                    peaks = json.load(f)
+            flop = 21632.0 * c.mesh.n_cells
+            app = {}
+            for kind in ("mma_sync", "tcgen05"):
+                s.mlp_set_kernel(kind)
+                ms = s.profile_mlp(50)
+                app[kind] = {"ms": round(ms, 5), "tflops": round(flop / (ms * 1e-3) / 1e12, 2)}
+            app["flop_per_application"] = flop
+            app["bf16_peak_tflops"] = peaks.get("bf16_tflops")
+            app["frac_tcgen05"] = (round(app["tcgen05"]["tflops"] / peaks["bf16_tflops"], 4)
+                                   if peaks.get("bf16_tflops") else None)
+            runs["learned"]["mlp_apply"] = app
     conv = {k: v for k, v in runs.items() if v["converged"]}
     best = min(conv, key=lambda k: conv[k]["wall_ms"]) if conv else "coupled"
     out = {"metric": "seconds to 1e-8 relative steady residual", "value": round(runs[best]["wall_ms"] / 1e3, 4),

@@ -165,6 +165,8 @@ EXPORTS = {
     "fv3d_mlp_dataset": ([C.c_void_p, C.POINTER(C.c_int)], C.c_int),
     "fv3d_mlp_train": ([C.c_void_p, C.POINTER(MlpTrainOpts), C.POINTER(MlpTrainStats)], C.c_int),
     "fv3d_mlp_adam_step": ([C.c_void_p, _f4p, C.c_double], C.c_int),
+    "fv3d_mlp_set_kernel": ([C.c_void_p, C.c_int], C.c_int),
+    "fv3d_profile_mlp": ([C.c_void_p, C.c_int, _f8p], C.c_int),
 }
 
 _lib = None
@@ -499,6 +501,16 @@ class Solver:
         self._check(self.lib.fv3d_mlp_train(self.h, C.byref(MlpTrainOpts(epochs, batch, lr, seed)),
                                             C.byref(st)))
         return {f: getattr(st, f) for f, _ in MlpTrainStats._fields_}
+
+    def mlp_set_kernel(self, kind: str):
+        """The network's inference kernels: "tcgen05" (default) or "mma_sync"."""
+        self._check(self.lib.fv3d_mlp_set_kernel(self.h, {"mma_sync": 0, "tcgen05": 1}[kind]))
+
+    def profile_mlp(self, n_reps: int = 20) -> float:
+        """Average ms of one application of the network on the mesh."""
+        ms = C.c_double()
+        self._check(self.lib.fv3d_profile_mlp(self.h, n_reps, C.byref(ms)))
+        return ms.value
 
     def mlp_adam_step(self, grad, lr=1e-3):
         """One Adam step of the parameters with the given gradient."""

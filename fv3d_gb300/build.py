@@ -17,7 +17,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfv3d_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["api.cu", "mesh.cu", "kernels_f64.cu", "kernels_mx_sides.cu", "kernels_mx_flux.cu",
-           "implicit.cu", "coupled.cu", "mlp.cu"]
+           "implicit.cu", "coupled.cu", "mlp.cu", "mlp_tc.cu"]
 FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "--expt-relaxed-constexpr", f"-I{ROOT}/include"]
 

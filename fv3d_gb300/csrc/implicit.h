@@ -32,6 +32,14 @@ struct Mlp {
   fv3d_status apply(Ctx& ctx, const double* v, double* z);
   fv3d_status apply(Ctx& ctx, const float* v, float* z);
   fv3d_status harvest(Ctx& ctx, const Implicit& im);
+  // the tcgen05 (TMEM-accumulator) forward (mlp_tc.cu); the inference
+  // kernels used: tcgen05 (default) or the warp-level mma.sync ones
+  bool use_tc = true, tc_ready = false;
+  DevBuf<int> tc_status;            // nonzero: a bounded wait of the tcgen05 kernel ran out
+  fv3d_status tc_setup(Ctx& ctx);
+  fv3d_status forward_tc(Ctx& ctx, const float* dX, int n, float* dY);
+  template <class VT>
+  fv3d_status apply_tc(Ctx& ctx, const VT* v, VT* z);
 };
 
 // cell-coupling preconditioner (coupled.cu): z = M v, M an inner GMRES on

@@ -40,10 +40,8 @@ __device__ __forceinline__ void mma16816(float* c, uint32_t a0, uint32_t a1, uin
       : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
 }
 
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
-__device__ __forceinline__ float gelu_d(float x) {
-  return 0.5f * (1.f + erff(x * 0.70710678118654752f)) + x * expf(-0.5f * x * x) * 0.39894228040143268f;
-}
+__device__ __forceinline__ float gelu(float x) { return mlp_gelu(x); }
+__device__ __forceinline__ float gelu_d(float x) { return mlp_gelu_d(x); }
 
 struct MlpW {  // BF16 weights in the layouts the fragments read
   bf16 W0[MLP_H * LD_X];   // [out][in]
@@ -569,7 +567,7 @@ fv3d_status Mlp::init(Ctx& ctx, unsigned long long seed) {
   adam_t = 0;
   ready = true;
   MCK(cudaFuncSetAttribute(k_mlp_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)train_smem()));
-  return FV3D_OK;
+  return tc_setup(ctx);  // outside any stream capture: the solve's graphs launch the tcgen05 kernels
 }
 
 fv3d_status Mlp::ensure_scratch(Ctx& ctx, int nbatch) {
@@ -585,10 +583,23 @@ fv3d_status Mlp::forward_host(Ctx& ctx, const float* X, int n, float* Y) {
   MCK(dX.alloc((size_t)n * MLP_IN));
   MCK(dY.alloc((size_t)n * MLP_OUT));
   MCK(cudaMemcpy(dX.p, X, sizeof(float) * n * MLP_IN, cudaMemcpyHostToDevice));
-  k_mlp_forward<<<inference_grid((n + 16 * kInfWarps - 1) / (16 * kInfWarps)), 32 * kInfWarps, 0, ctx.stream>>>(
-      P.p, dX.p, n, dY.p);
+  if (use_tc) {
+    fv3d_status st = forward_tc(ctx, dX.p, n, dY.p);
+    if (st != FV3D_OK) return st;
+  } else {
+    k_mlp_forward<<<inference_grid((n + 16 * kInfWarps - 1) / (16 * kInfWarps)), 32 * kInfWarps, 0, ctx.stream>>>(
+        P.p, dX.p, n, dY.p);
+  }
   MCK(cudaGetLastError());
   MCK(cudaStreamSynchronize(ctx.stream));
+  if (use_tc) {
+    int flag = 0;
+    MCK(cudaMemcpy(&flag, tc_status.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) {
+      MCK(cudaMemset(tc_status.p, 0, sizeof(int)));
+      return ctx.fail(FV3D_ERR_TIMEOUT, "tcgen05 forward: a bounded wait for the tensor cores ran out");
+    }
+  }
   MCK(cudaMemcpy(Y, dY.p, sizeof(float) * n * MLP_OUT, cudaMemcpyDeviceToHost));
   return FV3D_OK;
 }
@@ -689,6 +700,7 @@ fv3d_status Mlp::build_features(Ctx& ctx, const Implicit& im) {
 }
 
 fv3d_status Mlp::apply(Ctx& ctx, const double* vin, double* zout) {
+  if (use_tc) return apply_tc<double>(ctx, vin, zout);
   k_mlp_apply<double><<<inference_grid((ctx.nc + 16 * kInfWarps - 1) / (16 * kInfWarps)), 32 * kInfWarps, 0,
                         ctx.stream>>>(P.p, ctx.nc, feat.p, vin,
                                                                                           zout);
@@ -697,6 +709,7 @@ fv3d_status Mlp::apply(Ctx& ctx, const double* vin, double* zout) {
 }
 
 fv3d_status Mlp::apply(Ctx& ctx, const float* vin, float* zout) {
+  if (use_tc) return apply_tc<float>(ctx, vin, zout);
   k_mlp_apply<float><<<inference_grid((ctx.nc + 16 * kInfWarps - 1) / (16 * kInfWarps)), 32 * kInfWarps, 0,
                        ctx.stream>>>(P.p, ctx.nc, feat.p, vin,
                                                                                          zout);
@@ -762,6 +775,41 @@ extern "C" fv3d_status fv3d_mlp_set_params(fv3d_ctx* handle, const float* params
 }
 
 extern "C" int fv3d_mlp_num_params(void) { return MLP_NPARAM; }
+
+extern "C" fv3d_status fv3d_profile_mlp(fv3d_ctx* handle, int n_reps, double* ms) {
+  if (handle == nullptr || ms == nullptr || n_reps < 1) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  Mlp* net = ctx->mlp;
+  if (!net || !net->ready || net->feat.n < (size_t)ctx->nc * MLP_FEAT)
+    return ctx->fail(FV3D_ERR_STATE, "no network or no cell features (run a learned or harvesting solve first)");
+  if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "cudaSetDevice");
+  DevBuf<float> v, z;
+  if (v.alloc(5 * (size_t)ctx->nc) != cudaSuccess || z.alloc(5 * (size_t)ctx->nc) != cudaSuccess)
+    return ctx->fail(FV3D_ERR_DEVICE, "allocation");
+  std::vector<float> h(5 * (size_t)ctx->nc);
+  for (size_t i = 0; i < h.size(); ++i) h[i] = 1.f + 0.25f * (float)((i * 2654435761u) % 97) / 97.f;
+  if (cudaMemcpy(v.p, h.data(), sizeof(float) * h.size(), cudaMemcpyHostToDevice) != cudaSuccess)
+    return ctx->fail(FV3D_ERR_DEVICE, "copy");
+  fv3d_status st = net->apply(*ctx, v.p, z.p);  // warm-up
+  if (st != FV3D_OK) return st;
+  if (cudaEventRecord(ctx->ev0, ctx->stream) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "event");
+  for (int r = 0; r < n_reps; ++r)
+    if ((st = net->apply(*ctx, v.p, z.p)) != FV3D_OK) return st;
+  float t = 0.f;
+  if (cudaEventRecord(ctx->ev1, ctx->stream) != cudaSuccess || cudaEventSynchronize(ctx->ev1) != cudaSuccess ||
+      cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1) != cudaSuccess)
+    return ctx->fail(FV3D_ERR_DEVICE, "timing");
+  *ms = t / n_reps;
+  return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_mlp_set_kernel(fv3d_ctx* handle, int tensor_core) {
+  if (handle == nullptr || (tensor_core != 0 && tensor_core != 1)) return FV3D_ERR_INVALID_ARG;
+  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+  if (ctx->implicit) ctx->implicit->release_graphs();  // captured steps hold the inference kernel
+  mlp_of(ctx)->use_tc = tensor_core == 1;
+  return FV3D_OK;
+}
 
 extern "C" fv3d_status fv3d_mlp_adam_step(fv3d_ctx* handle, const float* grad, double lr) {
   if (handle == nullptr || grad == nullptr) return FV3D_ERR_INVALID_ARG;

@@ -393,6 +393,15 @@ fv3d_status fv3d_mlp_train(fv3d_ctx *ctx, const fv3d_mlp_train_opts *opts,
  * of fv3d_mlp_train takes; moments and step count carry over between calls
  * and training (fv3d_mlp_init resets them) */
 fv3d_status fv3d_mlp_adam_step(fv3d_ctx *ctx, const float *grad, double lr);
+/* the network's inference kernels (forward and the preconditioner's
+ * application): 1 (default) the tcgen05 ones, accumulators in tensor memory,
+ * 128-cell tiles; 0 the warp-level mma.sync ones.  Same BF16 roundings. */
+fv3d_status fv3d_mlp_set_kernel(fv3d_ctx *ctx, int tensor_core);
+/* average device time (ms, CUDA events on the context's stream) of one
+ * application of the network to a vector field on the mesh, over n_reps
+ * back-to-back applications with the current inference kernels (needs the
+ * cell features of a learned or harvesting solve) */
+fv3d_status fv3d_profile_mlp(fv3d_ctx *ctx, int n_reps, double *ms);
 
 /* ---- measurement helpers ------------------------------------------------------ */
 /* average device time (ms) per launch of each kernel of one explicit stage

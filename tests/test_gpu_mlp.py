@@ -34,7 +34,8 @@ def unpack(p):
 
 def torch_loss(params, X, T):
     W0, b0, W1, b1, W2, b2, W3, b3 = params
-    gelu = torch.nn.functional.gelu
+    def gelu(v):
+        return torch.nn.functional.gelu(v, approximate="tanh")
     a = gelu(X @ W0.T + b0)
     a = gelu(a @ W1.T + b1)
     a = gelu(a @ W2.T + b2)
@@ -59,14 +60,17 @@ def bf16_np(a):
     return r.view(np.float32).astype(np.float64)
 
 
+C_GELU = np.sqrt(2.0 / np.pi)
+
+
 def gelu_np(x):
-    from scipy.special import erf
-    return 0.5 * x * (1.0 + erf(x / np.sqrt(2.0)))
+    """GELU in its tanh form, the kernels' activation."""
+    return 0.5 * x * (1.0 + np.tanh(C_GELU * (x + 0.044715 * x ** 3)))
 
 
 def gelu_d_np(x):
-    from scipy.special import erf
-    return 0.5 * (1.0 + erf(x / np.sqrt(2.0))) + x * np.exp(-0.5 * x * x) / np.sqrt(2.0 * np.pi)
+    t = np.tanh(C_GELU * (x + 0.044715 * x ** 3))
+    return 0.5 * (1.0 + t) + 0.5 * x * (1.0 - t * t) * C_GELU * (1.0 + 3 * 0.044715 * x * x)
 
 
 def kernel_arithmetic(p, X, T):
@@ -126,8 +130,10 @@ def test_forward_and_gradient_match_cpu_fp64(solver):
     el = abs(loss - L2) / L2
     eg = np.linalg.norm(g - g2) / np.linalg.norm(g2)
     print("kernel arithmetic: forward", ey, "loss", el, "gradient", eg)
-    # measured on GB300: forward 5.4e-6, loss 1.0e-7, gradient 4.6e-5
-    assert ey < 5e-5 and el < 1e-5 and eg < 5e-4, (ey, el, eg)
+    # measured on GB300: forward 2.5e-3, loss 5.0e-7, gradient 2.5e-4 (the
+    # kernels' hardware tanh differs from the exact one by about 2^-11, which
+    # moves some activations across a BF16 rounding boundary)
+    assert ey < 5e-3 and el < 1e-5 and eg < 1e-3, (ey, el, eg)
 
 
 def test_adam_step_matches_numpy(solver):
@@ -223,3 +229,30 @@ def test_learned_with_coupled_fallback_reaches_the_oracle_tolerance():
     r0 = np.linalg.norm(o.time_derivative(0.0))
     o.set_conserved(u)
     assert np.linalg.norm(o.time_derivative(0.0)) / r0 <= 1e-7
+
+
+def test_tcgen05_forward_matches_mma_sync_and_the_bf16_arithmetic(solver):
+    """The tcgen05 inference kernel (128-cell tiles, accumulators in tensor
+    memory) against the warp-level mma.sync one and against the FP64
+    arithmetic with the kernels' BF16 roundings; a row count that is not a
+    multiple of the tile."""
+    rng = np.random.default_rng(9)
+    p = (rng.standard_normal(NP) * 0.2).astype(np.float32)
+    solver.mlp_set_params(p)
+    X = rng.standard_normal((1000, 36)).astype(np.float32)
+    T = np.zeros((1000, 5))
+    solver.mlp_set_kernel("mma_sync")
+    y_mma = solver.mlp_forward(X)
+    solver.mlp_set_kernel("tcgen05")
+    y_tc = solver.mlp_forward(X)
+    y_ref = kernel_arithmetic(p, X.astype(np.float64), T)[0]
+    scale = np.abs(y_ref).max()
+    e_tc = np.abs(y_tc - y_ref).max() / scale
+    e_mma = np.abs(y_mma - y_ref).max() / scale
+    print("tcgen05 vs FP64 BF16 arithmetic", e_tc, "mma.sync", e_mma, "tcgen05 vs mma.sync",
+          np.abs(y_tc - y_mma).max() / scale)
+    # measured on GB300: tcgen05 and mma.sync agree bitwise; against the FP64
+    # arithmetic 3.0e-3 (largest of 1,000 rows: the hardware tanh moves some
+    # activations across a BF16 rounding boundary)
+    assert e_tc < 5e-3 and e_mma < 5e-3
+    assert np.abs(y_tc - y_mma).max() / scale < 1e-6

@@ -117,9 +117,9 @@ def tgv_mixed(n=16, gradient=GREEN_GAUSS, jitter=0.1, seed=20240601) -> Case:
     return Case("tgv_mixed", mesh, params, np.array([mg.BC_FLOW]), prim, u0, "rk33", 0.5, 50)
 
 
-def channel(nx=96, ny=48, nz=48, ratio=1.1) -> Case:
+def channel(nx=96, ny=48, nz=48, ratio=1.1, tets=False) -> Case:
     kappa = 1.4
-    mesh = mg.channel(nx, ny, nz, 2.0, 1.0, 1.0, ratio)
+    mesh = mg.channel(nx, ny, nz, 2.0, 1.0, 1.0, ratio, tets=tets)
     p_in = 1.0 / kappa
     T_in = p_in / 1.0          # rho = 1, R = 1
     # second-order AUSM without a limiter: the configuration names none and

@@ -471,6 +471,140 @@ __device__ __forceinline__ void mx_make_state(float rho, float mx, float my, flo
   y = make_float4(E, p, p * ir / ph.R, ir);
 }
 
+// one face of a cell in the flux pass: the convective flux from both side
+// records (this cell's m, the other side's o) plus the averaged viscous
+// flux (the sides' viscous energy fluxes vm, vo), with this cell's sign
+template <bool VISC>
+__device__ __forceinline__ void mx_face_signed(const float4 m0, const float4 m1, const float4 o0, const float4 o1,
+                                               const float4 nA, const float vm, const float vo, const int side,
+                                               const MxPhys& ph, float* out) {
+  // cell 0's side left, cell 1's right: both cells evaluate the face
+  // from the same operands in the same order
+  const float4 l0 = side ? o0 : m0, l1 = side ? o1 : m1;
+  const float4 r0 = side ? m0 : o0, r1 = side ? m1 : o1;
+  const float l[5] = {l0.x, l0.y, l0.z, l0.w, l1.x};
+  const float r[5] = {r0.x, r0.y, r0.z, r0.w, r1.x};
+  float F[5];
+  mx_conv_flux(l, r, nA, ph, F);
+  if (VISC) {
+    const float2 ve = side ? make_float2(vo, vm) : make_float2(vm, vo);
+    F[1] += 0.5f * (l1.y + r1.y);
+    F[2] += 0.5f * (l1.z + r1.z);
+    F[3] += 0.5f * (l1.w + r1.w);
+    F[4] += 0.5f * (ve.x + ve.y);
+  }
+  // the second cell takes the flux with the opposite sign (sub(x) is
+  // add(-x)): a select, not a divergent branch
+  const float sg = side ? -1.f : 1.f;
+#pragma unroll
+  for (int j = 0; j < 5; ++j) out[j] = sg * F[j];
+}
+
+// slot k of cell c with both side records in global memory (the own side
+// at k * ncp + c, the other side at e >> 1), added to s
+template <bool VISC>
+__device__ __forceinline__ void mx_face_global(const MxArgs& a, const MxPhys& ph, int k, int c, int e,
+                                               Acc<float, false>* s) {
+  const size_t own = (size_t)k * a.ncp + c, oth = (size_t)(e >> 1);
+  float4 m0, m1, o0, o1;
+  ld_rec_nc(a.fs + own * 8, m0, m1);  // this cell's side (a warp's loads contiguous)
+  ld_rec_nc(a.fs + oth * 8, o0, o1);  // the other side
+  const float4 nA = __ldg(&a.slotNk[own]);
+  float vm = 0.f, vo = 0.f;
+  if (VISC) { vm = __ldg(a.fsv + own); vo = __ldg(a.fsv + oth); }
+  float F[5];
+  mx_face_signed<VISC>(m0, m1, o0, o1, nA, vm, vo, e & 1, ph, F);
+#pragma unroll
+  for (int j = 0; j < 5; ++j) s[j].add(F[j]);
+}
+
+// the rest of the flux + update pass for cell c once its face sums s are
+// complete: -sum/V, the RK update, the FP32 stage record and (DT) the
+// cell's time-step bound
+template <int MODE, bool DT, bool STORE>
+__device__ __forceinline__ void mx_update_cell(const MxArgs& a, const StageCoef& co, const MxPhys& ph, const int c,
+                                               const Acc<float, false>* s, unsigned long long& lam_bits,
+                                               bool& finite) {
+  const float rv = __ldg(&a.cgeo[c]).w;
+  float rr[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) rr[j] = -s[j].value() * rv;
+  if (MODE == 0 || STORE) {
+#pragma unroll
+    for (int j = 0; j < 5; ++j) a.dphi[(size_t)j * a.nc + c] = (double)rr[j];
+  }
+  if (MODE != 0) {
+    const double dt = a.sc->dt;
+    float du[5];
+    if (MODE == 1) {
+      const float gdt = (float)(dt * co.g);
+#pragma unroll
+      for (int j = 0; j < 5; ++j) {
+        const size_t i = (size_t)j * a.ncp + c;
+        const float kj = co.first ? rr[j] : fmaf(a.kf[i], (float)co.a, rr[j]);
+        if (!co.last) a.kf[i] = kj;
+        du[j] = co.first ? gdt * kj : fmaf(gdt, kj, a.dU[i]);
+      }
+    } else {
+      const float fdt = (float)dt, c1 = (float)co.c1;
+#pragma unroll
+      for (int j = 0; j < 5; ++j) {
+        const size_t i = (size_t)j * a.ncp + c;
+        du[j] = co.first ? fdt * rr[j] : c1 * fmaf(fdt, rr[j], a.dU[i]);
+      }
+    }
+    float* sh = a.Uf + 8 * (size_t)c;
+    float4 o0 = make_float4(0.f, 0.f, 0.f, 0.f), o1 = o0;
+    if (DT && MODE == 1) ld_rec(sh, o0, o1);  // stage-input state
+    float un[5];
+    if (co.last) {
+      // end of step: U_{n+1} = U_n + dU in FP64, new base record
+#pragma unroll
+      for (int j = 0; j < 5; ++j) {
+        const size_t i = (size_t)j * a.nc + c;
+        const double uj = a.U[i] + (double)du[j];
+        a.U[i] = uj;
+        un[j] = (float)uj;
+        finite = finite && isfinite(uj);
+      }
+      float4 x, y;
+      mx_make_state(un[0], un[1], un[2], un[3], un[4], ph, x, y);
+      st_rec(a.UfN + 8 * (size_t)c, x, y);
+      st_rec(sh, x, y);
+    } else {
+      float4 b0, b1;
+      ld_rec_nc(a.UfN + 8 * (size_t)c, b0, b1);
+      un[0] = b0.x + du[0]; un[1] = b0.y + du[1]; un[2] = b0.z + du[2]; un[3] = b0.w + du[3];
+      un[4] = b1.x + du[4];
+#pragma unroll
+      for (int j = 0; j < 5; ++j) {
+        a.dU[(size_t)j * a.ncp + c] = du[j];
+        finite = finite && isfinite(du[j]);
+      }
+      float4 x, y;
+      mx_make_state(un[0], un[1], un[2], un[3], un[4], ph, x, y);
+      st_rec(sh, x, y);
+    }
+    if (DT) {
+      // calc_ns_timestep on the reference's phi_total: new density, the
+      // stage-input u, v, w, p for the low-storage schemes (see
+      // k_gather_update); new state for SSP-RK3
+      const float ir = 1.f / un[0];
+      float pu = un[1] * ir, pv = un[2] * ir, pw = un[3] * ir;
+      float pp = fmaxf(1.00E-10f, ph.km1 * (un[4] - 0.5f * (un[1] * pu + un[2] * pv + un[3] * pw)));
+      if (MODE == 1) {
+        const float io = o1.w;  // 1 / rho of the stage-input record
+        pu = o0.y * io; pv = o0.z * io; pw = o0.w * io; pp = o1.y;
+      }
+      const float cs = sqrtf(ph.kappa * pp * ir);
+      const float4 dxv = __ldg(&a.cdx[c]);
+      const float ds = (fabsf(pu) + cs) * dxv.x + (fabsf(pv) + cs) * dxv.y + (fabsf(pw) + cs) * dxv.z;
+      const double lam = (double)(dxv.w / ds);
+      if (lam > 0.0) lam_bits = (unsigned long long)__double_as_longlong(lam);
+    }
+  }
+}
+
 // MODE 0: residual only; 1: low-storage RK stage; 2: SSP-RK3 stage.
 // co.first / co.last mark the step's first and last stage.
 // STORE: also store the stage's time derivative in dphi (co.store_r; a
@@ -494,114 +628,9 @@ __global__ void __launch_bounds__(256, MCF == 4 ? FV3D_FLUX4_MINBLOCKS : FV3D_FL
     // the registers that keep 5 blocks of the 4-face kernel resident
     Acc<float, false> s[5];
 #pragma unroll kFluxUnroll
-    for (int k = 0; k < MCF; ++k) {
-      if (e[k] < 0) continue;
-      const int side = e[k] & 1;
-      const size_t own = (size_t)k * a.ncp + c, oth = (size_t)(e[k] >> 1);
-      float4 m0, m1, o0, o1;
-      ld_rec_nc(a.fs + own * 8, m0, m1);  // this cell's side (a warp's loads contiguous)
-      ld_rec_nc(a.fs + oth * 8, o0, o1);  // the other side
-      // cell 0's side left, cell 1's right: both cells evaluate the face
-      // from the same operands in the same order
-      const float4 l0 = side ? o0 : m0, l1 = side ? o1 : m1;
-      const float4 r0 = side ? m0 : o0, r1 = side ? m1 : o1;
-      const float l[5] = {l0.x, l0.y, l0.z, l0.w, l1.x};
-      const float r[5] = {r0.x, r0.y, r0.z, r0.w, r1.x};
-      const float4 nA = __ldg(&a.slotNk[(size_t)k * a.ncp + c]);
-      float F[5];
-      mx_conv_flux(l, r, nA, ph, F);
-      if (VISC) {
-        const float vm = __ldg(a.fsv + own), vo = __ldg(a.fsv + oth);
-        const float2 ve = side ? make_float2(vo, vm) : make_float2(vm, vo);
-        F[1] += 0.5f * (l1.y + r1.y);
-        F[2] += 0.5f * (l1.z + r1.z);
-        F[3] += 0.5f * (l1.w + r1.w);
-        F[4] += 0.5f * (ve.x + ve.y);
-      }
-      // the second cell takes the flux with the opposite sign (sub(x) is
-      // add(-x)): a select, not a divergent branch
-      const float sg = side ? -1.f : 1.f;
-#pragma unroll
-      for (int j = 0; j < 5; ++j) s[j].add(sg * F[j]);
-    }
-    const float rv = __ldg(&a.cgeo[c]).w;
-    float rr[5];
-#pragma unroll
-    for (int j = 0; j < 5; ++j) rr[j] = -s[j].value() * rv;
-    if (MODE == 0 || STORE) {
-#pragma unroll
-      for (int j = 0; j < 5; ++j) a.dphi[(size_t)j * a.nc + c] = (double)rr[j];
-    }
-    if (MODE != 0) {
-      const double dt = a.sc->dt;
-      float du[5];
-      if (MODE == 1) {
-        const float gdt = (float)(dt * co.g);
-#pragma unroll
-        for (int j = 0; j < 5; ++j) {
-          const size_t i = (size_t)j * a.ncp + c;
-          const float kj = co.first ? rr[j] : fmaf(a.kf[i], (float)co.a, rr[j]);
-          if (!co.last) a.kf[i] = kj;
-          du[j] = co.first ? gdt * kj : fmaf(gdt, kj, a.dU[i]);
-        }
-      } else {
-        const float fdt = (float)dt, c1 = (float)co.c1;
-#pragma unroll
-        for (int j = 0; j < 5; ++j) {
-          const size_t i = (size_t)j * a.ncp + c;
-          du[j] = co.first ? fdt * rr[j] : c1 * fmaf(fdt, rr[j], a.dU[i]);
-        }
-      }
-      float* sh = a.Uf + 8 * (size_t)c;
-      float4 o0 = make_float4(0.f, 0.f, 0.f, 0.f), o1 = o0;
-      if (DT && MODE == 1) ld_rec(sh, o0, o1);  // stage-input state
-      float un[5];
-      if (co.last) {
-        // end of step: U_{n+1} = U_n + dU in FP64, new base record
-#pragma unroll
-        for (int j = 0; j < 5; ++j) {
-          const size_t i = (size_t)j * a.nc + c;
-          const double uj = a.U[i] + (double)du[j];
-          a.U[i] = uj;
-          un[j] = (float)uj;
-          finite = finite && isfinite(uj);
-        }
-        float4 x, y;
-        mx_make_state(un[0], un[1], un[2], un[3], un[4], ph, x, y);
-        st_rec(a.UfN + 8 * (size_t)c, x, y);
-        st_rec(sh, x, y);
-      } else {
-        float4 b0, b1;
-        ld_rec_nc(a.UfN + 8 * (size_t)c, b0, b1);
-        un[0] = b0.x + du[0]; un[1] = b0.y + du[1]; un[2] = b0.z + du[2]; un[3] = b0.w + du[3];
-        un[4] = b1.x + du[4];
-#pragma unroll
-        for (int j = 0; j < 5; ++j) {
-          a.dU[(size_t)j * a.ncp + c] = du[j];
-          finite = finite && isfinite(du[j]);
-        }
-        float4 x, y;
-        mx_make_state(un[0], un[1], un[2], un[3], un[4], ph, x, y);
-        st_rec(sh, x, y);
-      }
-      if (DT) {
-        // calc_ns_timestep on the reference's phi_total: new density, the
-        // stage-input u, v, w, p for the low-storage schemes (see
-        // k_gather_update); new state for SSP-RK3
-        const float ir = 1.f / un[0];
-        float pu = un[1] * ir, pv = un[2] * ir, pw = un[3] * ir;
-        float pp = fmaxf(1.00E-10f, ph.km1 * (un[4] - 0.5f * (un[1] * pu + un[2] * pv + un[3] * pw)));
-        if (MODE == 1) {
-          const float io = o1.w;  // 1 / rho of the stage-input record
-          pu = o0.y * io; pv = o0.z * io; pw = o0.w * io; pp = o1.y;
-        }
-        const float cs = sqrtf(ph.kappa * pp * ir);
-        const float4 dxv = __ldg(&a.cdx[c]);
-        const float ds = (fabsf(pu) + cs) * dxv.x + (fabsf(pv) + cs) * dxv.y + (fabsf(pw) + cs) * dxv.z;
-        const double lam = (double)(dxv.w / ds);
-        if (lam > 0.0) lam_bits = (unsigned long long)__double_as_longlong(lam);
-      }
-    }
+    for (int k = 0; k < MCF; ++k)
+      if (e[k] >= 0) mx_face_global<VISC>(a, ph, k, c, e[k], s);
+    mx_update_cell<MODE, DT, STORE>(a, co, ph, c, s, lam_bits, finite);
   }
   if (MODE != 0) {
     if (!finite) atomicOr(&a.sc->status, 1);

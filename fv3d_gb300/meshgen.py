@@ -487,14 +487,20 @@ def stretched_coords(n, length, ratio):
     return y
 
 
-def channel(nx=96, ny=48, nz=48, lx=2.0, ly=1.0, lz=1.0, ratio=1.1, name=None):
+def channel(nx=96, ny=48, nz=48, lx=2.0, ly=1.0, lz=1.0, ratio=1.1, name=None, tets=False):
     """Stretched-hex channel: walls at y=0 and y=ly, inflow x=0, pressure outlet
-    x=lx, periodic in z.  Regions: 0 flow, 1 inflow, 2 outlet, 3 wall."""
+    x=lx, periodic in z.  Regions: 0 flow, 1 inflow, 2 outlet, 3 wall.
+    tets=True splits every hex into 6 Kuhn tetrahedra."""
     xs = np.linspace(0.0, lx, nx + 1)
     ys = stretched_coords(ny, ly, ratio)
     zs = np.linspace(0.0, lz, nz + 1)
     nodes, cn, sh = _structured(nx, ny, nz, xs, ys, zs, (False, False, True), 0.0, 0,
                                 (lx, ly, lz))
+    kind = "hex"
+    if tets:
+        cn = cn[:, KUHN_TETS].reshape(-1, 4)
+        sh = sh[:, KUHN_TETS, :].reshape(-1, 4, 3)
+        kind = "tet"
 
     def regions(fx, fn):
         r = np.full(fx.shape[0], 3)                      # walls
@@ -502,9 +508,10 @@ def channel(nx=96, ny=48, nz=48, lx=2.0, ly=1.0, lz=1.0, ratio=1.1, name=None):
         r[np.abs(fx[:, 0] - lx) < 1e-12] = 2             # outlet
         return r
 
-    return build_mesh(nodes, cn, sh, "hex", boundary_region_of_face=regions,
+    return build_mesh(nodes, cn, sh, kind, boundary_region_of_face=regions,
                       region_names=("flow", "inflow", "outlet", "wall"),
-                      region_is_boundary=(0, 1, 1, 1), name=name or f"channel{nx}x{ny}x{nz}")
+                      region_is_boundary=(0, 1, 1, 1),
+                      name=name or f"channel{'_tet' if tets else ''}{nx}x{ny}x{nz}")
 
 
 def mesh_checksum(mesh: Mesh) -> str:

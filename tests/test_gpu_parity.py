@@ -151,6 +151,29 @@ def test_boundary_types_mixed_20_rk3_steps(oracle, label, btype, limiter):
     assert emx.max() < MIXED_STATE_TOL, emx
 
 
+@pytest.mark.parametrize("btype", [None, mg.BC_WALL_SLIP, mg.BC_WALL_ISOTHERMAL, mg.BC_STATE])
+def test_boundary_types_mixed_tets_20_rk3_steps(oracle, btype):
+    """The tetrahedral production kernels (4 face slots: the persistent
+    staged gradient pass) on boundary faces: the channel split into Kuhn
+    tetrahedra, Barth-Jespersen, viscous, 20 RK3 steps against the oracle."""
+    c = cases.channel(12, 6, 4, tets=True)
+    c.params.update(limiter=cases.BARTH_JESPERSEN, mu_mix=0.01)
+    if btype is not None:
+        c.region_type[2] = btype
+        c.region_prim[2] = [0.2, 0.01, 0.0, 1 / 1.4, 0.9 / 1.4]
+        if btype == mg.BC_WALL_ISOTHERMAL:
+            c.region_type[3] = btype
+            c.region_prim[3] = [0.0, 0.0, 0.0, 1 / 1.4, 0.8 / 1.4]
+    c.u0 = perturbed(c)
+    u_ref, t_ref = run_oracle(oracle, c, "rk33", 20, 0.5)
+    with api.from_case(c, "mixed") as s:
+        st = s.step_explicit("rk33", 20, cfl=0.5)
+        emx = rel_l2(s.get_conserved(), u_ref, u_ref=0.3)
+        assert abs(st["t"] / t_ref - 1) < 1e-5
+    print(btype, "tets mixed", emx.max())
+    assert emx.max() < MIXED_STATE_TOL, emx
+
+
 @pytest.mark.parametrize("name", golden_io.names())
 def test_residual_fp64_matches_reference_golden(name):
     """Against outputs of the reference's own C code (committed fixtures)."""

@@ -1135,8 +1135,8 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
     opts.fallback = FV3D_PC_BLOCK_JACOBI;
   if (opts.preconditioner == FV3D_PC_COUPLED ||
       (opts.preconditioner == FV3D_PC_LEARNED && opts.fallback == FV3D_PC_COUPLED)) {
-    if (opts.inner_dim == 0) opts.inner_dim = 10;
-    if (opts.inner_sweeps == 0) opts.inner_sweeps = 4;
+    if (opts.inner_dim == 0) opts.inner_dim = 12;
+    if (opts.inner_sweeps == 0) opts.inner_sweeps = 2;
     if (opts.inner_omega == 0.0) opts.inner_omega = 0.7;
     if (opts.inner_dim < 1 || opts.inner_dim > 30 || opts.inner_sweeps < 1 || opts.inner_sweeps > 8 ||
         !(opts.inner_omega > 0.0 && opts.inner_omega <= 2.0))
@@ -1413,8 +1413,8 @@ extern "C" fv3d_status fv3d_implicit_default_opts(fv3d_implicit_opts* o) {
   o->pc_refresh = 1;
   o->max_restarts = 0;
   o->sync_every = 10;
-  o->inner_dim = 10;
-  o->inner_sweeps = 4;
+  o->inner_dim = 12;
+  o->inner_sweeps = 2;
   o->inner_omega = 0.7;
   o->fallback = FV3D_PC_BLOCK_JACOBI;
   return FV3D_OK;

@@ -227,9 +227,9 @@ typedef struct fv3d_implicit_opts {
     int sync_every;        /* Arnoldi steps launched between host synchronisations (10; 0 takes
                               10): the Givens rotations of a chunk run after it, so a cycle that
                               meets eta inside a chunk computes up to sync_every - 1 unused steps */
-    int inner_dim;         /* FV3D_PC_COUPLED: inner GMRES iterations per application, 1..30 (10) */
+    int inner_dim;         /* FV3D_PC_COUPLED: inner GMRES iterations per application, 1..30 (12) */
     int inner_sweeps;      /* FV3D_PC_COUPLED: Rusanov block-Jacobi sweeps per inner
-                              preconditioning, 1..8 (4) */
+                              preconditioning, 1..8 (2) */
     double inner_omega;    /* FV3D_PC_COUPLED: damping of those sweeps, (0, 2] (0.7) */
     int fallback;          /* FV3D_PC_LEARNED: the preconditioner a stagnating cycle is redone
                               with, FV3D_PC_BLOCK_JACOBI (default) or FV3D_PC_COUPLED */

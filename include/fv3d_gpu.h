@@ -184,8 +184,8 @@ fv3d_status fv3d_global_residual(fv3d_ctx *ctx, double dt, double res[5]);
  * (320 KiB per device), so meshes of at most FV3D_NOALLOC_MAX_CELLS cells;
  * larger meshes get FV3D_ERR_UNSUPPORTED.  Results are bitwise those of
  * fv3d_global_residual.  The first call on a device looks up the array's
- * address (cudaGetSymbolAddress); make that first call before any stream
- * capture begins.  The address is kept for the rest of the process: after a
+ * address (cudaGetSymbolAddress).  The address is kept for the rest of the
+ * process: after a
  * cudaDeviceReset of that device (which also ends every context of this
  * library on it) do not call this function on the device again.  Each call
  * waits for the context's stream before it returns, as the result is

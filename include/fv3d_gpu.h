@@ -207,10 +207,10 @@ enum {
     FV3D_PC_LEARNED = 2,       /* per-cell MLP; a stagnating cycle is redone with `fallback` */
     FV3D_PC_NONE = 3,
     FV3D_PC_COUPLED = 4        /* couples cells: inner GMRES(inner_dim) on I/dt - dR1/dU, R1 the
-                                  first-order inviscid residual with the case's flux (its blocks
-                                  by finite differences per face), right-preconditioned by
-                                  inner_sweeps block-Jacobi sweeps of the first-order Rusanov
-                                  Jacobian (analytic, wave speed frozen) */
+                                  first-order inviscid residual with the case's flux (applied
+                                  matrix-free: each face flux's exact derivative), right-
+                                  preconditioned by inner_sweeps damped block-Jacobi sweeps of the
+                                  first-order Rusanov Jacobian (analytic, wave speed frozen) */
 };
 typedef struct fv3d_implicit_opts {
     double cfl_start;      /* initial CFL (100) */

@@ -36,6 +36,7 @@ struct Mlp {
   // kernels used: tcgen05 (default) or the warp-level mma.sync ones
   bool use_tc = true, tc_ready = false;
   DevBuf<int> tc_status;            // nonzero: a bounded wait of the tcgen05 kernel ran out
+  DevBuf<unsigned char> tc_img;     // the weights as BF16 tiles in the kernel's shared-memory layout
   fv3d_status tc_setup(Ctx& ctx);
   fv3d_status forward_tc(Ctx& ctx, const float* dX, int n, float* dY);
   template <class VT>

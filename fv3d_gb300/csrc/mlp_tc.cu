@@ -20,6 +20,7 @@
 // Every wait on the mbarrier is bounded (0.5 s by %globaltimer); a wait that
 // runs out sets *status and the CTA stops taking tiles (the host reports
 // FV3D_ERR_TIMEOUT).
+#include <cstddef>
 #include <algorithm>
 
 #include <cuda_bf16.h>
@@ -123,33 +124,44 @@ __device__ __forceinline__ bool bar_wait_bounded(uint32_t bar, uint32_t parity) 
 
 __device__ __forceinline__ float tc_gelu(float x) { return mlp_gelu(x); }
 
-// the FP32 master parameters as BF16 core-matrix tiles (W [out][in]: N x K, K-major)
+// the FP32 master parameters as BF16 core-matrix tiles (W [out][in]: N x K,
+// K-major) and FP32 biases, into the weight part of a TcSmem layout (here
+// an image in device memory that each CTA of the network kernels copies)
 __device__ void tc_load_weights(const float* __restrict__ P, TcSmem& S) {
   unsigned char* w0 = reinterpret_cast<unsigned char*>(S.W0);
   unsigned char* w1 = reinterpret_cast<unsigned char*>(S.W1);
   unsigned char* w2 = reinterpret_cast<unsigned char*>(S.W2);
   unsigned char* w3 = reinterpret_cast<unsigned char*>(S.W3);
-  for (int i = threadIdx.x; i < 64 * 48; i += blockDim.x) {
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x, ts = gridDim.x * blockDim.x;
+  for (int i = t0; i < 64 * 48; i += ts) {
     const int o = i / 48, k = i % 48;
     *reinterpret_cast<bf16*>(w0 + core_off(o, k, kKG0)) = __float2bfloat16(k < MLP_IN ? P[MLP_W0 + o * MLP_IN + k] : 0.f);
   }
-  for (int i = threadIdx.x; i < 64 * 64; i += blockDim.x) {
+  for (int i = t0; i < 64 * 64; i += ts) {
     const int o = i / 64, k = i % 64;
     *reinterpret_cast<bf16*>(w1 + core_off(o, k, kKG)) = __float2bfloat16(P[MLP_W1 + o * MLP_H + k]);
     *reinterpret_cast<bf16*>(w2 + core_off(o, k, kKG)) = __float2bfloat16(P[MLP_W2 + o * MLP_H + k]);
   }
-  for (int i = threadIdx.x; i < 16 * 64; i += blockDim.x) {
+  for (int i = t0; i < 16 * 64; i += ts) {
     const int o = i / 64, k = i % 64;
     *reinterpret_cast<bf16*>(w3 + core_off(o, k, kKG)) =
         __float2bfloat16(o < MLP_OUT ? P[MLP_W3 + o * MLP_H + k] : 0.f);
   }
-  for (int i = threadIdx.x; i < 64; i += blockDim.x) {
+  for (int i = t0; i < 64; i += ts) {
     S.b0[i] = P[MLP_B0 + i];
     S.b1[i] = P[MLP_B1 + i];
     S.b2[i] = P[MLP_B2 + i];
   }
-  if (threadIdx.x < 16) S.b3[threadIdx.x] = threadIdx.x < MLP_OUT ? P[MLP_B3 + threadIdx.x] : 0.f;
+  if (t0 < 16) S.b3[t0] = t0 < MLP_OUT ? P[MLP_B3 + t0] : 0.f;
 }
+
+// the packing kernel: the weight image in device memory
+__global__ void k_mlp_pack_tc(const float* __restrict__ P, TcSmem* img) { tc_load_weights(P, *img); }
+
+// bytes of the weight part of TcSmem (W0 .. b3), copied by one bulk copy
+constexpr size_t kTcWeightOff = offsetof(TcSmem, W0);
+constexpr size_t kTcWeightBytes = offsetof(TcSmem, bar) - offsetof(TcSmem, W0);
+static_assert(kTcWeightOff % 16 == 0 && kTcWeightBytes % 16 == 0, "bulk copies move 16-byte multiples");
 
 // the 8 BF16 of K-group j of this thread's row into the A tile
 __device__ __forceinline__ void put_group(TcSmem& S, int row, int j, const float* x) {
@@ -201,7 +213,7 @@ __device__ __forceinline__ void tc_hidden_epilogue(TcSmem& S, uint32_t tmem, con
 // src itself; IN(row, row's floats, x[48]) fills a row's inputs (false: no
 // such row), OUT(row, y[5]) takes its outputs
 template <class IN, class OUT>
-__device__ void tc_forward(const float* __restrict__ P, int n, int* status, const float* __restrict__ src,
+__device__ void tc_forward(const TcSmem* __restrict__ img, int n, int* status, const float* __restrict__ src,
                            int width, IN in, OUT out) {
   extern __shared__ __align__(1024) unsigned char tc_raw[];
   TcSmem& S = *reinterpret_cast<TcSmem*>(tc_raw + ((1024 - (smem_addr(tc_raw) & 1023)) & 1023));
@@ -216,13 +228,30 @@ __device__ void tc_forward(const float* __restrict__ P, int n, int* status, cons
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    // the packed weights: one bulk copy, completing phase 0 of the barrier
+    const uint32_t dst = smem_addr(S.W0);
+    const unsigned char* srcw = reinterpret_cast<const unsigned char*>(img) + kTcWeightOff;
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"((uint32_t)kTcWeightBytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(srcw), "r"((uint32_t)kTcWeightBytes), "r"(bar)
+                 : "memory");
   }
-  tc_load_weights(P, S);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = S.tmem;
-  uint32_t phase = 0;
+  if (__syncthreads_or(!bar_wait_bounded(bar, 0))) {
+    // the weights did not land in time (every thread takes this branch):
+    // report, wait once more so that the copy does not outlive the CTA,
+    // free the tensor memory
+    if (tid == 0) atomicOr(status, 1);
+    bar_wait_bounded(bar, 0);
+    if (warp == 0)
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
+    return;
+  }
+  uint32_t phase = 1;
   const int tiles = (n + kTcRows - 1) / kTcRows;
   for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
     const int row = t * kTcRows + tid;
@@ -278,11 +307,11 @@ __device__ void tc_forward(const float* __restrict__ P, int n, int* status, cons
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcCols) : "memory");
 }
 
-__global__ void __launch_bounds__(kTcRows, 1) k_mlp_forward_tc(const float* __restrict__ P,
+__global__ void __launch_bounds__(kTcRows, 1) k_mlp_forward_tc(const TcSmem* __restrict__ img,
                                                                const float* __restrict__ X, int n,
                                                                float* __restrict__ Y, int* status) {
   tc_forward(
-      P, n, status, X, MLP_IN,
+      img, n, status, X, MLP_IN,
       [&](int row, const float* xs, float* x) {
         if (row >= n) return false;
         for (int k = 0; k < 48; ++k) x[k] = (k < MLP_IN) ? xs[k] : 0.f;
@@ -296,12 +325,12 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_forward_tc(const float* __re
 
 // z = M(v) inside FGMRES: the features of k_mlp_apply, rescaled by |v| / ||D||_F
 template <class T>
-__global__ void __launch_bounds__(kTcRows, 1) k_mlp_apply_tc(const float* __restrict__ P, int nc,
+__global__ void __launch_bounds__(kTcRows, 1) k_mlp_apply_tc(const TcSmem* __restrict__ img, int nc,
                                                              const float* __restrict__ feat,
                                                              const T* __restrict__ v, T* __restrict__ z,
                                                              int* status) {
   tc_forward(
-      P, nc, status, feat, MLP_FEAT,
+      img, nc, status, feat, MLP_FEAT,
       [&](int c, const float* fs, float* x) {
         if (c >= nc) return false;
         float vv[5], s = 0.f;
@@ -327,6 +356,13 @@ __global__ void __launch_bounds__(kTcRows, 1) k_mlp_apply_tc(const float* __rest
       });
 }
 
+// persistent grid of the network kernels: this many CTAs per
+// multiprocessor (5 fit: 43 KB of shared memory, 64 tensor-memory columns
+// and 95 registers x 128 threads each; measured on the channel 3 / 4 / 5:
+// 41.9 / 39.2 / 36.4 us per application)
+#ifndef FV3D_TC_CTAS_PER_SM
+#define FV3D_TC_CTAS_PER_SM 5
+#endif
 int tc_grid(int tiles) {
   static int sms = 0;
   if (sms == 0) {
@@ -334,10 +370,11 @@ int tc_grid(int tiles) {
     if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
       sms = 1;
   }
-  return std::max(1, std::min(tiles, 4 * sms));
+  return std::max(1, std::min(tiles, FV3D_TC_CTAS_PER_SM * sms));
 }
 
 constexpr size_t kTcSmem = sizeof(TcSmem) + 1024;  // + alignment slack
+constexpr int kTcPackBlocks = 16;                    // 4,096 threads pack the 11,013 parameters
 
 }  // namespace
 
@@ -354,6 +391,8 @@ fv3d_status Mlp::tc_setup(Ctx& ctx) {
   TCK(cudaFuncSetAttribute(k_mlp_apply_tc<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmem));
   TCK(tc_status.alloc(1));
   TCK(cudaMemset(tc_status.p, 0, sizeof(int)));
+  TCK(tc_img.alloc(sizeof(TcSmem)));
+  TCK(cudaMemset(tc_img.p, 0, sizeof(TcSmem)));
   tc_ready = true;
   return FV3D_OK;
 }
@@ -361,7 +400,9 @@ fv3d_status Mlp::tc_setup(Ctx& ctx) {
 fv3d_status Mlp::forward_tc(Ctx& ctx, const float* dX, int n, float* dY) {
   fv3d_status st = tc_setup(ctx);
   if (st != FV3D_OK) return st;
-  k_mlp_forward_tc<<<tc_grid((n + kTcRows - 1) / kTcRows), kTcRows, kTcSmem, ctx.stream>>>(P.p, dX, n, dY,
+  TcSmem* img = reinterpret_cast<TcSmem*>(tc_img.p);
+  k_mlp_pack_tc<<<kTcPackBlocks, 256, 0, ctx.stream>>>(P.p, img);
+  k_mlp_forward_tc<<<tc_grid((n + kTcRows - 1) / kTcRows), kTcRows, kTcSmem, ctx.stream>>>(img, dX, n, dY,
                                                                                          tc_status.p);
   TCK(cudaGetLastError());
   return FV3D_OK;
@@ -371,8 +412,12 @@ fv3d_status Mlp::forward_tc(Ctx& ctx, const float* dX, int n, float* dY) {
 template <class VT>
 fv3d_status Mlp::apply_tc(Ctx& ctx, const VT* v, VT* z) {
   if (!tc_ready) return ctx.fail(FV3D_ERR_STATE, "tcgen05 kernels not set up");
+  // the weight image from the current parameters (they change between
+  // training steps), then the network
+  TcSmem* img = reinterpret_cast<TcSmem*>(tc_img.p);
+  k_mlp_pack_tc<<<kTcPackBlocks, 256, 0, ctx.stream>>>(P.p, img);
   k_mlp_apply_tc<VT><<<tc_grid((ctx.nc + kTcRows - 1) / kTcRows), kTcRows, kTcSmem, ctx.stream>>>(
-      P.p, ctx.nc, feat.p, v, z, tc_status.p);
+      img, ctx.nc, feat.p, v, z, tc_status.p);
   TCK(cudaGetLastError());
   return FV3D_OK;
 }

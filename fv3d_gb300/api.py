@@ -354,7 +354,7 @@ class Solver:
             if k in ("preconditioner", "fallback") and isinstance(v, str):
                 v = PRECONDITIONERS[v]
             if k == "jv_precision" and isinstance(v, str):
-                v = {"fp64": 0, "fp32": 1}[v]
+                v = {"fp64": 0, "fp32": 1, "fp32_fp64_arnoldi": 2}[v]
             setattr(o, k, v)
         st = ImplicitStats()
         rc = self.lib.fv3d_solve_implicit(self.h, C.byref(o), C.byref(st))

@@ -920,7 +920,7 @@ fv3d_status Implicit::fd_residual(Ctx& ctx, const T* z, bool unit) {
     eps = hdev.p + 70;
     jv_ieps = hdev.p + 71;
   }
-  if (opts.jv_precision == 1) {
+  if (opts.jv_precision >= 1) {
     k_fd_record<T><<<blocks(ctx.nc), 256, 0, ctx.stream>>>(ctx.nc, ctx.d_U.p, z, eps, ctx.d_Uf.p, ctx.phys.f32[1],
                                                           ctx.phys.f32[4]);
     ICK(cudaGetLastError());
@@ -1012,7 +1012,7 @@ fv3d_status Implicit::enqueue_arnoldi(Ctx& ctx, T* Vt, T* Zt, T* wt, int k) {
 template <class T>
 fv3d_status Implicit::arnoldi_step(Ctx& ctx, T* Vt, T* Zt, T* wt, int k) {
   const int pc = (opts.preconditioner == FV3D_PC_LEARNED && use_fallback) ? opts.fallback : opts.preconditioner;
-  const long long key = (((long long)k * 8 + pc) * 2 + (sizeof(T) == 4 ? 1 : 0)) * 2 + opts.jv_precision;
+  const long long key = (((long long)k * 8 + pc) * 2 + (sizeof(T) == 4 ? 1 : 0)) * 3 + opts.jv_precision;
   auto it = arnoldi_graphs.find(key);
   if (it == arnoldi_graphs.end()) {
     cudaGraph_t g = nullptr;
@@ -1135,7 +1135,7 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
     opts.fallback = FV3D_PC_BLOCK_JACOBI;
   if (opts.preconditioner == FV3D_PC_COUPLED ||
       (opts.preconditioner == FV3D_PC_LEARNED && opts.fallback == FV3D_PC_COUPLED)) {
-    if (opts.inner_dim == 0) opts.inner_dim = 12;
+    if (opts.inner_dim == 0) opts.inner_dim = 10;
     if (opts.inner_sweeps == 0) opts.inner_sweeps = 2;
     if (opts.inner_omega == 0.0) opts.inner_omega = 0.7;
     if (opts.inner_dim < 1 || opts.inner_dim > 30 || opts.inner_sweeps < 1 || opts.inner_sweeps > 8 ||
@@ -1145,10 +1145,10 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
   if (opts.preconditioner == FV3D_PC_LEARNED && !(ctx.mlp && ctx.mlp->ready))
     return ctx.fail(FV3D_ERR_STATE, "learned preconditioner requested but no MLP initialised");
   fv3d_status st = ensure_fp64_path(ctx);
-  if (st == FV3D_OK && opts.jv_precision == 1) st = ensure_mixed_path(ctx);
+  if (st == FV3D_OK && opts.jv_precision >= 1) st = ensure_mixed_path(ctx);
   if (st == FV3D_OK) st = setup(ctx, opts.krylov_dim);
   if (st != FV3D_OK) return st;
-  // Krylov basis in the precision of the Jacobian-vector products
+  // Krylov basis: FP32 with jv_precision 1, FP64 otherwise (2: FP32 products, FP64 Arnoldi)
   {
     const size_t nv = (size_t)(opts.krylov_dim + 1) * ldb, nz = (size_t)opts.krylov_dim * ldb;
     cudaError_t e = cudaSuccess;
@@ -1183,7 +1183,7 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
     if ((st = norm(ctx, ctx.d_U.p, &unorm)) != FV3D_OK) return st;
     {
       // c = rel (1 + |U|) for the finite-difference steps of this Newton step
-      const double rel = (opts.jv_precision == 1) ? 5e-4 : opts.fd_eps;
+      const double rel = (opts.jv_precision >= 1) ? 5e-4 : opts.fd_eps;
       hpin[0] = rel * (1.0 + unorm);
       hpin[1] = 1.0 / hpin[0];
       ICK(cudaMemcpyAsync(hdev.p + 100, hpin, 2 * sizeof(double), cudaMemcpyHostToDevice, ctx.stream));
@@ -1197,7 +1197,7 @@ fv3d_status Implicit::solve(Ctx& ctx, const fv3d_implicit_opts& o, fv3d_implicit
       if (newton % std::max(1, opts.pc_refresh) == 0 || attempt > 0) {
         if ((st = build_blocks(ctx)) != FV3D_OK) return st;
       }
-      if (opts.jv_precision == 1) st = residual32(ctx, ctx.d_U.p, Rb.p);
+      if (opts.jv_precision >= 1) st = residual32(ctx, ctx.d_U.p, Rb.p);
       else st = ICK_copy(ctx, Rb.p, R.p);
       if (st != FV3D_OK) return st;
       int it = 0;
@@ -1413,7 +1413,7 @@ extern "C" fv3d_status fv3d_implicit_default_opts(fv3d_implicit_opts* o) {
   o->pc_refresh = 1;
   o->max_restarts = 0;
   o->sync_every = 10;
-  o->inner_dim = 12;
+  o->inner_dim = 10;
   o->inner_sweeps = 2;
   o->inner_omega = 0.7;
   o->fallback = FV3D_PC_BLOCK_JACOBI;
@@ -1429,7 +1429,7 @@ extern "C" fv3d_status fv3d_solve_implicit(fv3d_ctx* handle, const fv3d_implicit
     if (!(ctx->region_set & (1u << ctx->h_fregion[b])))
       return ctx->fail(FV3D_ERR_STATE, "boundary region %d has no condition", ctx->h_fregion[b]);
   if (opts->preconditioner < 0 || opts->preconditioner > FV3D_PC_COUPLED || opts->jv_precision < 0 ||
-      opts->jv_precision > 1 || !(opts->tol_rel > 0.0) || !(opts->cfl_start > 0.0) || opts->max_newton < 0)
+      opts->jv_precision > 2 || !(opts->tol_rel > 0.0) || !(opts->cfl_start > 0.0) || opts->max_newton < 0)
     return ctx->fail(FV3D_ERR_INVALID_ARG, "bad implicit options");
   if (cudaSetDevice(ctx->cfg.device) != cudaSuccess) return ctx->fail(FV3D_ERR_DEVICE, "cudaSetDevice");
   if (!ctx->implicit) ctx->implicit = new Implicit();

@@ -63,6 +63,12 @@ namespace fv3d {
 #ifndef FV3D_FLUX_UNROLL
 #define FV3D_FLUX_UNROLL 8
 #endif
+// the flux pass sums a cell's face fluxes in slot order (ascending
+// reference face id) with compensated (Kahan) FP32 sums; 0 = plain sums
+#ifndef FV3D_FLUX_KAHAN
+#define FV3D_FLUX_KAHAN 1
+#endif
+constexpr bool kFluxKahan = FV3D_FLUX_KAHAN != 0;
 constexpr int kSidesUnroll = FV3D_SIDES_UNROLL;
 constexpr int kFluxUnroll = FV3D_FLUX_UNROLL;
 
@@ -504,7 +510,7 @@ __device__ __forceinline__ void mx_face_signed(const float4 m0, const float4 m1,
 // at k * ncp + c, the other side at e >> 1), added to s
 template <bool VISC>
 __device__ __forceinline__ void mx_face_global(const MxArgs& a, const MxPhys& ph, int k, int c, int e,
-                                               Acc<float, false>* s) {
+                                               Acc<float, kFluxKahan>* s) {
   const size_t own = (size_t)k * a.ncp + c, oth = (size_t)(e >> 1);
   float4 m0, m1, o0, o1;
   ld_rec_nc(a.fs + own * 8, m0, m1);  // this cell's side (a warp's loads contiguous)
@@ -523,7 +529,7 @@ __device__ __forceinline__ void mx_face_global(const MxArgs& a, const MxPhys& ph
 // cell's time-step bound
 template <int MODE, bool DT, bool STORE>
 __device__ __forceinline__ void mx_update_cell(const MxArgs& a, const StageCoef& co, const MxPhys& ph, const int c,
-                                               const Acc<float, false>* s, unsigned long long& lam_bits,
+                                               const Acc<float, kFluxKahan>* s, unsigned long long& lam_bits,
                                                bool& finite) {
   const float rv = __ldg(&a.cgeo[c]).w;
   float rr[5];
@@ -622,11 +628,12 @@ __global__ void __launch_bounds__(256, MCF == 4 ? FV3D_FLUX4_MINBLOCKS : FV3D_FL
     ph.load(a.pc);
     int e[MCF];
     load_cface<MCF>(a.cother + (size_t)c * MCF, e);
-    // plain FP32 sums in slot order (ascending reference face id): with 4
-    // to 8 terms a compensated sum changed the state after 500 steps by
-    // nothing measurable (the faces' FP32 arithmetic dominates) and cost
-    // the registers that keep 5 blocks of the 4-face kernel resident
-    Acc<float, false> s[5];
+    // compensated FP32 sums in slot order (ascending reference face id):
+    // at 5 resident blocks of the 4-face kernel (48 registers, about 120 B
+    // spilled) they cost 1.5 % of a stage over plain sums, and they change
+    // the state after 500 steps by nothing measurable (the faces' FP32
+    // arithmetic dominates the error)
+    Acc<float, kFluxKahan> s[5];
 #pragma unroll kFluxUnroll
     for (int k = 0; k < MCF; ++k)
       if (e[k] >= 0) mx_face_global<VISC>(a, ph, k, c, e[k], s);

@@ -220,14 +220,17 @@ typedef struct fv3d_implicit_opts {
     int krylov_dim;        /* FGMRES restart length, 1..31 (30) */
     double eta;            /* linear relative tolerance per Newton step (1e-2) */
     double fd_eps;         /* relative finite-difference step of FP64 J v (1e-7) */
-    int jv_precision;      /* 0: J v from the FP64 residual, 1: from the FP32 residual */
+    int jv_precision;      /* 0: J v from the FP64 residual, FP64 Krylov basis; 1: J v from the
+                              FP32 residual, FP32 basis and Gram-Schmidt products (FP64 sums and
+                              coefficients); 2: J v from the FP32 residual, FP64 basis,
+                              Gram-Schmidt and Givens rotations */
     int preconditioner;    /* FV3D_PC_* */
     int pc_refresh;        /* rebuild the blocks every pc_refresh Newton steps */
     int max_restarts;      /* FGMRES restarts per Newton step (0: one cycle) */
     int sync_every;        /* Arnoldi steps launched between host synchronisations (10; 0 takes
                               10): the Givens rotations of a chunk run after it, so a cycle that
                               meets eta inside a chunk computes up to sync_every - 1 unused steps */
-    int inner_dim;         /* FV3D_PC_COUPLED: inner GMRES iterations per application, 1..30 (12) */
+    int inner_dim;         /* FV3D_PC_COUPLED: inner GMRES iterations per application, 1..30 (10) */
     int inner_sweeps;      /* FV3D_PC_COUPLED: Rusanov block-Jacobi sweeps per inner
                               preconditioning, 1..8 (2) */
     double inner_omega;    /* FV3D_PC_COUPLED: damping of those sweeps, (0, 2] (0.7) */

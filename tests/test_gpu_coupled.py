@@ -127,10 +127,12 @@ def test_nested_solve_takes_the_cpu_counts_and_reaches_the_oracle_tolerance():
     assert oracle_residual_norm(c, u) / r0 <= 10 * TOL
 
 
-@pytest.mark.parametrize("jv", ["fp32", "fp64"])
+@pytest.mark.parametrize("jv", ["fp32", "fp64", "fp32_fp64_arnoldi"])
 def test_coupled_cuts_the_krylov_work(jv):
     """Against the solve without a preconditioner and with block Jacobi:
-    far fewer Krylov iterations to the same tolerance, and the answers agree."""
+    far fewer Krylov iterations to the same tolerance, and the answers agree
+    (Jacobian-vector products from FP32 or FP64 residuals; with FP32 ones
+    the Arnoldi basis in FP32 or in FP64)."""
     c = cases.channel(12, 8, 4)
     out = {}
     for pc in ("none", "coupled"):

@@ -721,16 +721,16 @@ __device__ __forceinline__ void load_slots_shared(const int* cf, int* e) {
 }
 
 // shared-memory tile: byte offsets (all multiples of 16)
-template <int MCF, int GMODE>
+template <int MCF, int GMODE, int TL = kTile>
 struct SidesTile {
-  static constexpr int uf = 0;                                    // float [kTile][8]
-  static constexpr int cf = uf + kTile * 32;                      // int [kTile][MCF]
-  static constexpr int cn = cf + kTile * MCF * 4;                 // int [kTile][MCF]
-  static constexpr int cg = cn + kTile * MCF * 4;                 // float4 [kTile]
-  static constexpr int sn = cg + kTile * 16;                      // float4 [MCF][kTile]
-  static constexpr int sd = sn + MCF * kTile * 16;                // float4 [MCF][kTile]
-  static constexpr int sw = sd + MCF * kTile * 16;                // float4 [MCF][kTile] (LSQ)
-  static constexpr int bytes = sw + (GMODE == 2 ? MCF * kTile * 16 : 0);
+  static constexpr int uf = 0;                                    // float [TL][8]
+  static constexpr int cf = uf + TL * 32;                         // int [TL][MCF]
+  static constexpr int cn = cf + TL * MCF * 4;                    // int [TL][MCF]
+  static constexpr int cg = cn + TL * MCF * 4;                    // float4 [TL]
+  static constexpr int sn = cg + TL * 16;                         // float4 [MCF][TL]
+  static constexpr int sd = sn + MCF * TL * 16;                   // float4 [MCF][TL]
+  static constexpr int sw = sd + MCF * TL * 16;                   // float4 [MCF][TL] (LSQ)
+  static constexpr int bytes = sw + (GMODE == 2 ? MCF * TL * 16 : 0);
   static constexpr int bar = bytes;                               // mbarrier (8 bytes)
   static constexpr int total = bytes + 16;
 };
@@ -740,9 +740,9 @@ constexpr int kStatusStageTimeout = 4;
 
 // one tile of the staged gradient pass, from the tile in shared memory
 // (layout SidesTile) for the cell c0 + tid: the arithmetic of k_mx_sides
-template <int MCF, int GMODE, bool LINEAR, bool LIMIT, bool VISC>
+template <int MCF, int GMODE, bool LINEAR, bool LIMIT, bool VISC, int TL = kTile>
 __device__ __forceinline__ void sides_tile(const MxArgs& a, const unsigned char* smem, int c0, int tid) {
-  using L = SidesTile<MCF, GMODE>;
+  using L = SidesTile<MCF, GMODE, TL>;
   const int c = c0 + tid;
   if (c >= a.nc) return;
   MxPhys ph;
@@ -766,7 +766,7 @@ __device__ __forceinline__ void sides_tile(const MxArgs& a, const unsigned char*
   for (int k = 0; k < MCF; ++k) {
     if (o[k] == -2) continue;
     const int f = e[k] >> 1, side = e[k] & 1;
-    const float4 nA = sN[k * kTile + tid];
+    const float4 nA = sN[k * TL + tid];
     float qo[10];
     if (o[k] < 0) {
       const float n[3] = {nA.x, nA.y, nA.z};
@@ -774,11 +774,11 @@ __device__ __forceinline__ void sides_tile(const MxArgs& a, const unsigned char*
     } else {
       // a neighbour inside this tile is already in shared memory
       const unsigned lo = (unsigned)(o[k] - c0);
-      if (lo < (unsigned)kTile) mx_unpack(sUf[2 * lo], sUf[2 * lo + 1], qo);
+      if (lo < (unsigned)TL) mx_unpack(sUf[2 * lo], sUf[2 * lo + 1], qo);
       else ld_unpack(a.Uf + 8 * (size_t)o[k], qo);
     }
     if (GMODE == 1) {
-      const float w = sD[k * kTile + tid].w * nA.w;
+      const float w = sD[k * TL + tid].w * nA.w;
       const float sw = side ? -w : w;
       const float ax = nA.x * sw, ay = nA.y * sw, az = nA.z * sw;
 #pragma unroll
@@ -790,7 +790,7 @@ __device__ __forceinline__ void sides_tile(const MxArgs& a, const unsigned char*
         g[v][2] += dq * az;
       }
     } else {
-      const float4 wl = sW[k * kTile + tid];
+      const float4 wl = sW[k * TL + tid];
 #pragma unroll
       for (int v = 0; v < NG; ++v) {
         const int j = (v < 8) ? v : TT;
@@ -828,11 +828,11 @@ __device__ __forceinline__ void sides_tile(const MxArgs& a, const unsigned char*
   for (int k = 0; k < MCF; ++k) {
     if (o[k] == -2) continue;
     const int f = e[k] >> 1, side = e[k] & 1;
-    const float4 nA4 = sN[k * kTile + tid];
+    const float4 nA4 = sN[k * TL + tid];
     const float nA[3] = {nA4.x * nA4.w, nA4.y * nA4.w, nA4.z * nA4.w};
     float r[12];
     if (LINEAR) {
-      const float4 d = sD[k * kTile + tid];
+      const float4 d = sD[k * TL + tid];
 #pragma unroll
       for (int v = 0; v < 8; ++v) {
         const float slope = d.x * g[v][0] + d.y * g[v][1] + d.z * g[v][2];
@@ -884,13 +884,13 @@ __device__ __forceinline__ void sides_tile(const MxArgs& a, const unsigned char*
   }
 }
 
-template <int MCF, int GMODE, bool LINEAR, bool LIMIT, bool VISC>
-__global__ void __launch_bounds__(kTile, FV3D_TMA_MINBLOCKS) k_mx_sides_tma(const __grid_constant__ MxArgs a) {
+template <int MCF, int GMODE, bool LINEAR, bool LIMIT, bool VISC, int TL = kTile>
+__global__ void __launch_bounds__(TL, FV3D_TMA_MINBLOCKS) k_mx_sides_tma(const __grid_constant__ MxArgs a) {
   static_assert(GMODE != 0, "the staged gradient pass needs gradients");
-  using L = SidesTile<MCF, GMODE>;
+  using L = SidesTile<MCF, GMODE, TL>;
   extern __shared__ __align__(128) unsigned char smem[];
   const int tid = threadIdx.x;
-  const int c0 = blockIdx.x * kTile;
+  const int c0 = blockIdx.x * TL;
   const uint32_t bar = smem_u32(smem + L::bar);
   if (tid == 0) {
     mbar_init(bar, 1);
@@ -900,15 +900,15 @@ __global__ void __launch_bounds__(kTile, FV3D_TMA_MINBLOCKS) k_mx_sides_tma(cons
   if (tid == 0) {
     mbar_expect_tx(bar, L::bytes);
     const uint32_t s0 = smem_u32(smem);
-    bulk_g2s(s0 + L::uf, a.Uf + 8 * (size_t)c0, kTile * 32, bar);
-    bulk_g2s(s0 + L::cf, a.cface + (size_t)c0 * MCF, kTile * MCF * 4, bar);
-    bulk_g2s(s0 + L::cn, a.cnbr + (size_t)c0 * MCF, kTile * MCF * 4, bar);
-    bulk_g2s(s0 + L::cg, a.cgeo + c0, kTile * 16, bar);
+    bulk_g2s(s0 + L::uf, a.Uf + 8 * (size_t)c0, TL * 32, bar);
+    bulk_g2s(s0 + L::cf, a.cface + (size_t)c0 * MCF, TL * MCF * 4, bar);
+    bulk_g2s(s0 + L::cn, a.cnbr + (size_t)c0 * MCF, TL * MCF * 4, bar);
+    bulk_g2s(s0 + L::cg, a.cgeo + c0, TL * 16, bar);
 #pragma unroll
     for (int k = 0; k < MCF; ++k) {
-      bulk_g2s(s0 + L::sn + k * kTile * 16, a.slotNk + (size_t)k * a.ncp + c0, kTile * 16, bar);
-      bulk_g2s(s0 + L::sd + k * kTile * 16, a.slotDk + (size_t)k * a.ncp + c0, kTile * 16, bar);
-      if (GMODE == 2) bulk_g2s(s0 + L::sw + k * kTile * 16, a.slotWk + (size_t)k * a.ncp + c0, kTile * 16, bar);
+      bulk_g2s(s0 + L::sn + k * TL * 16, a.slotNk + (size_t)k * a.ncp + c0, TL * 16, bar);
+      bulk_g2s(s0 + L::sd + k * TL * 16, a.slotDk + (size_t)k * a.ncp + c0, TL * 16, bar);
+      if (GMODE == 2) bulk_g2s(s0 + L::sw + k * TL * 16, a.slotWk + (size_t)k * a.ncp + c0, TL * 16, bar);
     }
   }
   if (!mbar_wait_bounded(bar, 0, 500000000ull)) {
@@ -918,7 +918,7 @@ __global__ void __launch_bounds__(kTile, FV3D_TMA_MINBLOCKS) k_mx_sides_tma(cons
     mbar_wait_bounded(bar, 0, 500000000ull);
     return;
   }
-  sides_tile<MCF, GMODE, LINEAR, LIMIT, VISC>(a, smem, c0, tid);
+  sides_tile<MCF, GMODE, LINEAR, LIMIT, VISC, TL>(a, smem, c0, tid);
 }
 
 // ---------------------------------------------------------------------------

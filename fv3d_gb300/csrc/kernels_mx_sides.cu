@@ -16,6 +16,18 @@ static int g_sm_count = 0;  // multiprocessors of the device, read in setup_mx_s
 #ifndef FV3D_PERSIST_MAX_SMEM
 #define FV3D_PERSIST_MAX_SMEM (64 * 1024)
 #endif
+// cells per tile of the one-tile-per-CTA staged pass: 6- and 8-slot cells
+// take tiles of FV3D_WIDE_TILE (their 128-cell tiles fit 4 CTAs per
+// multiprocessor and leave a ragged last wave on meshes of a few hundred
+// thousand cells)
+#ifndef FV3D_WIDE_TILE
+#define FV3D_WIDE_TILE 64
+#endif
+template <int MCF>
+constexpr int wide_tile() {
+  return MCF >= 6 ? FV3D_WIDE_TILE : kTile;
+}
+
 template <int MCF, int G>
 constexpr bool sides_persistent() {
   return 2 * sides_buf_stride<MCF, G>() <= FV3D_PERSIST_MAX_SMEM;
@@ -29,7 +41,8 @@ static void launch_staged(const MxArgs& a, cudaStream_t s) {
     const int grid = std::min(ntiles, std::max(1, g_sm_count) * 4);
     k_mx_sides_tma2<MCF, G, L, M, V><<<grid, kTile, 2 * sides_buf_stride<MCF, G>(), s>>>(a);
   } else {
-    k_mx_sides_tma<MCF, G, L, M, V><<<a.ncp / kTile, kTile, SidesTile<MCF, G>::total, s>>>(a);
+    constexpr int TL = wide_tile<MCF>();
+    k_mx_sides_tma<MCF, G, L, M, V, TL><<<a.ncp / TL, TL, SidesTile<MCF, G, TL>::total, s>>>(a);
   }
 }
 
@@ -39,8 +52,8 @@ static cudaError_t staged_attr() {
     return cudaFuncSetAttribute(k_mx_sides_tma2<MCF, G, L, M, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 2 * sides_buf_stride<MCF, G>());
   else
-    return cudaFuncSetAttribute(k_mx_sides_tma<MCF, G, L, M, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                SidesTile<MCF, G>::total);
+    return cudaFuncSetAttribute(k_mx_sides_tma<MCF, G, L, M, V, wide_tile<MCF>()>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, SidesTile<MCF, G, wide_tile<MCF>()>::total);
 }
 #define MX_SIDES(G, L, M, V)                                              \
   do {                                                                   \

@@ -32,7 +32,8 @@ cudaError_t launch_mx_flux_update(const MxArgs& a, const Disc& d, int mode, bool
   const int B = (a.nc + 255) / 256;
   // 6- and 8-slot cells: blocks of FV3D_FLUX_WIDE_THREADS (their kernels keep
   // 64+ registers, so 256-thread blocks fit 3 per multiprocessor and leave
-  // a ragged last wave on meshes of a few hundred thousand cells)
+  // a ragged last wave on meshes of a few hundred thousand cells: the
+  // 262 k jittered hexes +13 % per stage with 64-thread blocks)
   const int BW = (a.nc + FV3D_FLUX_WIDE_THREADS - 1) / FV3D_FLUX_WIDE_THREADS;
   if (a.mcf == 4) flux_mcf<4>(a, d, mode, dt, co, s, B);
   else if (a.mcf == 6) flux_mcf<6>(a, d, mode, dt, co, s, BW, FV3D_FLUX_WIDE_THREADS);

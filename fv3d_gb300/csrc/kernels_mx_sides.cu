@@ -17,9 +17,9 @@ static int g_sm_count = 0;  // multiprocessors of the device, read in setup_mx_s
 #define FV3D_PERSIST_MAX_SMEM (64 * 1024)
 #endif
 // cells per tile of the one-tile-per-CTA staged pass: 6- and 8-slot cells
-// take tiles of FV3D_WIDE_TILE (their 128-cell tiles fit 4 CTAs per
-// multiprocessor and leave a ragged last wave on meshes of a few hundred
-// thousand cells)
+// take tiles of FV3D_WIDE_TILE (more, smaller CTAs per multiprocessor than
+// their 128-cell tiles allow; measured: the 577 k-cell mixed-element box
+// +0.8 %, the 262 k jittered hexes unchanged at 32, 64 or 128)
 #ifndef FV3D_WIDE_TILE
 #define FV3D_WIDE_TILE 64
 #endif

@@ -511,6 +511,48 @@ __global__ void __launch_bounds__(256, 4) k_cpl_product(int nc, const float* __r
   for (int j = 0; j < 5; ++j) y[(size_t)j * nc + c] = acc[j];
 }
 
+// the first damped sweep of P_R from zero for cell c: y = omega Dinv b
+// (k_cpl_sweep's arithmetic with x null)
+__device__ __forceinline__ void first_sweep(const float* __restrict__ Di, int nc, int c, float omega,
+                                            const float* b, float* __restrict__ y) {
+  float r[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  block_mul_add(Di + c, nc, b, r);
+#pragma unroll
+  for (int j = 0; j < 5; ++j) y[(size_t)j * nc + c] = 0.f + omega * r[j];
+}
+
+// the update pass of the inner Gram-Schmidt, per cell: v = (w - sum_i h_i
+// V_i) * s, s = 1 / |w - sum_i h_i V_i| (k_gs's PASS 3 arithmetic: the same
+// FP32 products and order, so the same values); with y0 set, the first
+// sweep of P_R on the new vector too
+__global__ void __launch_bounds__(256, 4) k_cpl_next(int nc, size_t ldb, const float* __restrict__ w,
+                                                  const float* __restrict__ V, int k, const double* __restrict__ h,
+                                                  const double* __restrict__ scale_p, float* __restrict__ vout,
+                                                  const float* __restrict__ Di, float omega,
+                                                  float* __restrict__ y0) {
+  __shared__ float hs[32];
+  if (threadIdx.x < 32) hs[threadIdx.x] = (threadIdx.x < (unsigned)k) ? (float)h[threadIdx.x] : 0.f;
+  __syncthreads();
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
+  float sum[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int i = 0; i < k; ++i) {
+    float a[5];
+    ld5(V + (size_t)i * ldb, nc, c, a);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) sum[j] = fmaf(hs[i], a[j], sum[j]);
+  }
+  const float scale = (float)*scale_p;
+  float v[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    const size_t e = (size_t)j * nc + c;
+    v[j] = (__ldg(w + e) - sum[j]) * scale;
+    vout[e] = v[j];
+  }
+  if (y0 != nullptr) first_sweep(Di, nc, c, omega, v, y0);
+}
+
 // P_A written out as blocks (for the block export), by the product's own
 // arithmetic: column j of the diagonal block is the response to x_c = e_j,
 // of slot k's block the response of that slot to x_o = e_j
@@ -579,12 +621,23 @@ __global__ void __launch_bounds__(256) k_cpl_sweep(int nc, const float* __restri
   for (int j = 0; j < 5; ++j) y[(size_t)j * nc + c] = (TO)(xc[j] + omega * (r[j] - xc[j]));
 }
 
-// V_0 = v / |v| (the inverse norm from a device slot), stored FP32
+// V_0 = v / |v| (the inverse norm from a device slot), stored FP32, per
+// cell, and the first sweep of P_R on it into y0
 template <class T>
-__global__ void k_cpl_start(size_t n, const T* __restrict__ v, const double* __restrict__ inv, float* __restrict__ V0) {
+__global__ void __launch_bounds__(256) k_cpl_start(int nc, const T* __restrict__ v, const double* __restrict__ inv,
+                                                   float* __restrict__ V0, const float* __restrict__ Di, float omega,
+                                                   float* __restrict__ y0) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc) return;
   const double s = *inv;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    V0[i] = (float)((double)v[i] * s);
+  float b[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    const size_t e = (size_t)j * nc + c;
+    b[j] = (float)((double)v[e] * s);
+    V0[e] = b[j];
+  }
+  first_sweep(Di, nc, c, omega, b, y0);
 }
 
 // the inner least-squares problem min |beta e_1 - H y| by Givens rotations
@@ -710,14 +763,16 @@ fv3d_status Coupled::build(Ctx& ctx, Implicit& im) {
   return FV3D_OK;
 }
 
-// out = M_R b: `count` block-Jacobi sweeps of P_R from zero
+// out = M_R b: `count` damped block-Jacobi sweeps of P_R from zero, the
+// first of them (omega Dinv b) already in x0, written by the pass that
+// formed b (x0 is out itself for one sweep)
 template <class TO>
-fv3d_status Coupled::sweeps(Ctx& ctx, int count, const float* b, TO* out) {
+fv3d_status Coupled::sweeps(Ctx& ctx, int count, const float* b, const float* x0, TO* out) {
   const int g = nblk(nc);
   const float gm1 = (float)ctx.phys.km1;
   // the sweeps alternate between ti and wi, the last one writes out; b is never overwritten
-  const float* x = nullptr;
-  for (int s = 0; s < count; ++s) {
+  const float* x = x0;
+  for (int s = 1; s < count; ++s) {
     const bool last = (s == count - 1);
     float* tmp = (s % 2 == 0) ? ti.p : wi.p;
 #define CPL_SWEEP(M)                                                                                     \
@@ -742,15 +797,18 @@ fv3d_status Coupled::apply(Ctx& ctx, Implicit& im, const T* v, T* z) {
   // |v| (FP64 for a FP64 input, FP32 otherwise) and V_0 = v / |v|
   fv3d_status st = im.gs_pass<T>(ctx, 0, const_cast<T*>(v), v, 1, nullptr, hb, 1.0, nullptr);
   if (st != FV3D_OK) return st;
-  k_cpl_start<T><<<std::min(4096, nblk(n)), 256, 0, ctx.stream>>>(n, v, hb + 1, Vi.p);
-  CCK(cudaGetLastError());
   const int g = nblk(nc);
+  // the first sweep of each v_j is made by the pass that forms v_j, into ti
+  // (into t_j itself with one sweep)
+  auto first = [&](int j) { return sw == 1 ? Ti.p + (size_t)j * ldb : ti.p; };
+  k_cpl_start<T><<<g, 256, 0, ctx.stream>>>(nc, v, hb + 1, Vi.p, PRi.p, omega, first(0));
+  CCK(cudaGetLastError());
   for (int j = 0; j < m; ++j) {
     float* vj = Vi.p + (size_t)j * ldb;
     double* hc = hin.p + (size_t)j * kHcol;
     // t_j = M_R v_j (kept: the inner solve is flexible), w = P_A t_j
     float* tj = Ti.p + (size_t)j * ldb;
-    if ((st = sweeps<float>(ctx, sw, vj, tj)) != FV3D_OK) return st;
+    if ((st = sweeps<float>(ctx, sw, vj, first(j), tj)) != FV3D_OK) return st;
 #define CPL_PRODUCT(M)                                                                                      \
   k_cpl_product<M><<<g, 256, 0, ctx.stream>>>(nc, cst.p, idt.p, pna.p, nbr.p, gst.p, gjac.p, rusanov, gam, gm1, \
                                               tj, wi.p)
@@ -760,13 +818,20 @@ fv3d_status Coupled::apply(Ctx& ctx, Implicit& im, const T* v, T* z) {
 #undef CPL_PRODUCT
     CCK(cudaGetLastError());
     // classical Gram-Schmidt once (dots and |w|^2 in one pass, the norm of
-    // the projected w by Pythagoras), v_{j+1} = w / |w|, FP32: a short
-    // inner solve that only preconditions needs no re-orthogonalisation
+    // the projected w by Pythagoras), FP32: a short inner solve that only
+    // preconditions needs no re-orthogonalisation.  (The dots summed inside
+    // the product's pass instead made that pass longer than the two apart:
+    // 617 against 555 ms for the channel's solve.)
     if ((st = im.gs_pass<float>(ctx, 4, wi.p, Vi.p, j + 1, nullptr, hc, 0.0, nullptr, nullptr, hc + 64)) != FV3D_OK)
       return st;
-    if ((st = im.gs_pass<float>(ctx, 3, wi.p, Vi.p, j + 1, hc, nullptr, 0.0, nullptr, nullptr, nullptr,
-                                Vi.p + (size_t)(j + 1) * ldb, hc + 65)) != FV3D_OK)
-      return st;
+    // v_{j+1} = (w - sum_i h_i v_i) / its norm, and its first sweep; the
+    // last iteration's is never used (the least-squares problem takes only
+    // the norm)
+    if (j + 1 < m) {
+      k_cpl_next<<<g, 256, 0, ctx.stream>>>(nc, ldb, wi.p, Vi.p, j + 1, hc, hc + 65, Vi.p + (size_t)(j + 1) * ldb,
+                                            PRi.p, omega, first(j + 1));
+      CCK(cudaGetLastError());
+    }
   }
   k_cpl_lsq<<<1, 32, 0, ctx.stream>>>(m, hin.p);
   // z = sum_j y_j t_j

@@ -31,6 +31,7 @@
 #include "context.h"
 #include "implicit.h"
 #include "fo_flux.cuh"
+#include "gs_reduce.cuh"
 
 namespace fv3d {
 
@@ -186,66 +187,7 @@ __device__ __forceinline__ void st_group(T* p, const T* x) {
 //           solves of the coupled preconditioner): the last block forms
 //           |w - sum_j h_j V_j| by Pythagoras; PASS 3 follows with h
 // Products and sums in T (FP32 basis: FP32 pipe), the final sums and the
-// coefficients in FP64.
-template <class T>
-__device__ void gs_finalize(const T* __restrict__ partial, int nb, int k, double* __restrict__ out, bool norm,
-                            double c, unsigned int* counter, double* __restrict__ out2 = nullptr) {
-  __shared__ bool last;
-  // the threads that wrote this block's partials make them visible, then
-  // one thread takes the ticket
-  if (threadIdx.x < 32) __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  // one warp per column: each lane sums a fixed set of block partials
-  // (independent loads), then a fixed xor tree
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int j = warp; j < k; j += 8) {
-    T s0 = T(0), s1 = T(0);
-    int b = lane;
-    for (; b + 32 < nb; b += 64) {
-      s0 += __ldcg(partial + (size_t)b * 32 + j);
-      s1 += __ldcg(partial + (size_t)(b + 32) * 32 + j);
-    }
-    if (b < nb) s0 += __ldcg(partial + (size_t)b * 32 + j);
-    T v = s0 + s1;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) {
-      const double t = (double)v;
-      if (norm) {
-        const double r = sqrt(t);
-        out[0] = r;
-        out[1] = (r > 0.0) ? 1.0 / r : 0.0;
-        out[2] = (r > 0.0) ? c / r : 0.0;
-        out[3] = (r > 0.0) ? r / c : 0.0;
-      } else {
-        out[j] = t;
-      }
-    }
-  }
-  if (out2 != nullptr) {
-    // column 31: |w|^2; the norm of w - sum_j out_j V_j by Pythagoras
-    __syncthreads();
-    if (warp == 0) {
-      T s0 = T(0);
-      for (int b = lane; b < nb; b += 32) s0 += __ldcg(partial + (size_t)b * 32 + 31);
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s0 += __shfl_xor_sync(0xffffffffu, s0, o);
-      if (lane == 0) {
-        double hh = 0.0;
-        for (int j = 0; j < k; ++j) hh += out[j] * out[j];
-        const double b2 = (double)s0 - hh;
-        const double r = (b2 > 0.0) ? sqrt(b2) : 0.0;
-        out2[0] = r;
-        out2[1] = (r > 0.0) ? 1.0 / r : 0.0;
-      }
-    }
-  }
-  if (threadIdx.x == 0) *counter = 0u;  // ready for the next pass
-}
+// coefficients in FP64 (gs_finalize, gs_reduce.cuh).
 
 // w = z / dt_i - (R(U + eps z) - R(U)) / eps (k_jv_combine's arithmetic),
 // formed inside the first Gram-Schmidt pass when z is set

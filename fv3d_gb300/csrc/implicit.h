@@ -67,7 +67,7 @@ struct Coupled {
   template <class T>
   fv3d_status apply(Ctx& ctx, Implicit& im, const T* v, T* z);
   template <class TO>
-  fv3d_status sweeps(Ctx& ctx, int count, const float* b, TO* out);
+  fv3d_status sweeps(Ctx& ctx, int count, const float* b, const float* x0, TO* out);
 };
 
 struct Implicit {

@@ -641,59 +641,92 @@ __global__ void __launch_bounds__(256) k_cpl_start(int nc, const T* __restrict__
 }
 
 // the inner least-squares problem min |beta e_1 - H y| by Givens rotations
-// (FP32, one thread, H in shared memory): H from the Gram-Schmidt passes'
-// columns, y [m] into hin + m * kHcol + 8; the columns past a breakdown (a
-// zero subdiagonal or a zero or non-finite rotation) get y = 0
+// (FP32, H in shared memory): H from the Gram-Schmidt passes' columns, y [m]
+// into hin + m * kHcol + 8; the columns past a breakdown (a zero
+// subdiagonal or a zero or non-finite rotation) get y = 0.  One thread per
+// column, in rounds: round r forms rotation r from column r (which has had
+// rotations 0 .. r-1) and the columns past r apply it, so each column sees
+// its rotations in the serial order; the back substitution is serial.
+// Launched with at least m * 31 threads (one load each), a multiple of 32.
 __global__ void k_cpl_lsq(int m, double* __restrict__ hin) {
   __shared__ float H[30][31];
   __shared__ float cs[30], sn[30], g[31], y[30];
+  __shared__ int kk_s, stop;
   const int t = threadIdx.x;
-  // the columns, loaded by the block (one Gram-Schmidt pass: h at [0, 32))
+  // the columns (one Gram-Schmidt pass: h at [0, 32), the norm at 64)
   for (int q = t; q < m * 31; q += blockDim.x) {
     const int j = q / 31, i = q % 31;
     const double* hc = hin + (size_t)j * kHcol;
     H[j][i] = (i <= j) ? (float)hc[i] : (i == j + 1 ? (float)hc[64] : 0.f);
   }
+  if (t <= m) g[t] = (t == 0) ? (float)hin[(size_t)m * kHcol] : 0.f;  // |v| from the norm pass
+  if (t == 0) {
+    kk_s = 0;
+    stop = 0;
+  }
   __syncthreads();
-  if (t != 0) return;
-  for (int i = 0; i <= m; ++i) g[i] = 0.f;
-  g[0] = (float)hin[(size_t)m * kHcol];  // |v| from the norm pass
-  int kk = 0;
-  for (int j = 0; j < m; ++j) {
-    const float hn = H[j][j + 1];
-    for (int i = 0; i < j; ++i) {
-      const float a0 = H[j][i], b0 = H[j][i + 1];
-      H[j][i] = cs[i] * a0 + sn[i] * b0;
-      H[j][i + 1] = -sn[i] * a0 + cs[i] * b0;
+  for (int r = 0; r < m; ++r) {
+    if (t == r) {
+      const float hn = H[r][r + 1];
+      const float a0 = H[r][r], b0 = H[r][r + 1];
+      const float rr = sqrtf(a0 * a0 + b0 * b0);
+      if (!(rr > 0.f) || !isfinite(rr)) {
+        stop = 1;
+      } else {
+        cs[r] = a0 / rr;
+        sn[r] = b0 / rr;
+        H[r][r] = rr;
+        g[r + 1] = -sn[r] * g[r];
+        g[r] = cs[r] * g[r];
+        kk_s = r + 1;
+        if (!(hn > 0.f)) stop = 1;  // the Krylov space is invariant: exact solution
+      }
     }
-    const float a0 = H[j][j], b0 = H[j][j + 1];
-    const float r = sqrtf(a0 * a0 + b0 * b0);
-    if (!(r > 0.f) || !isfinite(r)) break;
-    cs[j] = a0 / r;
-    sn[j] = b0 / r;
-    H[j][j] = r;
-    g[j + 1] = -sn[j] * g[j];
-    g[j] = cs[j] * g[j];
-    kk = j + 1;
-    if (!(hn > 0.f)) break;  // the Krylov space is invariant: exact solution
+    __syncthreads();
+    if (stop) break;  // the same value in every thread
+    if (t > r && t < m) {
+      const float a0 = H[t][r], b0 = H[t][r + 1];
+      H[t][r] = cs[r] * a0 + sn[r] * b0;
+      H[t][r + 1] = -sn[r] * a0 + cs[r] * b0;
+    }
+    __syncthreads();
   }
-  for (int i = kk - 1; i >= 0; --i) {
-    float s = g[i];
-    for (int j = i + 1; j < kk; ++j) s -= H[j][i] * y[j];
-    y[i] = s / H[i][i];
+  const int kk = kk_s;
+  if (t == 0) {
+    for (int i = kk - 1; i >= 0; --i) {
+      float s = g[i];
+      for (int j = i + 1; j < kk; ++j) s -= H[j][i] * y[j];
+      y[i] = s / H[i][i];
+    }
   }
-  double* out = hin + (size_t)m * kHcol + 8;
-  for (int i = 0; i < m; ++i) out[i] = (i < kk) ? (double)y[i] : 0.0;
+  __syncthreads();
+  if (t < m) hin[(size_t)m * kHcol + 8 + t] = (t < kk) ? (double)y[t] : 0.0;
 }
 
-// u = sum_j y_j T_j (FP32 directions, ldb apart)
+// u = sum_j y_j T_j (FP32 directions, ldb apart: 16-byte aligned), four
+// consecutive elements per thread with 16-byte loads, then the n % 4 tail
 template <class TO>
 __global__ void k_cpl_combine(size_t n, size_t ldb, const float* __restrict__ V, const double* __restrict__ y, int m,
                               TO* __restrict__ u) {
   __shared__ float ys[32];
   if (threadIdx.x < 32) ys[threadIdx.x] = (threadIdx.x < (unsigned)m) ? (float)y[threadIdx.x] : 0.f;
   __syncthreads();
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x, gid = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+  const size_t nq = n / 4;
+  for (size_t q = gid; q < nq; q += stride) {
+    float s[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll 4
+    for (int j = 0; j < m; ++j) {
+      const float4 v = __ldg(reinterpret_cast<const float4*>(V + (size_t)j * ldb) + q);
+      s[0] = fmaf(ys[j], v.x, s[0]);
+      s[1] = fmaf(ys[j], v.y, s[1]);
+      s[2] = fmaf(ys[j], v.z, s[2]);
+      s[3] = fmaf(ys[j], v.w, s[3]);
+    }
+#pragma unroll
+    for (int l = 0; l < 4; ++l) u[4 * q + l] = (TO)s[l];
+  }
+  for (size_t i = 4 * nq + gid; i < n; i += stride) {
     float s = 0.f;
     for (int j = 0; j < m; ++j) s = fmaf(ys[j], __ldg(V + (size_t)j * ldb + i), s);
     u[i] = (TO)s;
@@ -833,9 +866,9 @@ fv3d_status Coupled::apply(Ctx& ctx, Implicit& im, const T* v, T* z) {
       CCK(cudaGetLastError());
     }
   }
-  k_cpl_lsq<<<1, 32, 0, ctx.stream>>>(m, hin.p);
+  k_cpl_lsq<<<1, (m * 31 + 31) / 32 * 32, 0, ctx.stream>>>(m, hin.p);
   // z = sum_j y_j t_j
-  k_cpl_combine<T><<<std::min(4096, nblk(n)), 256, 0, ctx.stream>>>(n, ldb, Ti.p, hb + 8, m, z);
+  k_cpl_combine<T><<<std::min(4096, nblk((n + 3) / 4)), 256, 0, ctx.stream>>>(n, ldb, Ti.p, hb + 8, m, z);
   CCK(cudaGetLastError());
   return FV3D_OK;
 }

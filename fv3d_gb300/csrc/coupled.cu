@@ -41,6 +41,7 @@
 #include <vector>
 
 #include "context.h"
+#include "block5.cuh"
 #include "fo_flux.cuh"
 #include "implicit.h"
 
@@ -70,7 +71,8 @@ __global__ void k_cpl_nbr(int nc, int mcf, int nf_int, const int* __restrict__ c
 
 // Euler flux Jacobian d(F.n)/dU (row-major) of a conserved state, with
 // |u.n| + c and rho
-__device__ void euler_jacobian(const double* U, const double* n, double kappa, double* A, double* lam) {
+__device__ __forceinline__ void euler_jacobian(const double* U, const double* n, double kappa, double* A,
+                                               double* lam) {
   const double rho = U[0], ir = 1.0 / rho;
   const double u[3] = {U[1] * ir, U[2] * ir, U[3] * ir};
   const double q2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
@@ -81,16 +83,29 @@ __device__ void euler_jacobian(const double* U, const double* n, double kappa, d
   A[0] = 0.0;
   A[1] = n[0]; A[2] = n[1]; A[3] = n[2];
   A[4] = 0.0;
+#pragma unroll
   for (int i = 0; i < 3; ++i) {
     A[(1 + i) * 5] = phi * n[i] - u[i] * un;
+#pragma unroll
     for (int j = 0; j < 3; ++j)
       A[(1 + i) * 5 + 1 + j] = u[i] * n[j] - (kappa - 1.0) * u[j] * n[i] + (i == j ? un : 0.0);
     A[(1 + i) * 5 + 4] = (kappa - 1.0) * n[i];
   }
   A[20] = un * (phi - H);
+#pragma unroll
   for (int j = 0; j < 3; ++j) A[21 + j] = H * n[j] - (kappa - 1.0) * u[j] * un;
   A[24] = kappa * un;
   *lam = fabs(un) + sqrt(kappa * fmax(p, 1.00E-10) * ir);
+}
+
+// |u.n| + c of a conserved state (euler_jacobian's lam, the same arithmetic)
+__device__ __forceinline__ double wave_speed(const double* U, const double* n, double kappa) {
+  const double rho = U[0], ir = 1.0 / rho;
+  const double u[3] = {U[1] * ir, U[2] * ir, U[3] * ir};
+  const double q2 = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+  const double p = (kappa - 1.0) * (U[4] - 0.5 * rho * q2);
+  const double un = u[0] * n[0] + u[1] * n[1] + u[2] * n[2];
+  return fabs(un) + sqrt(kappa * fmax(p, 1.00E-10) * ir);
 }
 
 __device__ __forceinline__ void store_block(float* __restrict__ dst, size_t nc, const double* B) {
@@ -292,35 +307,6 @@ __device__ __forceinline__ void slot_jvp(const float4 c0, const float4 c1, const
   for (int j = 0; j < 5; ++j) acc[j] = fmaf(na.w, dF[j], acc[j]);
 }
 
-// 5x5 inverse (row-major, FP64 Gauss-Jordan with partial pivoting); false
-// when singular
-__device__ bool invert5(const double* B, double* X) {
-  double M[5][10];
-  for (int i = 0; i < 5; ++i)
-    for (int j = 0; j < 5; ++j) {
-      M[i][j] = B[i * 5 + j];
-      M[i][5 + j] = (i == j) ? 1.0 : 0.0;
-    }
-  for (int col = 0; col < 5; ++col) {
-    int piv = col;
-    for (int i = col + 1; i < 5; ++i)
-      if (fabs(M[i][col]) > fabs(M[piv][col])) piv = i;
-    if (!(fabs(M[piv][col]) > 1e-300)) return false;
-    if (piv != col)
-      for (int j = 0; j < 10; ++j) { const double t = M[col][j]; M[col][j] = M[piv][j]; M[piv][j] = t; }
-    const double ip = 1.0 / M[col][col];
-    for (int j = 0; j < 10; ++j) M[col][j] *= ip;
-    for (int i = 0; i < 5; ++i) {
-      if (i == col) continue;
-      const double fct = M[i][col];
-      for (int j = 0; j < 10; ++j) M[i][j] -= fct * M[col][j];
-    }
-  }
-  for (int i = 0; i < 5; ++i)
-    for (int j = 0; j < 5; ++j) X[i * 5 + j] = M[i][5 + j];
-  return true;
-}
-
 // P_R's slot blocks are applied without being stored: the block of slot k
 // is a_k A(U_o) + b_k I (the Euler flux Jacobian of the neighbour's state
 // along the face normal, a and b from the face's area, volume, wave speed and
@@ -344,13 +330,64 @@ __device__ __forceinline__ void rus_jx(const float4 st, float gm1, const float4 
   y[4] = st.w * q + un * (dp + x[4]);
 }
 
+// P_R's diagonal block of each boundary face per unit weight (s A / V):
+// (A(U_c) + lam I) / 2 + (A(U_g) - lam I) / 2 . d ghost / d U_c, the ghost's
+// dependence on its cell by forward differences of update_boundaries
+// (boundary.c:188-320) in FP64, row-major [nb][25].  Apart from the cell
+// pass so that the boundary arithmetic does not set that pass's register
+// budget.
+__global__ void __launch_bounds__(128) k_cpl_build_bnd(KArgs<double> a, double* __restrict__ bpr) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= a.nf - a.nf_int) return;
+  const int f = a.nf_int + b, c = a.fc0[f];  // a boundary face's cell is its cell 0
+  const size_t nc = a.nc;
+  Phys<double> ph;
+  ph.load(a.pc);
+  const double kappa = a.pc.kappa;
+  double qc[10];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) qc[j] = a.U[(size_t)j * nc + c];
+  cons_to_prims(qc, ph);
+  const double* g = a.geo + (size_t)f * GEO;
+  double n[4];
+  face_normal(g, true, n);
+  double Ac[25], lc;
+  euler_jacobian(qc, n, kappa, Ac, &lc);
+  const int region = a.fregion[b];
+  double qg[10], Ag[25], lg;
+  ghost_state(qc, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qg);
+  euler_jacobian(qg, n, kappa, Ag, &lg);
+  const double lam = fmax(lc, lg) + 2.0 * a.pc.mu / (qc[0] * n[3]);
+  double* out = bpr + 25 * (size_t)b;
+  for (int v = 0; v < 5; ++v) {
+    // column v of d ghost / d U_c, then column v of the block
+    const double h = 1e-7 * fmax(fabs(qc[v]), 1e-3);
+    double qp[10], qh[10], G[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) qp[j] = qc[j];
+    qp[v] += h;
+    cons_to_prims(qp, ph);
+    ghost_state(qp, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qh);
+#pragma unroll
+    for (int i = 0; i < 5; ++i) G[i] = (qh[i] - qg[i]) / h;
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+      double s = 0.5 * (Ac[i * 5 + v] + (i == v ? lam : 0.0));
+#pragma unroll
+      for (int l = 0; l < 5; ++l) s += 0.5 * (Ag[i * 5 + l] - (i == l ? lam : 0.0)) * G[l];
+      out[i * 5 + v] = s;
+    }
+  }
+}
+
 // P_R: the inverted diagonal blocks (FP64 Gauss-Jordan, stored FP32), the
 // slot coefficients of the matrix-free off-diagonal blocks and the cell's
 // (u, v, w, H)
 template <int MCF>
 __global__ void __launch_bounds__(128) k_cpl_build_pr(KArgs<double> a, const double* __restrict__ dtl,
-                                                      float* __restrict__ PRi, float4* __restrict__ rna,
-                                                      float* __restrict__ rb, float4* __restrict__ st4) {
+                                                      const double* __restrict__ bpr, float* __restrict__ PRi,
+                                                      float4* __restrict__ rna, float* __restrict__ rb,
+                                                      float4* __restrict__ st4) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.nc) return;
   const size_t nc = a.nc;
@@ -383,15 +420,14 @@ __global__ void __launch_bounds__(128) k_cpl_build_pr(KArgs<double> a, const dou
     double n[4];
     face_normal(g, bnd, n);
     const double w = (side ? -1.0 : 1.0) * g[G_A] * iv;
-    double Ac[25], lc;
-    euler_jacobian(qc, n, kappa, Ac, &lc);
     if (!bnd) {
+      double Ac[25], lc;
+      euler_jacobian(qc, n, kappa, Ac, &lc);
       const int o = side ? a.fc0[f] : a.fc1[f];
       double qo[5];
 #pragma unroll
       for (int j = 0; j < 5; ++j) qo[j] = a.U[(size_t)j * nc + o];
-      double Ao[25], lo;
-      euler_jacobian(qo, n, kappa, Ao, &lo);
+      const double lo = wave_speed(qo, n, kappa);
       const double lam = fmax(lc, lo) + 2.0 * mu / (0.5 * (qc[0] + qo[0]) * n[3]);
       // own: cell 0 -> (A + lam I) / 2, cell 1 -> (A - lam I) / 2; the other the opposite
       const double so = side ? -lam : lam;
@@ -400,34 +436,10 @@ __global__ void __launch_bounds__(128) k_cpl_build_pr(KArgs<double> a, const dou
       rna[sk] = make_float4((float)n[0], (float)n[1], (float)n[2], (float)(0.5 * w));
       rb[sk] = (float)(-0.5 * w * so);
     } else {
-      const int region = a.fregion[f - a.nf_int];
-      double qg[10], Ag[25], lg;
-      ghost_state(qc, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qg);
-      euler_jacobian(qg, n, kappa, Ag, &lg);
-      const double lam = fmax(lc, lg) + 2.0 * mu / (qc[0] * n[3]);
-      // d ghost / d U_c by forward differences
-      double G[25];
-      for (int v = 0; v < 5; ++v) {
-        const double h = 1e-7 * fmax(fabs(qc[v]), 1e-3);
-        double qp[10], qh[10];
+      // the face's block per unit weight, formed by k_cpl_build_bnd
+      const double* sb = bpr + 25 * (size_t)(f - a.nf_int);
 #pragma unroll
-        for (int j = 0; j < 5; ++j) qp[j] = qc[j];
-        qp[v] += h;
-        cons_to_prims(qp, ph);
-        ghost_state(qp, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qh);
-#pragma unroll
-        for (int i = 0; i < 5; ++i) G[i * 5 + v] = (qh[i] - qg[i]) / h;
-      }
-#pragma unroll
-      for (int i = 0; i < 5; ++i) {
-#pragma unroll
-        for (int j = 0; j < 5; ++j) {
-          double s = 0.5 * (Ac[i * 5 + j] + (i == j ? lam : 0.0));
-#pragma unroll
-          for (int l = 0; l < 5; ++l) s += 0.5 * (Ag[i * 5 + l] - (i == l ? lam : 0.0)) * G[l * 5 + j];
-          D[i * 5 + j] += w * s;
-        }
-      }
+      for (int e2 = 0; e2 < 25; ++e2) D[e2] += w * sb[e2];
       rna[sk] = make_float4(0.f, 0.f, 0.f, 0.f);
       rb[sk] = 0.f;
     }
@@ -762,6 +774,7 @@ fv3d_status Coupled::setup(Ctx& ctx, Implicit& im, int m_inner, int n_sweeps, fl
   if (e == cudaSuccess) e = pna.alloc((size_t)mcf * nc);
   if (e == cudaSuccess) e = gst.alloc(8 * (size_t)nb);
   if (e == cudaSuccess) e = gjac.alloc(25 * (size_t)nb);
+  if (e == cudaSuccess) e = bpr.alloc(25 * (size_t)std::max(nb, 1));
   if (e == cudaSuccess) e = PRi.alloc(25 * (size_t)nc);
   if (e == cudaSuccess) e = rna.alloc((size_t)mcf * nc);
   if (e == cudaSuccess) e = rb.alloc((size_t)mcf * nc);
@@ -785,9 +798,10 @@ fv3d_status Coupled::setup(Ctx& ctx, Implicit& im, int m_inner, int n_sweeps, fl
 fv3d_status Coupled::build(Ctx& ctx, Implicit& im) {
   KArgs<double> a = ctx.args<double>();
   const int g = nblk(nc, 128);
+  if (nb > 0) k_cpl_build_bnd<<<nblk(nb, 128), 128, 0, ctx.stream>>>(a, bpr.p);
 #define CPL_BUILD(M)                                                                           \
   k_cpl_build_state<M><<<g, 128, 0, ctx.stream>>>(a, im.dtl.p, cst.p, idt.p, pna.p, gst.p, gjac.p); \
-  k_cpl_build_pr<M><<<g, 128, 0, ctx.stream>>>(a, im.dtl.p, PRi.p, rna.p, rb.p, st4.p)
+  k_cpl_build_pr<M><<<g, 128, 0, ctx.stream>>>(a, im.dtl.p, bpr.p, PRi.p, rna.p, rb.p, st4.p)
   if (mcf == 4) { CPL_BUILD(4); }
   else if (mcf == 6) { CPL_BUILD(6); }
   else { CPL_BUILD(8); }

@@ -30,6 +30,7 @@
 
 #include "context.h"
 #include "implicit.h"
+#include "block5.cuh"
 #include "fo_flux.cuh"
 #include "gs_reduce.cuh"
 
@@ -533,36 +534,23 @@ __global__ void k_add_diag(int nc, const double* __restrict__ dtl, double* __res
   for (int j = 0; j < 5; ++j) D[(size_t)c * 25 + j * 5 + j] += idt;
 }
 
-// 5x5 inverse by Gauss-Jordan with partial pivoting (FP64), stored FP32;
-// a singular block falls back to the inverse of its diagonal.
-__global__ void k_block_invert(int nc, const double* __restrict__ D, float* __restrict__ Dinv) {
+// 5x5 inverse by Gauss-Jordan with partial pivoting (FP64, invert5),
+// stored FP32; a singular block falls back to the inverse of its diagonal.
+// Blocks column-major.
+__global__ void __launch_bounds__(128) k_block_invert(int nc, const double* __restrict__ D, float* __restrict__ Dinv) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
-  double M[5][10];
+  double B[25], X[25];
+#pragma unroll
   for (int i = 0; i < 5; ++i)
-    for (int j = 0; j < 5; ++j) {
-      M[i][j] = D[(size_t)c * 25 + j * 5 + i];  // column-major -> row i, col j
-      M[i][5 + j] = (i == j) ? 1.0 : 0.0;
-    }
-  bool ok = true;
-  for (int col = 0; col < 5; ++col) {
-    int piv = col;
-    for (int i = col + 1; i < 5; ++i)
-      if (fabs(M[i][col]) > fabs(M[piv][col])) piv = i;
-    if (!(fabs(M[piv][col]) > 1e-300)) { ok = false; break; }
-    if (piv != col)
-      for (int j = 0; j < 10; ++j) { double t = M[col][j]; M[col][j] = M[piv][j]; M[piv][j] = t; }
-    const double ip = 1.0 / M[col][col];
-    for (int j = 0; j < 10; ++j) M[col][j] *= ip;
-    for (int i = 0; i < 5; ++i) {
-      if (i == col) continue;
-      const double fct = M[i][col];
-      for (int j = 0; j < 10; ++j) M[i][j] -= fct * M[col][j];
-    }
-  }
+#pragma unroll
+    for (int j = 0; j < 5; ++j) B[i * 5 + j] = D[(size_t)c * 25 + j * 5 + i];  // column-major -> row-major
+  const bool ok = invert5(B, X);
+#pragma unroll
   for (int i = 0; i < 5; ++i)
+#pragma unroll
     for (int j = 0; j < 5; ++j) {
-      double v = ok ? M[i][5 + j] : ((i == j) ? 1.0 / D[(size_t)c * 25 + i * 5 + i] : 0.0);
+      const double v = ok ? X[i * 5 + j] : ((i == j) ? 1.0 / B[i * 5 + i] : 0.0);
       Dinv[(size_t)c * 25 + j * 5 + i] = (float)v;  // column-major
     }
 }

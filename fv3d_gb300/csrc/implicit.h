@@ -58,6 +58,7 @@ struct Coupled {
   DevBuf<float> cst, idt, gst, gjac;
   DevBuf<float4> pna;
   DevBuf<float> PRi;               // P_R: inverted diagonal blocks [25][nc]; its slot blocks are applied
+  DevBuf<double> bpr;              // P_R: each boundary face's diagonal block per unit weight [nb][25]
   DevBuf<float4> rna, st4;         // matrix-free: per slot (normal, a) [mcf][nc], per cell (u, v, w, H)
   DevBuf<float> rb;                // per slot b [mcf][nc]
   DevBuf<float> Vi, Ti, wi, ti;    // inner basis [(m_in + 1)][ldb], directions [m_in][ldb], work [ldb]

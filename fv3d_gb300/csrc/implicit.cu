@@ -186,7 +186,8 @@ __device__ __forceinline__ void st_group(T* p, const T* x) {
 //   PASS 0  |w| alone
 //   PASS 4  h_j = w . V_j and |w|^2 (one Gram-Schmidt pass, for the inner
 //           solves of the coupled preconditioner): the last block forms
-//           |w - sum_j h_j V_j| by Pythagoras; PASS 3 follows with h
+//           |w - sum_j h_j V_j| by Pythagoras (the next vector is then
+//           formed per cell by the coupled preconditioner's k_cpl_next)
 // Products and sums in T (FP32 basis: FP32 pipe), the final sums and the
 // coefficients in FP64 (gs_finalize, gs_reduce.cuh).
 

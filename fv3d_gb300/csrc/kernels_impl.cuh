@@ -8,10 +8,19 @@ namespace fv3d {
 
 static inline int blocks_for(int n, int t) { return (n + t - 1) / t; }
 
+// FP64 kernels in blocks of 64: at 140-170 registers a 256-thread block
+// fits once per multiprocessor (8 warps); 64-thread blocks fit 6-7 times
+// (measured, FP64 RK3 steps: tets +14 %, jittered hexes +9 %, the channel
+// +10 %).  Every cell's and face's arithmetic is its own, so the results
+// do not depend on the block size.
+#ifndef FV3D_F64_THREADS
+#define FV3D_F64_THREADS 64
+#endif
+
 template <class R>
 cudaError_t launch_gradients(const KArgs<R>& a, const Disc& d, cudaStream_t s) {
   constexpr bool K = sizeof(R) == 4;
-  const int T = 256, B = blocks_for(a.nc, T);
+  const int T = sizeof(R) == 8 ? FV3D_F64_THREADS : 256, B = blocks_for(a.nc, T);
   const bool lim = d.linear && d.limit;
   if (d.gmode == 0) k_gradients<R, 0, false, K><<<B, T, 0, s>>>(a);
   else if (d.gmode == 1) {
@@ -26,7 +35,7 @@ cudaError_t launch_gradients(const KArgs<R>& a, const Disc& d, cudaStream_t s) {
 
 template <class R>
 cudaError_t launch_face_flux(const KArgs<R>& a, const Disc& d, cudaStream_t s) {
-  const int T = 256, B = blocks_for(a.nf, T);
+  const int T = sizeof(R) == 8 ? FV3D_F64_THREADS : 256, B = blocks_for(a.nf, T);
   const bool lim = d.linear && d.limit;
   if (d.linear) {
     if (lim) {
@@ -46,7 +55,7 @@ cudaError_t launch_face_flux(const KArgs<R>& a, const Disc& d, cudaStream_t s) {
 template <class R>
 cudaError_t launch_gather(const KArgs<R>& a, int mode, bool dt, const StageCoef& co, cudaStream_t s) {
   constexpr bool K = sizeof(R) == 4;
-  const int T = 256, B = blocks_for(a.nc, T);
+  const int T = sizeof(R) == 8 ? FV3D_F64_THREADS : 256, B = blocks_for(a.nc, T);
   if (mode == 0) k_gather_update<R, 0, K, false><<<B, T, 0, s>>>(a, co);
   else if (mode == 1) {
     if (dt) k_gather_update<R, 1, K, true><<<B, T, 0, s>>>(a, co);

@@ -301,7 +301,7 @@ KArgs<R> Ctx::args() const {
   a.geo = (const R*)d_geo.p; a.lam = (const R*)d_lam.p; a.lsq = (const R*)d_lsq.p;
   a.fregion = d_fregion.p; a.cface = d_cface.p; a.rvol = (const R*)d_rvol.p;
   a.vol = d_vol.p; a.dx = d_dx.p;
-  a.U = d_U.p; a.K = d_K.p; a.U0 = d_U0.p; a.Uf = d_Uf.p;
+  a.U = d_U.p; a.Pq = d_Pq.p; a.K = d_K.p; a.U0 = d_U0.p; a.Uf = d_Uf.p;
   a.rec = (R*)d_rec.p; a.FA = (R*)d_FA.p; a.dphi = d_dphi.p; a.sc = d_sc.p;
   a.pc = phys;
   return a;

@@ -67,6 +67,7 @@ struct Ctx {
   DevBuf<double> d_vol, d_dx;
   // device solution data
   DevBuf<double> d_U, d_K, d_U0, d_dphi, d_stage, d_part;
+  DevBuf<double> d_Pq;  // FP64 path: the state's primitives [5][nc] (k_prims)
   DevBuf<float> d_Uf;
   DevBuf<char> d_rec, d_FA;
   // mixed path

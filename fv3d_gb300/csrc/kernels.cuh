@@ -58,6 +58,7 @@ struct KArgs {
   const double* __restrict__ vol;  // [nc]
   const double* __restrict__ dx;   // [nc][3]
   double* U;                       // [5][nc] conserved state (FP64)
+  double* Pq;                      // [5][nc] its primitives u, v, w, p, T (FP64 path: k_prims)
   double* K;                       // [5][nc] low-storage RK register
   double* U0;                      // [5][nc] SSP-RK3 stage-0 state
   float* Uf;                       // [nc][8] FP32 shadow (rho, m, E, p, T, 1/rho)
@@ -102,6 +103,40 @@ __device__ __forceinline__ void load_geo(const R* __restrict__ g, int f, R* o, i
 }
 
 // ---------------------------------------------------------------------------
+// K0 (FP64 path): every cell's primitives (u, v, w, p, T) of the state, once
+// per residual, so that the gradient pass reads a neighbour's instead of
+// recomputing them per face (four FP64 divisions each, at GB300's FP64
+// rate); the same cons_to_prims arithmetic, so the same values
+// ---------------------------------------------------------------------------
+template <class R>
+__global__ void __launch_bounds__(256) k_prims(const __grid_constant__ KArgs<R> a) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= a.nc) return;
+  Phys<R> ph;
+  ph.load(a.pc);
+  R q[10];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) q[j] = a.U[(size_t)j * a.nc + c];
+  cons_to_prims(q, ph);
+#pragma unroll
+  for (int j = 0; j < 5; ++j) a.Pq[(size_t)j * a.nc + c] = q[VU + j];
+}
+
+// a cell's conserved state and primitives: from k_prims's output on the
+// FP64 path, else computed
+template <class R>
+__device__ __forceinline__ void load_state(const KArgs<R>& a, int c, R* q, const Phys<R>& ph) {
+  if constexpr (sizeof(R) == 8) {
+#pragma unroll
+    for (int j = 0; j < 5; ++j) q[j] = a.U[(size_t)j * a.nc + c];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) q[VU + j] = a.Pq[(size_t)j * a.nc + c];
+  } else {
+    State<R>::load(a, c, q, ph);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // K1: gradients + neighbour min/max
 // GMODE 0: no gradients (first order, inviscid); 1 Green-Gauss; 2 least squares
 // ---------------------------------------------------------------------------
@@ -112,7 +147,7 @@ __global__ void __launch_bounds__(256) k_gradients(const __grid_constant__ KArgs
   Phys<R> ph;
   ph.load(a.pc);
   R q[10];
-  State<R>::load(a, c, q, ph);
+  load_state(a, c, q, ph);
   R* out = a.rec + (size_t)c * REC;
   if (GMODE != 0) {
     Acc<R, KAHAN> g[NG][3];
@@ -130,7 +165,7 @@ __global__ void __launch_bounds__(256) k_gradients(const __grid_constant__ KArgs
         ghost_state(q, a.fregion[f - a.nf_int], &go[G_N], &go[G_T1], &go[G_T2], a.pc, ph, qo);
       } else {
         const int o = side ? a.fc0[f] : a.fc1[f];
-        State<R>::load(a, o, qo, ph);
+        load_state(a, o, qo, ph);
       }
       if (GMODE == 1) {
         const R lamf = a.lam[f];

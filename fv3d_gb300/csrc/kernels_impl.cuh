@@ -22,6 +22,7 @@ cudaError_t launch_gradients(const KArgs<R>& a, const Disc& d, cudaStream_t s) {
   constexpr bool K = sizeof(R) == 4;
   const int T = sizeof(R) == 8 ? FV3D_F64_THREADS : 256, B = blocks_for(a.nc, T);
   const bool lim = d.linear && d.limit;
+  if (sizeof(R) == 8) k_prims<R><<<B, T, 0, s>>>(a);
   if (d.gmode == 0) k_gradients<R, 0, false, K><<<B, T, 0, s>>>(a);
   else if (d.gmode == 1) {
     if (lim) k_gradients<R, 1, true, K><<<B, T, 0, s>>>(a);

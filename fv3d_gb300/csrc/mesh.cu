@@ -362,6 +362,7 @@ fv3d_status ensure_fp64_path(Ctx& ctx) {
   ALLOC(ctx.d_U0, (size_t)nc * 5);
   ALLOC(ctx.d_FA, (size_t)nf * FAS * sizeof(double));
   ALLOC(ctx.d_rec, (size_t)nc * REC * sizeof(double));
+  ALLOC(ctx.d_Pq, (size_t)nc * 5);
   return FV3D_OK;
 }
 

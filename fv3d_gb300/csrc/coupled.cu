@@ -133,24 +133,19 @@ __device__ __forceinline__ void put_state(float* __restrict__ rec, const double*
 }
 
 // What P_A's matrix-free product reads, per Newton step: each cell's FP32
-// state record and 1/dt, each slot's (normal, s A / V), and at each boundary
-// face the ghost's record and d ghost / d U_cell (forward differences of
-// update_boundaries, boundary.c:188-320, in FP64)
+// state record and 1/dt and each slot's (normal, s A / V); the boundary
+// faces' ghost records and derivatives come from k_cpl_build_bnd
 template <int MCF>
 __global__ void __launch_bounds__(128) k_cpl_build_state(KArgs<double> a, const double* __restrict__ dtl,
                                                          float* __restrict__ cst, float* __restrict__ idt,
-                                                         float4* __restrict__ pna, float* __restrict__ gst,
-                                                         float* __restrict__ gjac) {
+                                                         float4* __restrict__ pna) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= a.nc) return;
   const size_t nc = a.nc;
-  Phys<double> ph;
-  ph.load(a.pc);
-  double qc[10];
+  double qc[5];
 #pragma unroll
   for (int j = 0; j < 5; ++j) qc[j] = a.U[(size_t)j * nc + c];
   put_state(cst + 8 * (size_t)c, qc, a.pc.kappa, a.pc.km1);
-  cons_to_prims(qc, ph);
   idt[c] = (float)(1.0 / dtl[c]);
   const double iv = 1.0 / a.vol[c];
   for (int k = 0; k < MCF; ++k) {
@@ -162,22 +157,6 @@ __global__ void __launch_bounds__(128) k_cpl_build_state(KArgs<double> a, const 
     // the sign of s A / V carries the side (A / V > 0)
     pna[sk] = make_float4((float)g[G_N], (float)g[G_N + 1], (float)g[G_N + 2],
                           (float)((side ? -1.0 : 1.0) * g[G_A] * iv));
-    if (f < a.nf_int) continue;
-    const int b = f - a.nf_int, region = a.fregion[b];
-    double qg[10];
-    ghost_state(qc, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qg);
-    put_state(gst + 8 * (size_t)b, qg, a.pc.kappa, a.pc.km1);
-    for (int v = 0; v < 5; ++v) {
-      const double h = 1e-7 * fmax(fabs(qc[v]), 1e-3);
-      double qp[10], qh[10];
-#pragma unroll
-      for (int j = 0; j < 5; ++j) qp[j] = qc[j];
-      qp[v] += h;
-      cons_to_prims(qp, ph);
-      ghost_state(qp, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qh);
-#pragma unroll
-      for (int i = 0; i < 5; ++i) gjac[25 * (size_t)b + i * 5 + v] = (float)((qh[i] - qg[i]) / h);
-    }
   }
 }
 
@@ -330,13 +309,14 @@ __device__ __forceinline__ void rus_jx(const float4 st, float gm1, const float4 
   y[4] = st.w * q + un * (dp + x[4]);
 }
 
-// P_R's diagonal block of each boundary face per unit weight (s A / V):
-// (A(U_c) + lam I) / 2 + (A(U_g) - lam I) / 2 . d ghost / d U_c, the ghost's
-// dependence on its cell by forward differences of update_boundaries
-// (boundary.c:188-320) in FP64, row-major [nb][25].  Apart from the cell
-// pass so that the boundary arithmetic does not set that pass's register
-// budget.
-__global__ void __launch_bounds__(128) k_cpl_build_bnd(KArgs<double> a, double* __restrict__ bpr) {
+// Per boundary face: the ghost's FP32 record and G = d ghost / d U_c (FP64
+// forward differences of update_boundaries, boundary.c:188-320, stored
+// FP32) for P_A's product, and P_R's diagonal block per unit weight (s A /
+// V), (A(U_c) + lam I) / 2 + (A(U_g) - lam I) / 2 . G, row-major [nb][25]
+// FP64.  Apart from the cell passes so that the boundary arithmetic does
+// not set their register budgets.
+__global__ void __launch_bounds__(128) k_cpl_build_bnd(KArgs<double> a, float* __restrict__ gst,
+                                                       float* __restrict__ gjac, double* __restrict__ bpr) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   if (b >= a.nf - a.nf_int) return;
   const int f = a.nf_int + b, c = a.fc0[f];  // a boundary face's cell is its cell 0
@@ -356,6 +336,7 @@ __global__ void __launch_bounds__(128) k_cpl_build_bnd(KArgs<double> a, double* 
   const int region = a.fregion[b];
   double qg[10], Ag[25], lg;
   ghost_state(qc, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qg);
+  put_state(gst + 8 * (size_t)b, qg, kappa, a.pc.km1);
   euler_jacobian(qg, n, kappa, Ag, &lg);
   const double lam = fmax(lc, lg) + 2.0 * a.pc.mu / (qc[0] * n[3]);
   double* out = bpr + 25 * (size_t)b;
@@ -369,7 +350,10 @@ __global__ void __launch_bounds__(128) k_cpl_build_bnd(KArgs<double> a, double* 
     cons_to_prims(qp, ph);
     ghost_state(qp, region, &g[G_N], &g[G_T1], &g[G_T2], a.pc, ph, qh);
 #pragma unroll
-    for (int i = 0; i < 5; ++i) G[i] = (qh[i] - qg[i]) / h;
+    for (int i = 0; i < 5; ++i) {
+      G[i] = (qh[i] - qg[i]) / h;
+      gjac[25 * (size_t)b + i * 5 + v] = (float)G[i];
+    }
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
       double s = 0.5 * (Ac[i * 5 + v] + (i == v ? lam : 0.0));
@@ -798,9 +782,9 @@ fv3d_status Coupled::setup(Ctx& ctx, Implicit& im, int m_inner, int n_sweeps, fl
 fv3d_status Coupled::build(Ctx& ctx, Implicit& im) {
   KArgs<double> a = ctx.args<double>();
   const int g = nblk(nc, 128);
-  if (nb > 0) k_cpl_build_bnd<<<nblk(nb, 128), 128, 0, ctx.stream>>>(a, bpr.p);
+  if (nb > 0) k_cpl_build_bnd<<<nblk(nb, 128), 128, 0, ctx.stream>>>(a, gst.p, gjac.p, bpr.p);
 #define CPL_BUILD(M)                                                                           \
-  k_cpl_build_state<M><<<g, 128, 0, ctx.stream>>>(a, im.dtl.p, cst.p, idt.p, pna.p, gst.p, gjac.p); \
+  k_cpl_build_state<M><<<g, 128, 0, ctx.stream>>>(a, im.dtl.p, cst.p, idt.p, pna.p);             \
   k_cpl_build_pr<M><<<g, 128, 0, ctx.stream>>>(a, im.dtl.p, bpr.p, PRi.p, rna.p, rb.p, st4.p)
   if (mcf == 4) { CPL_BUILD(4); }
   else if (mcf == 6) { CPL_BUILD(6); }

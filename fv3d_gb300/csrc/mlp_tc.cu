@@ -164,10 +164,12 @@ constexpr size_t kTcWeightBytes = offsetof(TcSmem, bar) - offsetof(TcSmem, W0);
 static_assert(kTcWeightOff % 16 == 0 && kTcWeightBytes % 16 == 0, "bulk copies move 16-byte multiples");
 
 // the 8 BF16 of K-group j of this thread's row into the A tile
+// (pairs rounded to nearest by one conversion each: the same values as one
+// at a time)
 __device__ __forceinline__ void put_group(TcSmem& S, int row, int j, const float* x) {
-  __align__(16) bf16 h[8];
+  __align__(16) __nv_bfloat162 h[4];
 #pragma unroll
-  for (int l = 0; l < 8; ++l) h[l] = __float2bfloat16(x[l]);
+  for (int l = 0; l < 4; ++l) h[l] = __floats2bfloat162_rn(x[2 * l], x[2 * l + 1]);
   *reinterpret_cast<uint4*>(reinterpret_cast<unsigned char*>(S.A) + core_off(row, 8 * j, kKG)) =
       *reinterpret_cast<const uint4*>(h);
 }

@@ -58,10 +58,16 @@ __global__ void k_import(int nc, const int* __restrict__ perm, const double* __r
 // host link into shared memory, then scatters them into the renumbered device
 // arrays (the host buffer must be 16-byte aligned; checked by the caller)
 constexpr int kIoRows = 128;
+// With conv_bits set (mixed path), the kernel also takes the state's
+// convective time-step bound, min V / sum_d (|u_d| + c) dx_d, from the FP32
+// records it writes - k_timestep_f32's arithmetic, so the same bound - while
+// the host link sets its pace.
 __global__ void __launch_bounds__(kIoRows) k_import_host(int nc, const int* __restrict__ iperm,
                                                          const double* __restrict__ in, double* __restrict__ U,
                                                          float* __restrict__ Uf, float* __restrict__ UfN,
-                                                         double km1, double R) {
+                                                         double km1, double R, const double* __restrict__ vol,
+                                                         const double* __restrict__ dx, float kappa,
+                                                         unsigned long long* conv_bits) {
   __shared__ __align__(16) double sm[kIoRows * 5];
   const size_t i0 = (size_t)blockIdx.x * kIoRows;
   const int cnt = (int)min((size_t)kIoRows, (size_t)nc - i0);
@@ -70,22 +76,39 @@ __global__ void __launch_bounds__(kIoRows) k_import_host(int nc, const int* __re
   for (int k = threadIdx.x; k < nd / 2; k += kIoRows) reinterpret_cast<double2*>(sm)[k] = src[k];
   if ((nd & 1) && threadIdx.x == 0) sm[nd - 1] = in[5 * i0 + nd - 1];
   __syncthreads();
-  if ((int)threadIdx.x >= cnt) return;
-  const int c = iperm[i0 + threadIdx.x];
-  double u[5];
+  unsigned long long bc = 0x7ff0000000000000ull;
+  if ((int)threadIdx.x < cnt) {
+    const int c = iperm[i0 + threadIdx.x];
+    double u[5];
 #pragma unroll
-  for (int j = 0; j < 5; ++j) { u[j] = sm[5 * threadIdx.x + j]; U[(size_t)j * nc + c] = u[j]; }
-  if (Uf != nullptr) {
-    float rho = (float)u[0], mx = (float)u[1], my = (float)u[2], mz = (float)u[3];
-    float ke = 0.5f * (mx * (mx / rho) + my * (my / rho) + mz * (mz / rho));
-    float p = fmaxf(1.00E-10f, (float)(km1 * (u[4] - (double)ke)));
-    float T = p / (rho * (float)R);
-    float4* d = reinterpret_cast<float4*>(Uf) + 2 * (size_t)c;
-    d[0] = make_float4(rho, mx, my, mz);
-    d[1] = make_float4((float)u[4], p, T, 1.0f / rho);
-    float4* b = reinterpret_cast<float4*>(UfN) + 2 * (size_t)c;
-    b[0] = d[0];
-    b[1] = d[1];
+    for (int j = 0; j < 5; ++j) { u[j] = sm[5 * threadIdx.x + j]; U[(size_t)j * nc + c] = u[j]; }
+    if (Uf != nullptr) {
+      float rho = (float)u[0], mx = (float)u[1], my = (float)u[2], mz = (float)u[3];
+      float ke = 0.5f * (mx * (mx / rho) + my * (my / rho) + mz * (mz / rho));
+      float p = fmaxf(1.00E-10f, (float)(km1 * (u[4] - (double)ke)));
+      float T = p / (rho * (float)R);
+      float4* d = reinterpret_cast<float4*>(Uf) + 2 * (size_t)c;
+      d[0] = make_float4(rho, mx, my, mz);
+      d[1] = make_float4((float)u[4], p, T, 1.0f / rho);
+      float4* b = reinterpret_cast<float4*>(UfN) + 2 * (size_t)c;
+      b[0] = d[0];
+      b[1] = d[1];
+      if (conv_bits != nullptr) {
+        const float ir = 1.f / rho;
+        const float uu = mx * ir, vv = my * ir, ww = mz * ir;
+        const float cs = sqrtf(kappa * p * ir);
+        const double* dc = dx + 3 * (size_t)c;
+        const float ds = (fabsf(uu) + cs) * (float)dc[0] + (fabsf(vv) + cs) * (float)dc[1] +
+                         (fabsf(ww) + cs) * (float)dc[2];
+        const double lc = (double)((float)vol[c] / ds);
+        if (lc > 0.0) bc = (unsigned long long)__double_as_longlong(lc);
+        if (!(lc == lc)) bc = 0x7ff8000000000000ull;
+      }
+    }
+  }
+  if (conv_bits != nullptr) {
+    bc = warp_min_u64(bc);
+    if ((threadIdx.x & 31) == 0) atomicMin(conv_bits, bc);
   }
 }
 
@@ -547,16 +570,22 @@ static const double* pinned_device_view(const double* p) {
   return static_cast<const double*>(at.devicePointer);
 }
 
-extern "C" fv3d_status fv3d_set_state(fv3d_ctx* handle, const double* u) {
-  if (handle == nullptr || u == nullptr) return FV3D_ERR_INVALID_ARG;
-  Ctx* ctx = reinterpret_cast<Ctx*>(handle);
+// the state from the caller's rows; with want_bound (mixed path, pinned
+// rows) the import kernel also reduces the initial time-step bound into
+// d_bits and *bound_done says so
+static fv3d_status set_state_rows(Ctx* ctx, const double* u, bool want_bound, bool* bound_done) {
+  if (bound_done != nullptr) *bound_done = false;
   if (!ctx->mesh_ready) return ctx->fail(FV3D_ERR_STATE, "no mesh loaded");
   CK(cudaSetDevice(ctx->cfg.device));
   const double* hdev = pinned_device_view(u);
   if (hdev != nullptr) {
     // pinned caller memory: one kernel reads it over the host link
+    const bool bound = want_bound && !ctx->fp64() && ctx->d_Uf.p != nullptr;
+    if (bound) CK(cudaMemsetAsync(ctx->d_bits.p, 0xff, 2 * sizeof(unsigned long long), ctx->stream));
     k_import_host<<<(ctx->nc + kIoRows - 1) / kIoRows, kIoRows, 0, ctx->stream>>>(
-        ctx->nc, ctx->d_iperm.p, hdev, ctx->d_U.p, ctx->d_Uf.p, ctx->d_UfN.p, ctx->phys.km1, ctx->cfg.R_mix);
+        ctx->nc, ctx->d_iperm.p, hdev, ctx->d_U.p, ctx->d_Uf.p, ctx->d_UfN.p, ctx->phys.km1, ctx->cfg.R_mix,
+        ctx->d_vol.p, ctx->d_dx.p, (float)ctx->cfg.kappa, bound ? ctx->d_bits.p : nullptr);
+    if (bound && bound_done != nullptr) *bound_done = true;
   } else {
     CK(cudaMemcpyAsync(ctx->d_stage.p, u, sizeof(double) * 5 * (size_t)ctx->nc, cudaMemcpyHostToDevice,
                        ctx->stream));
@@ -567,6 +596,11 @@ extern "C" fv3d_status fv3d_set_state(fv3d_ctx* handle, const double* u) {
   CK(cudaGetLastError());
   ctx->state_ready = true;
   return FV3D_OK;
+}
+
+extern "C" fv3d_status fv3d_set_state(fv3d_ctx* handle, const double* u) {
+  if (handle == nullptr || u == nullptr) return FV3D_ERR_INVALID_ARG;
+  return set_state_rows(reinterpret_cast<Ctx*>(handle), u, false, nullptr);
 }
 
 static fv3d_status export_soa(Ctx* ctx, const double* src, int m, int with_prims, double* out) {
@@ -778,7 +812,8 @@ static fv3d_status step_graph(Ctx* ctx, int scheme, double cfl, bool store_r, cu
 
 // n_steps explicit steps enqueued on the context stream (no synchronisation);
 // the caller reads the device scalars afterwards (finish_explicit)
-static fv3d_status enqueue_explicit(Ctx* ctx, int scheme, int n_steps, double cfl, double dt_fixed) {
+static fv3d_status enqueue_explicit(Ctx* ctx, int scheme, int n_steps, double cfl, double dt_fixed,
+                                   bool bound_ready = false) {
   REQUIRE(scheme >= 0 && scheme <= 3, FV3D_ERR_INVALID_ARG, "bad explicit scheme %d", scheme);
   REQUIRE(n_steps >= 0, FV3D_ERR_INVALID_ARG, "negative step count");
   REQUIRE(cfl > 0.0 || dt_fixed > 0.0, FV3D_ERR_INVALID_ARG, "need cfl > 0 or dt_fixed > 0");
@@ -787,7 +822,7 @@ static fv3d_status enqueue_explicit(Ctx* ctx, int scheme, int n_steps, double cf
   if (!ctx->state_ready) return ctx->fail(FV3D_ERR_STATE, "no state set");
   // initial dt from the current state (timedisc.c:163-165 at the first step)
   CK(cudaMemsetAsync(ctx->d_sc.p, 0, sizeof(DevScalars), ctx->stream));
-  if (cfl > 0.0) {
+  if (cfl > 0.0 && !bound_ready) {
     st = reduce_step_bound(ctx);
     if (st != FV3D_OK) return st;
   }
@@ -839,9 +874,11 @@ extern "C" fv3d_status fv3d_step_explicit_io(fv3d_ctx* handle, int scheme, int n
   if (handle == nullptr) return FV3D_ERR_INVALID_ARG;
   Ctx* ctx = reinterpret_cast<Ctx*>(handle);
   fv3d_status st;
-  if (u_in != nullptr && (st = fv3d_set_state(handle, u_in)) != FV3D_OK) return st;
+  // the initial time-step bound is taken by the import kernel where it can
+  bool bound = false;
+  if (u_in != nullptr && (st = set_state_rows(ctx, u_in, cfl > 0.0, &bound)) != FV3D_OK) return st;
   CK(cudaSetDevice(ctx->cfg.device));
-  if ((st = enqueue_explicit(ctx, scheme, n_steps, cfl, dt_fixed)) != FV3D_OK) return st;
+  if ((st = enqueue_explicit(ctx, scheme, n_steps, cfl, dt_fixed, bound)) != FV3D_OK) return st;
   // scalars into page-locked memory (asynchronous), then the export, which
   // synchronises the stream once for both
   CK(cudaMemcpyAsync(ctx->h_sc, ctx->d_sc.p, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream));

@@ -96,11 +96,27 @@ template <> struct State<float> {
   }
 };
 
-template <class R>
-__device__ __forceinline__ void load_geo(const R* __restrict__ g, int f, R* o, int n) {
+// N consecutive elements from p into o; FP64 rows that start on a 16-byte
+// boundary (the face geometry, the per-cell records) by 16-byte loads
+#ifndef FV3D_F64_VEC
+#define FV3D_F64_VEC 1
+#endif
+template <int N, class R>
+__device__ __forceinline__ void load_row(const R* __restrict__ p, R* o) {
+  if constexpr (sizeof(R) == 8 && N % 2 == 0 && FV3D_F64_VEC) {
+    const double2* q = reinterpret_cast<const double2*>(p);
 #pragma unroll
-  for (int j = 0; j < n; ++j) o[j] = g[(size_t)f * GEO + j];
+    for (int j = 0; j < N / 2; ++j) {
+      const double2 v = __ldg(q + j);
+      o[2 * j] = v.x;
+      o[2 * j + 1] = v.y;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < N; ++j) o[j] = p[j];
+  }
 }
+
 
 // ---------------------------------------------------------------------------
 // K0 (FP64 path): every cell's primitives (u, v, w, p, T) of the state, once
@@ -159,7 +175,7 @@ __global__ void __launch_bounds__(256) k_gradients(const __grid_constant__ KArgs
       if (e < 0) break;
       const int f = e >> 1, side = e & 1;
       R go[10];
-      load_geo(a.geo, f, go, 10);
+      load_row<10>(a.geo + (size_t)f * GEO, go);
       R qo[10];
       if (f >= a.nf_int) {
         ghost_state(q, a.fregion[f - a.nf_int], &go[G_N], &go[G_T1], &go[G_T2], a.pc, ph, qo);
@@ -256,17 +272,13 @@ __global__ void __launch_bounds__(256) k_face_flux(const __grid_constant__ KArgs
   Phys<R> ph;
   ph.load(a.pc);
   R go[GEO];
-  load_geo(a.geo, f, go, GEO);
+  load_row<GEO>(a.geo + (size_t)f * GEO, go);
   const R* n = &go[G_N];
   const R* t1 = &go[G_T1];
   const R* t2 = &go[G_T2];
   const int c0 = a.fc0[f];
   R rl[REC];
-  {
-    const R* src = a.rec + (size_t)c0 * REC;
-#pragma unroll
-    for (int j = 0; j < REC; ++j) rl[j] = src[j];
-  }
+  load_row<REC>(a.rec + (size_t)c0 * REC, rl);
   R ql[10], qr[10];
   R gml[12], gmr[12];   // gradients of rho_u, rho_v, rho_w, T for the viscous flux
   reconstruct<R, LINEAR, LIMIT>(rl, &go[G_D1], ql);
@@ -300,9 +312,7 @@ __global__ void __launch_bounds__(256) k_face_flux(const __grid_constant__ KArgs
   } else {
     const int c1 = a.fc1[f];
     R rr[REC];
-    const R* src = a.rec + (size_t)c1 * REC;
-#pragma unroll
-    for (int j = 0; j < REC; ++j) rr[j] = src[j];
+    load_row<REC>(a.rec + (size_t)c1 * REC, rr);
     reconstruct<R, LINEAR, LIMIT>(rr, &go[G_D2], qr);
     if (VISCOUS) {
 #pragma unroll

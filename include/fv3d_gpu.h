@@ -225,7 +225,8 @@ typedef struct fv3d_implicit_opts {
                               coefficients); 2: J v from the FP32 residual, FP64 basis,
                               Gram-Schmidt and Givens rotations */
     int preconditioner;    /* FV3D_PC_* */
-    int pc_refresh;        /* rebuild the blocks every pc_refresh Newton steps */
+    int pc_refresh;        /* rebuild the preconditioner every pc_refresh Newton steps (and after a
+                              CFL back-off); 0: 3 for FV3D_PC_COUPLED, 1 for the others */
     int max_restarts;      /* FGMRES restarts per Newton step (0: one cycle) */
     int sync_every;        /* Arnoldi steps launched between host synchronisations (10; 0 takes
                               10): the Givens rotations of a chunk run after it, so a cycle that

@@ -270,7 +270,7 @@ def implicit_channel(args, with_cpu=True):
     from fv3d_gb300 import api, cases
     c = cases.channel()
     runs = {}
-    plans = [("coupled", dict(inner_dim=10, inner_sweeps=2, inner_omega=0.7, sync_every=3,
+    plans = [("coupled", dict(inner_dim=10, inner_sweeps=2, inner_omega=0.7, sync_every=3, pc_refresh=3,
                               max_newton=args.max_newton)),
              ("none", dict(max_restarts=3, max_newton=args.max_newton)),
              ("block_jacobi", dict(max_newton=min(args.max_newton, 100)))]

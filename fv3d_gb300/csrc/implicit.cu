@@ -1002,7 +1002,9 @@ fv3d_status Implicit::fgmres_t(Ctx& ctx, T* Vt, T* Zt, T* wt, double rnorm, int*
     bool done = false;
     // chunks of Arnoldi steps run back to back on the device, their
     // coefficients processed after one synchronisation
-    const int chunk = opts.sync_every > 0 ? opts.sync_every : 10;
+    // 0: 3 Arnoldi steps a chunk with the coupled preconditioner (each step
+    // costs about 0.8 ms, so unused ones at the end of a cycle are dear), 10 otherwise
+    const int chunk = opts.sync_every > 0 ? opts.sync_every : (opts.preconditioner == FV3D_PC_COUPLED ? 3 : 10);
     for (int k1 = 0; k < m && !done;) {
       k1 = std::min(m, k + chunk);
       for (int j = k; j < k1; ++j) {
@@ -1347,7 +1349,7 @@ extern "C" fv3d_status fv3d_implicit_default_opts(fv3d_implicit_opts* o) {
   o->preconditioner = FV3D_PC_BLOCK_JACOBI;
   o->pc_refresh = 0;
   o->max_restarts = 0;
-  o->sync_every = 10;
+  o->sync_every = 0;
   o->inner_dim = 10;
   o->inner_sweeps = 2;
   o->inner_omega = 0.7;

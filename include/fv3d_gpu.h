@@ -228,9 +228,10 @@ typedef struct fv3d_implicit_opts {
     int pc_refresh;        /* rebuild the preconditioner every pc_refresh Newton steps (and after a
                               CFL back-off); 0: 3 for FV3D_PC_COUPLED, 1 for the others */
     int max_restarts;      /* FGMRES restarts per Newton step (0: one cycle) */
-    int sync_every;        /* Arnoldi steps launched between host synchronisations (10; 0 takes
-                              10): the Givens rotations of a chunk run after it, so a cycle that
-                              meets eta inside a chunk computes up to sync_every - 1 unused steps */
+    int sync_every;        /* Arnoldi steps launched between host synchronisations (0: 3 for
+                              FV3D_PC_COUPLED, 10 for the others): the Givens rotations of a chunk
+                              run after it, so a cycle that meets eta inside a chunk computes up
+                              to sync_every - 1 unused steps */
     int inner_dim;         /* FV3D_PC_COUPLED: inner GMRES iterations per application, 1..30 (10) */
     int inner_sweeps;      /* FV3D_PC_COUPLED: Rusanov block-Jacobi sweeps per inner
                               preconditioning, 1..8 (2) */

@@ -117,3 +117,16 @@ def test_header_is_c99_and_matches_the_bindings(lib, tmp_path):
         assert int(got[c]) == C.sizeof(cls), c
         for f in fields[c]:
             assert int(got[f"{c}.{f}"]) == getattr(cls, f).offset, f"{c}.{f}"
+
+
+def test_implicit_default_options(lib):
+    """fv3d_implicit_default_opts fills what the header documents; 0 for
+    pc_refresh and sync_every leaves them to the preconditioner (3 and 3 for
+    FV3D_PC_COUPLED, 1 and 10 for the others)."""
+    o = api.ImplicitOpts()
+    assert lib.fv3d_implicit_default_opts(C.byref(o)) == 0
+    assert (o.cfl_start, o.cfl_max, o.tol_rel, o.max_newton, o.krylov_dim) == (100.0, 1e4, 1e-8, 500, 30)
+    assert (o.eta, o.fd_eps, o.jv_precision, o.preconditioner) == (1e-2, 1e-7, 1, 0)
+    assert (o.pc_refresh, o.max_restarts, o.sync_every) == (0, 0, 0)
+    assert (o.inner_dim, o.inner_sweeps, o.inner_omega, o.fallback) == (10, 2, 0.7, 0)
+    assert lib.fv3d_implicit_default_opts(None) == 1  # FV3D_ERR_INVALID_ARG

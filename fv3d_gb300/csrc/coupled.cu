@@ -508,7 +508,7 @@ __global__ void __launch_bounds__(256, 4) k_cpl_product(int nc, const float* __r
 }
 
 // the first damped sweep of P_R from zero for cell c: y = omega Dinv b
-// (k_cpl_sweep's arithmetic with x null)
+// (k_cpl_sweep's arithmetic at x = 0)
 __device__ __forceinline__ void first_sweep(const float* __restrict__ Di, int nc, int c, float omega,
                                             const float* b, float* __restrict__ y) {
   float r[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
@@ -581,10 +581,11 @@ __global__ void k_cpl_expand_pa(int nc, const float* __restrict__ cst, const flo
   }
 }
 
-// one damped block-Jacobi sweep of P_R, y = x + omega (Dinv (b - O x) - x)
-// (x null: y = omega Dinv b), the slot blocks O applied matrix-free.
-// Undamped sweeps overshoot on this operator (at CFL 1e4 the error after
-// four of them is about 1.4 times that after four with omega = 0.7)
+// one damped block-Jacobi sweep of P_R after the first, y = x + omega (Dinv
+// (b - O x) - x), the slot blocks O applied matrix-free (the first sweep,
+// from x = 0, is first_sweep in the pass that forms b).  Undamped sweeps
+// overshoot on this operator (at CFL 1e4 the error after four of them is
+// about 1.4 times that after four with omega = 0.7)
 template <int MCF, class TO>
 __global__ void __launch_bounds__(256) k_cpl_sweep(int nc, const float* __restrict__ Di, const int* __restrict__ nbr,
                                                    const float4* __restrict__ rna, const float* __restrict__ rb,
@@ -593,26 +594,23 @@ __global__ void __launch_bounds__(256) k_cpl_sweep(int nc, const float* __restri
                                                    TO* __restrict__ y) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= nc) return;
-  float t[5], r[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, xc[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  float t[5], r[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, xc[5];
   ld5(b, nc, c, t);
-  if (x != nullptr) {
-    ld5(x, nc, c, xc);
+  ld5(x, nc, c, xc);
 #pragma unroll
-    for (int k = 0; k < MCF; ++k) {
-      const size_t sk = (size_t)k * nc + c;
-      const int o = __ldg(nbr + sk);
-      if (o < 0) continue;
-      float xo[5], jx[5];
-      ld5(x, nc, o, xo);
-      const float4 na = __ldg(rna + sk);
-      const float bk = __ldg(rb + sk);
-      rus_jx(__ldg(st4 + o), gm1, na, xo, jx);
+  for (int k = 0; k < MCF; ++k) {
+    const size_t sk = (size_t)k * nc + c;
+    const int o = __ldg(nbr + sk);
+    if (o < 0) continue;
+    float xo[5], jx[5];
+    ld5(x, nc, o, xo);
+    const float4 na = __ldg(rna + sk);
+    const float bk = __ldg(rb + sk);
+    rus_jx(__ldg(st4 + o), gm1, na, xo, jx);
 #pragma unroll
-      for (int j = 0; j < 5; ++j) t[j] -= na.w * jx[j] + bk * xo[j];
-    }
+    for (int j = 0; j < 5; ++j) t[j] -= na.w * jx[j] + bk * xo[j];
   }
   block_mul_add(Di + c, nc, t, r);
-  // damped: y = x + omega (Dinv (b - O x) - x)
 #pragma unroll
   for (int j = 0; j < 5; ++j) y[(size_t)j * nc + c] = (TO)(xc[j] + omega * (r[j] - xc[j]));
 }

@@ -793,10 +793,10 @@ fv3d_status Implicit::gs_pass(Ctx& ctx, int pass, T* wv, const T* Vb, int k, con
   k_gs<KM, P, T><<<nb, 256, 0, ctx.stream>>>(n, ldb, wv, Vb, k, h_in, pt, ctr, dst, c, c_dev, jv, dst2, vout, \
                                              scale)
   if (pass == 0) GS_LAUNCH(1, 0);
-  else if (pass == 3) { if (k <= 8) GS_LAUNCH(8, 3); else if (k <= 16) GS_LAUNCH(16, 3); else GS_LAUNCH(32, 3); }
-  else if (pass == 1) { if (k <= 8) GS_LAUNCH(8, 1); else if (k <= 16) GS_LAUNCH(16, 1); else GS_LAUNCH(32, 1); }
-  else if (pass == 4) { if (k <= 8) GS_LAUNCH(8, 4); else if (k <= 16) GS_LAUNCH(16, 4); else GS_LAUNCH(32, 4); }
-  else { if (k <= 8) GS_LAUNCH(8, 2); else if (k <= 16) GS_LAUNCH(16, 2); else GS_LAUNCH(32, 2); }
+  else if (pass == 3) { if (k <= 8) GS_LAUNCH(8, 3); else if (k <= 12) GS_LAUNCH(12, 3); else if (k <= 16) GS_LAUNCH(16, 3); else GS_LAUNCH(32, 3); }
+  else if (pass == 1) { if (k <= 8) GS_LAUNCH(8, 1); else if (k <= 12) GS_LAUNCH(12, 1); else if (k <= 16) GS_LAUNCH(16, 1); else GS_LAUNCH(32, 1); }
+  else if (pass == 4) { if (k <= 8) GS_LAUNCH(8, 4); else if (k <= 12) GS_LAUNCH(12, 4); else if (k <= 16) GS_LAUNCH(16, 4); else GS_LAUNCH(32, 4); }
+  else { if (k <= 8) GS_LAUNCH(8, 2); else if (k <= 12) GS_LAUNCH(12, 2); else if (k <= 16) GS_LAUNCH(16, 2); else GS_LAUNCH(32, 2); }
 #undef GS_LAUNCH
   ICK(cudaGetLastError());
   return FV3D_OK;
